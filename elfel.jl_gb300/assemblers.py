@@ -1,0 +1,300 @@
+"""System matrix / vector assemblers backed by the GB300 library.
+
+``SysmatAssemblerSparse`` and ``SysvecAssembler`` keep the reference's API
+(Elfel.jl src/Assemblers.jl): ``start``/``assemble``/``finish``, with
+``finish`` returning a CSC matrix (scipy.sparse.csc_matrix, Int64 indices) /
+a dense vector.  Triplets are appended on the host as the reference does;
+``finish`` moves them to the device, where the CSC is built and duplicates
+are summed in append order (SparseArrays.sparse semantics).
+
+``SysmatAssemblerGPU`` is the fused form: the element loop of the user's
+``integrate!`` for heat, elasticity or Stokes runs on the device, the pattern
+is built once and kept, and K and F stay resident for ``solve``.
+"""
+import ctypes
+
+import numpy as np
+import scipy.sparse as sp
+
+from . import _native as N
+from .feiterators import FEIterator, QPIterator
+from .local_assemblers import LocalMatrixAssembler, LocalVectorAssembler, Transpose
+
+
+class _Handle:
+    def __init__(self, ctx):
+        self.ctx = ctx or N.default_context()
+        self.lib = self.ctx.lib
+        h = ctypes.c_void_p()
+        self.ctx.check(self.lib.elfel_sysmat_create(self.ctx.h, ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.elfel_sysmat_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, rc):
+        self.ctx.check(rc)
+
+    def csc(self):
+        nr, nc, nnz = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        self.check(self.lib.elfel_sysmat_dims(self.h, ctypes.byref(nr), ctypes.byref(nc), ctypes.byref(nnz)))
+        colptr = np.empty(nc.value + 1, dtype=np.int64)
+        rowval = np.empty(max(nnz.value, 1), dtype=np.int64)
+        nzval = np.empty(max(nnz.value, 1), dtype=np.float64)
+        self.check(self.lib.elfel_sysmat_csc(self.h, N.ptr(colptr, N._i64p), N.ptr(rowval, N._i64p), N.ptr(nzval)))
+        k = nnz.value
+        # 1-based SparseMatrixCSC arrays -> 0-based scipy CSC (indices kept Int64)
+        return sp.csc_matrix((nzval[:k], rowval[:k] - 1, colptr - 1), shape=(nr.value, nc.value))
+
+
+class SysmatAssemblerSparse:
+    """Sparse system matrix assembler (src/Assemblers.jl:19-123), device CSC build."""
+
+    def __init__(self, zero=0.0, ctx=None):
+        self._ctx = ctx
+        self._hd = None
+        self.nrow = self.ncol = 0
+        self._chunks = []
+        self._scalar = ([], [], [])
+
+    def _flush_scalars(self):
+        r, c, v = self._scalar
+        if r:
+            self._chunks.append((np.array(r, dtype=np.int64), np.array(c, dtype=np.int64),
+                                 np.array(v, dtype=np.float64)))
+            self._scalar = ([], [], [])
+
+    def triplets(self):
+        """The appended (row, col, val) triplets, 1-based, in append order."""
+        self._flush_scalars()
+        if not self._chunks:
+            return (np.zeros(0, np.int64), np.zeros(0, np.int64), np.zeros(0))
+        return tuple(np.concatenate([ch[k] for ch in self._chunks]) for k in range(3))
+
+
+def start(a, nrow, ncol=None):
+    """start!(assembler, nrow, ncol) / start!(vector assembler, nrow)."""
+    if isinstance(a, SysmatAssemblerSparse):
+        a.nrow, a.ncol = int(nrow), int(ncol)
+        a._chunks = []
+        a._scalar = ([], [], [])
+        return a
+    if isinstance(a, SysvecAssembler):
+        a.ndofs = int(nrow)
+        a._rows, a._vals = [], []
+        return a
+    if isinstance(a, SysmatAssemblerGPU):
+        a.nrow, a.ncol = int(nrow), int(ncol)
+        return a
+    raise TypeError(type(a))
+
+
+def assemble(a, *args):
+    """assemble!(a, r, c, v) | assemble!(a, lma) | assemble!(a, transpose(lma)) |
+    assemble!(av, i, v) | assemble!(av, lva)   (src/Assemblers.jl:85-114, 205-221)."""
+    if isinstance(a, SysmatAssemblerSparse):
+        if len(args) == 3:
+            a._scalar[0].append(int(args[0]))
+            a._scalar[1].append(int(args[1]))
+            a._scalar[2].append(float(args[2]))
+            return a
+        lma = args[0]
+        a._flush_scalars()
+        if isinstance(lma, Transpose):
+            p = lma.parent  # parent entries row-major, row/col swapped (Assemblers.jl:109-114)
+            a._chunks.append((p.col.ravel(order="C").copy(), p.row.ravel(order="C").copy(),
+                              p.M.ravel(order="C").copy()))
+        elif isinstance(lma, LocalMatrixAssembler):
+            a._chunks.append((lma.row.ravel(order="F").copy(), lma.col.ravel(order="F").copy(),
+                              lma.M.ravel(order="F").copy()))
+        else:
+            raise TypeError(type(lma))
+        return a
+    if isinstance(a, SysvecAssembler):
+        if len(args) == 2:
+            a._rows.append(np.array([int(args[0])], dtype=np.int64))
+            a._vals.append(np.array([float(args[1])]))
+        else:
+            lva = args[0]
+            if not isinstance(lva, LocalVectorAssembler):
+                raise TypeError(type(lva))
+            a._rows.append(lva.row.copy())
+            a._vals.append(lva.V.copy())
+        return a
+    raise TypeError(type(a))
+
+
+def finish(a):
+    """finish!(a): CSC matrix (SysmatAssemblerSparse) or dense vector (SysvecAssembler)."""
+    if isinstance(a, SysmatAssemblerSparse):
+        I, J, V = a.triplets()
+        if a._hd is None:
+            a._hd = _Handle(a._ctx)
+        h = a._hd
+        h.check(h.lib.elfel_sysmat_start(h.h, a.nrow, a.ncol))
+        n = I.shape[0]
+        h.check(h.lib.elfel_sysmat_assemble_coo(h.h, N.ptr(I, N._i64p), N.ptr(J, N._i64p), N.ptr(V), n))
+        nnz = ctypes.c_int64()
+        h.check(h.lib.elfel_sysmat_finish(h.h, ctypes.byref(nnz)))
+        return h.csc()
+    if isinstance(a, SysvecAssembler):
+        ctx = a._ctx or N.default_context()
+        rows = np.concatenate(a._rows) if a._rows else np.zeros(0, np.int64)
+        vals = np.concatenate(a._vals) if a._vals else np.zeros(0)
+        out = np.zeros(a.ndofs)
+        ctx.check(ctx.lib.elfel_sysvec_assemble(ctx.h, a.ndofs, N.ptr(rows, N._i64p), N.ptr(vals), rows.shape[0],
+                                                N.ptr(out)))
+        return out
+    if isinstance(a, SysmatAssemblerGPU):
+        return a.csc()
+    raise TypeError(type(a))
+
+
+class SysvecAssembler:
+    """Dense system vector assembler (src/Assemblers.jl:170-230), device summation."""
+
+    def __init__(self, zero=0.0, ctx=None):
+        self._ctx = ctx
+        self.ndofs = 0
+        self._rows, self._vals = [], []
+
+
+# ---------------------------------------------------------------- fused form
+_SOLVERS = {"pcg64": N.ELFEL_PCG64, "pcg32_ir": N.ELFEL_PCG32_IR, "minres64": N.ELFEL_MINRES64,
+            "minres32_ir": N.ELFEL_MINRES32_IR}
+
+
+def _space_struct(elit: FEIterator, keep):
+    fesp = elit.fesp
+    mesh = fesp.mesh
+    conn = N.i64(mesh.conn)
+    xy = N.f64(mesh.xy)
+    dofs = N.i64(elit.eldofs_table())
+    keep.extend([conn, xy, dofs])
+    return N.Space(mesh.nodes_per_elem, fesp.nfecopies, mesh.nel, mesh.nnodes, N.ptr(conn, N._i64p), N.ptr(xy),
+                   N.ptr(dofs, N._i64p))
+
+
+class SysmatAssemblerGPU:
+    """Fused device assembler: the element loop runs on the GPU.
+
+    Usage mirrors the reference scripts::
+
+        am = start(SysmatAssemblerGPU(), ndofs(fesp), ndofs(fesp))
+        assemble_heat(am, FEIterator(fesp), QPIterator(fesp, {"npts": 3}), kappa, Q)
+        K = finish(am); F = am.rhs()
+        solve(T, am, None, nunknowns(fesp), method="pcg32_ir")
+    """
+
+    def __init__(self, ctx=None):
+        self._hd = _Handle(ctx)
+        self.nrow = self.ncol = 0
+        self._setup_key = None
+        self._keep = []
+        self.physics = None
+
+    @property
+    def ctx(self):
+        return self._hd.ctx
+
+    def setup(self, physics, elit, qpit, pelit=None, ndofs=None):
+        """Upload the mesh and DOF tables and build the pattern once."""
+        keep = []
+        u = _space_struct(elit, keep)
+        p = _space_struct(pelit, keep) if pelit is not None else N.Space()
+        qr = qpit.quadr
+        pc = N.f64(qr.param_coords)
+        w = N.f64(qr.weights)
+        keep.extend([pc, w])
+        n = int(ndofs if ndofs is not None else self.nrow)
+        d = N.FusedDesc(physics, qr.npts, N.ptr(pc), N.ptr(w), n, u, p)
+        self._hd.check(self._hd.lib.elfel_fused_setup(self._hd.h, ctypes.byref(d)))
+        self._keep = keep
+        self.physics = physics
+        self.nrow = self.ncol = n
+        self.nel = elit.fesp.mesh.nel
+        self._setup_key = (id(elit.fesp), id(pelit.fesp) if pelit is not None else None, qr.npts, physics, n)
+        return self
+
+    def _ensure(self, physics, elit, qpit, pelit=None):
+        key = (id(elit.fesp), id(pelit.fesp) if pelit is not None else None, qpit.quadr.npts, physics, self.nrow)
+        if key != self._setup_key:
+            self.setup(physics, elit, qpit, pelit)
+
+    def heat(self, kappa, Q):
+        """K and F of the heat weak form; kappa: scalar, per-element array, or None (resident)."""
+        if kappa is not None:
+            kappa = np.ascontiguousarray(np.broadcast_to(np.asarray(kappa, dtype=np.float64), (self.nel,)))
+        self._hd.check(self._hd.lib.elfel_fused_heat(self._hd.h, N.ptr(kappa), float(Q)))
+        return self
+
+    def elasticity(self, E, nu, plane_strain=True, bforce=None, trac_edges=None, traction=(0.0, 0.0)):
+        bf = N.f64(bforce) if bforce is not None else None
+        te = N.i64(trac_edges) if trac_edges is not None else None
+        tr = N.f64(traction)
+        nt = 0 if te is None else te.shape[0]
+        self._hd.check(self._hd.lib.elfel_fused_elasticity(self._hd.h, float(E), float(nu), int(bool(plane_strain)),
+                                                           N.ptr(bf), N.ptr(te, N._i64p), nt, N.ptr(tr)))
+        return self
+
+    def stokes(self, mu):
+        self._hd.check(self._hd.lib.elfel_fused_stokes(self._hd.h, float(mu)))
+        return self
+
+    def set_geometry(self, xy):
+        xy = N.f64(xy)
+        self._hd.check(self._hd.lib.elfel_fused_set_geometry(self._hd.h, N.ptr(xy)))
+
+    def csc(self):
+        return self._hd.csc()
+
+    def rhs(self):
+        F = np.zeros(self.nrow)
+        self._hd.check(self._hd.lib.elfel_sysmat_rhs(self._hd.h, N.ptr(F)))
+        return F
+
+    def solve(self, T, nu, F=None, method="pcg32_ir", rtol=1e-10, maxit=200000):
+        """solve!(T, K, F, nu) of test/test_heat.jl:73-76, on the device.  T is updated in place."""
+        st = N.SolveStats()
+        Fa = N.f64(F) if F is not None else None
+        if T.dtype != np.float64 or not T.flags.c_contiguous:
+            raise TypeError("T must be a contiguous float64 array")
+        rc = self._hd.lib.elfel_solve(self._hd.h, N.ptr(Fa), N.ptr(T), int(nu), _SOLVERS[method], float(rtol),
+                                      int(maxit), ctypes.byref(st))
+        stats = st.as_dict()
+        self._hd.check(rc)
+        return stats
+
+
+def assemble_heat(am, elit, qpit, kappa, Q):
+    """Fused integrate! of test/test_heat.jl:36-60: K and F on the device."""
+    am._ensure(N.ELFEL_HEAT, elit, qpit)
+    return am.heat(kappa, Q)
+
+
+def assemble_elasticity(am, elit, qpit, E, nu, plane_strain=True, bforce=None, trac_edges=None,
+                        traction=(0.0, 0.0)):
+    """Fused integrateK! of test/test_elasticity.jl:150-171 plus loads."""
+    am._ensure(N.ELFEL_ELASTICITY, elit, qpit)
+    return am.elasticity(E, nu, plane_strain, bforce, trac_edges, traction)
+
+
+def assemble_stokes(am, uelit, pelit, qpit, mu):
+    """Fused integrate! of test/test_stokes.jl:629-657 (vector Laplacian Taylor-Hood)."""
+    am._ensure(N.ELFEL_STOKES, uelit, qpit, pelit)
+    return am.stokes(mu)
+
+
+def solve(T, K, F, nu, method="pcg32_ir", rtol=1e-10, maxit=200000):
+    """solve!(T, K, F, nu): T[1:nu] = K[1:nu,1:nu] \\ (F - K*T)[1:nu] on the device."""
+    if not isinstance(K, SysmatAssemblerGPU):
+        raise TypeError("solve needs the device-resident system (SysmatAssemblerGPU)")
+    return K.solve(T, nu, F, method, rtol, maxit)

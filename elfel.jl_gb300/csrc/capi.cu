@@ -1,0 +1,552 @@
+// C ABI: SysmatAssemblerSparse (COO mode), SysvecAssembler, fused assembly.
+#include <math.h>
+
+#include "integrate.cuh"
+#include "solve.cuh"
+#include "sysmat.cuh"
+
+using namespace elfel;
+
+namespace elfel {
+
+// Dense vector from a 1 x n pattern: out[c] = sum of the contributions of column c.
+__global__ void reduce_row0_dense_k(const int64_t* __restrict__ colptr, const int32_t* __restrict__ cptr,
+                                    const int32_t* __restrict__ contrib, const double* __restrict__ store, int64_t n,
+                                    double* __restrict__ out) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k0 = colptr[c], k1 = colptr[c + 1];
+    double s = 0.0;
+    if (k1 > k0) {
+      const int32_t b = cptr[k0], e = cptr[k0 + 1];
+      s = store[contrib[b]];
+      for (int32_t t = b + 1; t < e; ++t) s += store[contrib[t]];
+    }
+    out[c] = s;
+  }
+}
+
+int reduce_dense(Ctx* c, const Pattern& P, const double* store, double* out) {
+  if (P.ncol == 0) return ELFEL_OK;
+  reduce_row0_dense_k<<<grid_for(P.ncol, 256, (int64_t)c->sm_count * 16), 256, 0, c->stream>>>(
+      P.colptr.p, P.cptr.p, P.contrib.p, store, P.ncol, out);
+  ELFEL_LAUNCH_CHECK(c);
+  return ELFEL_OK;
+}
+
+__global__ void csc_out_k(const int64_t* colptr, int64_t ncol, const int32_t* rowval, int64_t nnz, int64_t* colptr1,
+                          int64_t* rowval1) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i <= ncol || i < nnz;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    if (i <= ncol) colptr1[i] = colptr[i] + 1;
+    if (i < nnz) rowval1[i] = (int64_t)rowval[i] + 1;
+  }
+}
+
+__global__ void add_k(double* a, const double* b, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    a[i] += b[i];
+}
+
+// Edge DOF table of the traction edges: (edge node a, component) in order.
+__global__ void edge_dofs_k(int64_t ntrac, const int32_t* edges, const int32_t* dofs, int nn, int ncomp,
+                            int32_t* out) {
+  const int nen = nn == 6 ? 3 : 2;
+  const int nedof = nn * ncomp;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < ntrac; k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = edges[2 * k];
+    const int le = edges[2 * k + 1];
+    for (int a = 0; a < nen; ++a) {
+      const int ln = a == 0 ? le : (a == 1 ? (le + 1) % 3 : 3 + le);
+      for (int cc = 0; cc < ncomp; ++cc) out[k * nen * ncomp + a * ncomp + cc] = dofs[e * nedof + ln * ncomp + cc];
+    }
+  }
+}
+
+static int ensure_cap(Ctx* c, DBuf<int64_t>* b, size_t used, size_t need) {
+  if (need <= b->n) return ELFEL_OK;
+  size_t cap = b->n ? b->n : 1024;
+  while (cap < need) cap *= 2;
+  DBuf<int64_t> nb;
+  ELFEL_TRY(nb.alloc(c, cap));
+  if (used) ELFEL_CUDA(c, cudaMemcpyAsync(nb.p, b->p, used * sizeof(int64_t), cudaMemcpyDeviceToDevice, c->stream));
+  b->release(c);
+  *b = nb;
+  return ELFEL_OK;
+}
+static int ensure_cap(Ctx* c, DBuf<double>* b, size_t used, size_t need) {
+  if (need <= b->n) return ELFEL_OK;
+  size_t cap = b->n ? b->n : 1024;
+  while (cap < need) cap *= 2;
+  DBuf<double> nb;
+  ELFEL_TRY(nb.alloc(c, cap));
+  if (used) ELFEL_CUDA(c, cudaMemcpyAsync(nb.p, b->p, used * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  b->release(c);
+  *b = nb;
+  return ELFEL_OK;
+}
+
+__global__ void coo_index_k(const int64_t* src, int64_t n, int64_t limit, int32_t* dst, int* bad) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t v = src[i];
+    if (v < 1 || v > limit) {
+      atomicExch(bad, 1);
+      dst[i] = 0;
+    } else {
+      dst[i] = (int32_t)(v - 1);
+    }
+  }
+}
+
+}  // namespace elfel
+
+// COO staging buffers live with the sysmat (device).
+struct CooStage {
+  DBuf<int64_t> I, J;
+  DBuf<double> V;
+  int64_t n = 0;
+};
+
+static CooStage* stage_of(elfel_sysmat* m) {
+  static_assert(sizeof(CooStage) > 0, "");
+  return reinterpret_cast<CooStage*>(m->coo_stage);
+}
+
+#define CHECK_M(m)                          \
+  do {                                      \
+    if (!(m) || !(m)->h) return ELFEL_ERR_ARG; \
+  } while (0)
+
+extern "C" int elfel_sysmat_create(elfel_ctx* h, elfel_sysmat** out) {
+  if (!h || !out) return ELFEL_ERR_ARG;
+  elfel_sysmat* m = new elfel_sysmat();
+  m->h = h;
+  m->coo_stage = new CooStage();
+  *out = m;
+  return ELFEL_OK;
+}
+
+static void release_all(elfel_sysmat* m) {
+  Ctx* c = &m->h->c;
+  CooStage* s = stage_of(m);
+  s->I.release(c);
+  s->J.release(c);
+  s->V.release(c);
+  s->n = 0;
+  m->P.release(c);
+  m->vals.release(c);
+  m->rhs.release(c);
+  m->F.release(c);
+  solver_release(c, m);
+  m->has_rhs = 0;
+  m->fused = 0;
+  m->finished = 0;
+}
+
+extern "C" int elfel_sysmat_destroy(elfel_sysmat* m) {
+  if (!m) return ELFEL_OK;
+  if (m->h) {
+    cudaSetDevice(m->h->c.device);
+    release_all(m);
+    cudaStreamSynchronize(m->h->c.stream);
+  }
+  delete stage_of(m);
+  delete m;
+  return ELFEL_OK;
+}
+
+extern "C" int elfel_sysmat_start(elfel_sysmat* m, int64_t nrow, int64_t ncol) {
+  CHECK_M(m);
+  Ctx* c = &m->h->c;
+  if (nrow < 0 || ncol < 0) return fail(c, ELFEL_ERR_ARG, "start!: negative dimensions");
+  cudaSetDevice(c->device);
+  release_all(m);
+  m->nrow = nrow;
+  m->ncol = ncol;
+  m->started = 1;
+  return ELFEL_OK;
+}
+
+extern "C" int elfel_sysmat_assemble_coo(elfel_sysmat* m, const int64_t* rows, const int64_t* cols,
+                                         const double* vals, int64_t n) {
+  CHECK_M(m);
+  Ctx* c = &m->h->c;
+  if (!m->started || m->fused) return fail(c, ELFEL_ERR_STATE, "assemble!: call start! first (COO mode)");
+  if (n < 0 || (n > 0 && (!rows || !cols || !vals))) return fail(c, ELFEL_ERR_ARG, "assemble!: bad arrays");
+  if (n == 0) return ELFEL_OK;
+  cudaSetDevice(c->device);
+  CooStage* s = stage_of(m);
+  ELFEL_TRY(ensure_cap(c, &s->I, (size_t)s->n, (size_t)(s->n + n)));
+  ELFEL_TRY(ensure_cap(c, &s->J, (size_t)s->n, (size_t)(s->n + n)));
+  ELFEL_TRY(ensure_cap(c, &s->V, (size_t)s->n, (size_t)(s->n + n)));
+  ELFEL_CUDA(c, cudaMemcpyAsync(s->I.p + s->n, rows, sizeof(int64_t) * n, cudaMemcpyHostToDevice, c->stream));
+  ELFEL_CUDA(c, cudaMemcpyAsync(s->J.p + s->n, cols, sizeof(int64_t) * n, cudaMemcpyHostToDevice, c->stream));
+  ELFEL_CUDA(c, cudaMemcpyAsync(s->V.p + s->n, vals, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+  s->n += n;
+  m->finished = 0;
+  return ELFEL_OK;
+}
+
+extern "C" int elfel_sysmat_finish(elfel_sysmat* m, int64_t* nnz) {
+  CHECK_M(m);
+  Ctx* c = &m->h->c;
+  if (!m->started) return fail(c, ELFEL_ERR_STATE, "finish!: call start! first");
+  cudaSetDevice(c->device);
+  if (!m->fused) {
+    CooStage* s = stage_of(m);
+    const int64_t n = s->n;
+    DBuf<int32_t> I, J;
+    DBuf<int> bad;
+    ELFEL_TRY(I.alloc(c, (size_t)(n > 0 ? n : 1)));
+    ELFEL_TRY(J.alloc(c, (size_t)(n > 0 ? n : 1)));
+    ELFEL_TRY(bad.alloc(c, 1));
+    ELFEL_CUDA(c, cudaMemsetAsync(bad.p, 0, sizeof(int), c->stream));
+    if (n > 0) {
+      const unsigned g = grid_for(n, 256, (int64_t)c->sm_count * 16);
+      coo_index_k<<<g, 256, 0, c->stream>>>(s->I.p, n, m->nrow, I.p, bad.p);
+      coo_index_k<<<g, 256, 0, c->stream>>>(s->J.p, n, m->ncol, J.p, bad.p);
+      ELFEL_LAUNCH_CHECK(c);
+    }
+    int hbad = 0;
+    ELFEL_CUDA(c, cudaMemcpyAsync(&hbad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+    bad.release(c);
+    if (hbad) {
+      I.release(c);
+      J.release(c);
+      return fail(c, ELFEL_ERR_ARG, "assemble!: row/column number outside 1..%lld / 1..%lld", (long long)m->nrow,
+                  (long long)m->ncol);
+    }
+    SlotGen g;
+    g.I = I.p;
+    g.J = J.p;
+    g.ncoo = n;
+    ELFEL_TRY(build_pattern(c, g, m->nrow, m->ncol, &m->P));
+    I.release(c);
+    J.release(c);
+    ELFEL_TRY(m->vals.alloc(c, (size_t)(m->P.nnz > 0 ? m->P.nnz : 1)));
+    ELFEL_TRY(reduce_values(c, m->P, s->V.p, m->vals.p));
+    ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+    m->values_version++;
+  }
+  m->finished = 1;
+  if (nnz) *nnz = m->P.nnz;
+  return ELFEL_OK;
+}
+
+extern "C" int elfel_sysmat_dims(const elfel_sysmat* m, int64_t* nrow, int64_t* ncol, int64_t* nnz) {
+  if (!m) return ELFEL_ERR_ARG;
+  if (nrow) *nrow = m->nrow;
+  if (ncol) *ncol = m->ncol;
+  if (nnz) *nnz = m->P.nnz;
+  return ELFEL_OK;
+}
+
+extern "C" int elfel_sysmat_csc(elfel_sysmat* m, int64_t* colptr, int64_t* rowval, double* nzval) {
+  CHECK_M(m);
+  Ctx* c = &m->h->c;
+  if (!m->finished) return fail(c, ELFEL_ERR_STATE, "csc: call finish! first");
+  cudaSetDevice(c->device);
+  const int64_t nnz = m->P.nnz, ncol = m->P.ncol;
+  DBuf<int64_t> cp, rv;
+  ELFEL_TRY(cp.alloc(c, (size_t)ncol + 1));
+  ELFEL_TRY(rv.alloc(c, (size_t)(nnz > 0 ? nnz : 1)));
+  csc_out_k<<<grid_for(nnz > ncol + 1 ? nnz : ncol + 1, 256, (int64_t)c->sm_count * 16), 256, 0, c->stream>>>(
+      m->P.colptr.p, ncol, m->P.rowval.p, nnz, cp.p, rv.p);
+  ELFEL_LAUNCH_CHECK(c);
+  if (colptr) ELFEL_CUDA(c, cudaMemcpyAsync(colptr, cp.p, sizeof(int64_t) * (ncol + 1), cudaMemcpyDeviceToHost, c->stream));
+  if (rowval && nnz)
+    ELFEL_CUDA(c, cudaMemcpyAsync(rowval, rv.p, sizeof(int64_t) * nnz, cudaMemcpyDeviceToHost, c->stream));
+  if (nzval && nnz)
+    ELFEL_CUDA(c, cudaMemcpyAsync(nzval, m->vals.p, sizeof(double) * nnz, cudaMemcpyDeviceToHost, c->stream));
+  cp.release(c);
+  rv.release(c);
+  ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+  return ELFEL_OK;
+}
+
+extern "C" int elfel_sysmat_rhs(elfel_sysmat* m, double* F) {
+  CHECK_M(m);
+  Ctx* c = &m->h->c;
+  if (!m->has_rhs) return fail(c, ELFEL_ERR_STATE, "rhs: no fused assembly has run");
+  cudaSetDevice(c->device);
+  if (F && m->nrow)
+    ELFEL_CUDA(c, cudaMemcpyAsync(F, m->rhs.p, sizeof(double) * m->nrow, cudaMemcpyDeviceToHost, c->stream));
+  ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+  return ELFEL_OK;
+}
+
+extern "C" int elfel_sysvec_assemble(elfel_ctx* h, int64_t nrow, const int64_t* rows, const double* vals, int64_t n,
+                                     double* out) {
+  if (!h) return ELFEL_ERR_ARG;
+  Ctx* c = &h->c;
+  if (nrow < 0 || n < 0 || (n > 0 && (!rows || !vals)) || (nrow > 0 && !out))
+    return fail(c, ELFEL_ERR_ARG, "sysvec: bad arguments");
+  cudaSetDevice(c->device);
+  DBuf<int32_t> J;
+  DBuf<double> V, dense;
+  ELFEL_TRY(to_index32(c, rows, n, nrow, &J, "SysvecAssembler row"));
+  ELFEL_TRY(V.alloc(c, (size_t)(n > 0 ? n : 1)));
+  if (n) ELFEL_CUDA(c, cudaMemcpyAsync(V.p, vals, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+  SlotGen g;
+  g.nel = n;
+  g.slots_per_elem = 1;
+  g.store_per_elem = 1;
+  g.nblocks = 1;
+  g.b[0].R = nullptr;
+  g.b[0].C = J.p;
+  g.b[0].nr = 1;
+  g.b[0].nc = 1;
+  Pattern P;
+  ELFEL_TRY(build_pattern(c, g, 1, nrow, &P));
+  ELFEL_TRY(dense.alloc(c, (size_t)(nrow > 0 ? nrow : 1)));
+  ELFEL_TRY(reduce_dense(c, P, V.p, dense.p));
+  if (nrow) ELFEL_CUDA(c, cudaMemcpyAsync(out, dense.p, sizeof(double) * nrow, cudaMemcpyDeviceToHost, c->stream));
+  ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+  P.release(c);
+  J.release(c);
+  V.release(c);
+  dense.release(c);
+  return ELFEL_OK;
+}
+
+// ------------------------------------------------------------------ fused
+static int upload_space(Ctx* c, const elfel_space& s, int64_t ndofs, DBuf<int32_t>* conn, DBuf<double>* xy,
+                        DBuf<int32_t>* dofs, const char* name) {
+  if (s.nel < 0 || s.nnodes < 0 || !s.conn || !s.eldofs || (s.nnodes > 0 && !s.xy))
+    return fail(c, ELFEL_ERR_ARG, "%s space: missing arrays", name);
+  const int nedof = s.nodes_per_elem * s.ncomp;
+  std::string w1 = std::string(name) + " connectivity";
+  std::string w2 = std::string(name) + " eldofs";
+  ELFEL_TRY(to_index32(c, s.conn, s.nel * s.nodes_per_elem, s.nnodes, conn, w1.c_str()));
+  ELFEL_TRY(to_index32(c, s.eldofs, s.nel * nedof, ndofs, dofs, w2.c_str()));
+  if (xy) {
+    ELFEL_TRY(xy->alloc(c, (size_t)(s.nnodes > 0 ? 2 * s.nnodes : 1)));
+    if (s.nnodes)
+      ELFEL_CUDA(c, cudaMemcpyAsync(xy->p, s.xy, sizeof(double) * 2 * s.nnodes, cudaMemcpyHostToDevice, c->stream));
+  }
+  return ELFEL_OK;
+}
+
+extern "C" int elfel_fused_setup(elfel_sysmat* m, const elfel_fused_desc* d) {
+  CHECK_M(m);
+  Ctx* c = &m->h->c;
+  if (!d) return fail(c, ELFEL_ERR_ARG, "fused_setup: NULL descriptor");
+  cudaSetDevice(c->device);
+  if (d->ndofs < 0) return fail(c, ELFEL_ERR_ARG, "fused_setup: negative ndofs");
+  const elfel_space& u = d->u;
+  if (u.nodes_per_elem != 3 && u.nodes_per_elem != 6)
+    return fail(c, ELFEL_ERR_UNSUPPORTED, "fused_setup: elements with %d nodes are not provided (T3, T6 only)",
+                u.nodes_per_elem);
+  if (d->npts < 1 || d->npts > kMaxQP || !d->qp_coords || !d->qp_weights)
+    return fail(c, ELFEL_ERR_ARG, "fused_setup: quadrature with %d points (1..%d)", d->npts, kMaxQP);
+  if (d->physics == ELFEL_HEAT && u.ncomp != 1)
+    return fail(c, ELFEL_ERR_ARG, "heat: scalar space expected (ncomp = %d)", u.ncomp);
+  if (d->physics == ELFEL_ELASTICITY && u.ncomp != 2)
+    return fail(c, ELFEL_ERR_ARG, "elasticity: 2-component space expected (ncomp = %d)", u.ncomp);
+  if (d->physics == ELFEL_STOKES) {
+    if (u.nodes_per_elem != 6 || u.ncomp != 2 || d->p.nodes_per_elem != 3 || d->p.ncomp != 1 || d->p.nel != u.nel)
+      return fail(c, ELFEL_ERR_UNSUPPORTED, "Stokes: vector T6 velocity and scalar T3 pressure on the same elements");
+  } else if (d->physics != ELFEL_HEAT && d->physics != ELFEL_ELASTICITY) {
+    return fail(c, ELFEL_ERR_ARG, "fused_setup: unknown physics %d", d->physics);
+  }
+  release_all(m);
+  Fused& F = m->F;
+  F.physics = d->physics;
+  F.npts = d->npts;
+  F.nn_u = u.nodes_per_elem;
+  F.ncomp_u = u.ncomp;
+  F.nel = u.nel;
+  F.nnodes_u = u.nnodes;
+  ELFEL_TRY(make_tables(u.nodes_per_elem, d->npts, d->qp_coords, d->qp_weights, &F.tab));
+  ELFEL_TRY(upload_space(c, u, d->ndofs, &F.conn_u, &F.xy_u, &F.dofs_u, "primary"));
+  const int nedof = u.nodes_per_elem * u.ncomp;
+  SlotGen& g = F.kgen;
+  g = SlotGen();
+  g.nel = u.nel;
+  g.nblocks = 1;
+  g.b[0].R = F.dofs_u.p;
+  g.b[0].C = F.dofs_u.p;
+  g.b[0].nr = g.b[0].nc = nedof;
+  g.b[0].sym = 1;
+  g.slots_per_elem = nedof * nedof;
+  g.store_per_elem = nedof * (nedof + 1) / 2;
+  if (d->physics == ELFEL_STOKES) {
+    F.nn_p = 3;
+    F.nnodes_p = d->p.nnodes;
+    ELFEL_TRY(upload_space(c, d->p, d->ndofs, &F.conn_p, nullptr, &F.dofs_p, "pressure"));
+    g.nblocks = 3;
+    g.b[1].R = F.dofs_u.p;
+    g.b[1].C = F.dofs_p.p;
+    g.b[1].nr = 12;
+    g.b[1].nc = 3;
+    g.b[1].slot_off = 144;
+    g.b[1].store_off = 78;
+    g.b[2] = g.b[1];
+    g.b[2].transposed = 1;
+    g.b[2].slot_off = 180;
+    g.slots_per_elem = 216;
+    g.store_per_elem = 78 + 36;
+  }
+  m->nrow = m->ncol = d->ndofs;
+  ELFEL_TRY(build_pattern(c, g, d->ndofs, d->ndofs, &m->P));
+  // right-hand side: a 1 x ndofs "matrix" of the element vectors
+  SlotGen& fg = F.fgen;
+  fg = SlotGen();
+  fg.nel = u.nel;
+  fg.nblocks = 1;
+  fg.b[0].R = nullptr;
+  fg.b[0].C = F.dofs_u.p;
+  fg.b[0].nr = 1;
+  fg.b[0].nc = nedof;
+  fg.slots_per_elem = nedof;
+  fg.store_per_elem = nedof;
+  ELFEL_TRY(build_pattern(c, fg, 1, d->ndofs, &F.fpat));
+  if (d->physics == ELFEL_STOKES) {
+    SlotGen pg;
+    pg.nel = u.nel;
+    pg.nblocks = 1;
+    pg.b[0].R = nullptr;
+    pg.b[0].C = F.dofs_p.p;
+    pg.b[0].nr = 1;
+    pg.b[0].nc = 3;
+    pg.slots_per_elem = 3;
+    pg.store_per_elem = 3;
+    ELFEL_TRY(build_pattern(c, pg, 1, d->ndofs, &F.pmpat));
+    ELFEL_TRY(F.pmass_store.alloc(c, (size_t)(u.nel * 3 > 0 ? u.nel * 3 : 1)));
+    ELFEL_TRY(F.pmass_diag.alloc(c, (size_t)(d->ndofs > 0 ? d->ndofs : 1)));
+  }
+  ELFEL_TRY(F.kstore.alloc(c, (size_t)(u.nel * g.store_per_elem > 0 ? u.nel * g.store_per_elem : 1)));
+  ELFEL_TRY(F.fstore.alloc(c, (size_t)(u.nel * nedof > 0 ? u.nel * nedof : 1)));
+  ELFEL_TRY(m->vals.alloc(c, (size_t)(m->P.nnz > 0 ? m->P.nnz : 1)));
+  ELFEL_TRY(m->rhs.alloc(c, (size_t)(d->ndofs > 0 ? d->ndofs : 1)));
+  ELFEL_TRY(F.coef.alloc(c, (size_t)(u.nel > 0 ? 2 * u.nel : 1)));
+  ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+  m->fused = 1;
+  m->started = 1;
+  m->finished = 0;
+  return ELFEL_OK;
+}
+
+extern "C" int elfel_fused_set_geometry(elfel_sysmat* m, const double* xy) {
+  CHECK_M(m);
+  Ctx* c = &m->h->c;
+  if (!m->fused) return fail(c, ELFEL_ERR_STATE, "set_geometry: call fused_setup first");
+  if (!xy) return fail(c, ELFEL_ERR_ARG, "set_geometry: NULL coordinates");
+  cudaSetDevice(c->device);
+  if (m->F.nnodes_u)
+    ELFEL_CUDA(c, cudaMemcpyAsync(m->F.xy_u.p, xy, sizeof(double) * 2 * m->F.nnodes_u, cudaMemcpyHostToDevice,
+                                  c->stream));
+  return ELFEL_OK;
+}
+
+static int finish_values(elfel_sysmat* m) {
+  Ctx* c = &m->h->c;
+  ELFEL_TRY(reduce_values(c, m->P, m->F.kstore.p, m->vals.p));
+  ELFEL_TRY(reduce_dense(c, m->F.fpat, m->F.fstore.p, m->rhs.p));
+  m->has_rhs = 1;
+  m->finished = 1;
+  m->values_version++;
+  return ELFEL_OK;
+}
+
+extern "C" int elfel_fused_heat(elfel_sysmat* m, const double* kappa, double Q) {
+  CHECK_M(m);
+  Ctx* c = &m->h->c;
+  if (!m->fused || m->F.physics != ELFEL_HEAT) return fail(c, ELFEL_ERR_STATE, "heat: fused_setup(ELFEL_HEAT) first");
+  cudaSetDevice(c->device);
+  Fused& F = m->F;
+  if (kappa && F.nel)
+    ELFEL_CUDA(c, cudaMemcpyAsync(F.coef.p, kappa, sizeof(double) * F.nel, cudaMemcpyHostToDevice, c->stream));
+  ELFEL_TRY(launch_heat(c, F.nn_u, F.nel, F.conn_u.p, F.xy_u.p, F.coef.p, Q, F.tab, F.kstore.p, F.fstore.p));
+  return finish_values(m);
+}
+
+extern "C" int elfel_fused_elasticity(elfel_sysmat* m, double E, double nu, int32_t plane_strain,
+                                      const double* bforce, const int64_t* trac_edges, int64_t ntrac,
+                                      const double* traction) {
+  CHECK_M(m);
+  Ctx* c = &m->h->c;
+  if (!m->fused || m->F.physics != ELFEL_ELASTICITY)
+    return fail(c, ELFEL_ERR_STATE, "elasticity: fused_setup(ELFEL_ELASTICITY) first");
+  if (ntrac < 0 || (ntrac > 0 && (!trac_edges || !traction))) return fail(c, ELFEL_ERR_ARG, "elasticity: traction");
+  cudaSetDevice(c->device);
+  Fused& F = m->F;
+  Mat3 D;
+  memset(&D, 0, sizeof(D));
+  if (plane_strain) {
+    const double f = E / ((1 + nu) * (1 - 2 * nu));
+    D.a[0][0] = D.a[1][1] = f * (1 - nu);
+    D.a[0][1] = D.a[1][0] = f * nu;
+    D.a[2][2] = f * (1 - 2 * nu) / 2;
+  } else {
+    const double f = E / (1 - nu * nu);
+    D.a[0][0] = D.a[1][1] = f;
+    D.a[0][1] = D.a[1][0] = f * nu;
+    D.a[2][2] = f * (1 - nu) / 2;
+  }
+  const double* bf = nullptr;
+  if (bforce && F.nel) {
+    ELFEL_CUDA(c, cudaMemcpyAsync(F.coef.p, bforce, sizeof(double) * 2 * F.nel, cudaMemcpyHostToDevice, c->stream));
+    bf = F.coef.p;
+  }
+  ELFEL_TRY(launch_elasticity(c, F.nn_u, F.nel, F.conn_u.p, F.xy_u.p, D, bf, F.tab, F.kstore.p, F.fstore.p));
+  ELFEL_TRY(finish_values(m));
+  if (ntrac > 0) {
+    const int nen = F.nn_u == 6 ? 3 : 2;
+    // (element, local edge) 1-based -> 0-based, range checked
+    std::vector<int64_t> flat((size_t)ntrac * 2);
+    for (int64_t k = 0; k < ntrac; ++k) {
+      int64_t e = trac_edges[2 * k], le = trac_edges[2 * k + 1];
+      if (e < 1 || e > F.nel || le < 1 || le > 3) return fail(c, ELFEL_ERR_ARG, "traction edge %lld invalid", (long long)k);
+      flat[2 * k] = e;
+      flat[2 * k + 1] = le;
+    }
+    DBuf<int32_t> edges, edofs;
+    DBuf<double> tstore, tvec;
+    ELFEL_TRY(to_index32(c, flat.data(), 2 * ntrac, F.nel, &edges, "traction edges"));
+    ELFEL_TRY(edofs.alloc(c, (size_t)ntrac * nen * 2));
+    edge_dofs_k<<<grid_for(ntrac, 128), 128, 0, c->stream>>>(ntrac, edges.p, F.dofs_u.p, F.nn_u, 2, edofs.p);
+    ELFEL_LAUNCH_CHECK(c);
+    ELFEL_TRY(tstore.alloc(c, (size_t)ntrac * nen * 2));
+    ELFEL_TRY(launch_traction(c, ntrac, edges.p, F.conn_u.p, F.nn_u, F.xy_u.p, traction[0], traction[1], tstore.p));
+    SlotGen tg;
+    tg.nel = ntrac;
+    tg.nblocks = 1;
+    tg.b[0].R = nullptr;
+    tg.b[0].C = edofs.p;
+    tg.b[0].nr = 1;
+    tg.b[0].nc = nen * 2;
+    tg.slots_per_elem = nen * 2;
+    tg.store_per_elem = nen * 2;
+    Pattern tp;
+    ELFEL_TRY(build_pattern(c, tg, 1, m->nrow, &tp));
+    ELFEL_TRY(tvec.alloc(c, (size_t)m->nrow));
+    ELFEL_TRY(reduce_dense(c, tp, tstore.p, tvec.p));
+    add_k<<<grid_for(m->nrow, 256, (int64_t)c->sm_count * 16), 256, 0, c->stream>>>(m->rhs.p, tvec.p, m->nrow);
+    ELFEL_LAUNCH_CHECK(c);
+    ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+    tp.release(c);
+    edges.release(c);
+    edofs.release(c);
+    tstore.release(c);
+    tvec.release(c);
+  }
+  return ELFEL_OK;
+}
+
+extern "C" int elfel_fused_stokes(elfel_sysmat* m, double mu) {
+  CHECK_M(m);
+  Ctx* c = &m->h->c;
+  if (!m->fused || m->F.physics != ELFEL_STOKES)
+    return fail(c, ELFEL_ERR_STATE, "stokes: fused_setup(ELFEL_STOKES) first");
+  cudaSetDevice(c->device);
+  Fused& F = m->F;
+  ELFEL_TRY(launch_stokes(c, F.nel, F.conn_u.p, F.xy_u.p, mu, F.tab, F.kstore.p, F.pmass_store.p));
+  ELFEL_TRY(reduce_values(c, m->P, F.kstore.p, m->vals.p));
+  ELFEL_CUDA(c, cudaMemsetAsync(m->rhs.p, 0, sizeof(double) * m->nrow, c->stream));
+  ELFEL_TRY(reduce_dense(c, F.pmpat, F.pmass_store.p, F.pmass_diag.p));
+  m->has_rhs = 1;
+  m->finished = 1;
+  m->values_version++;
+  return ELFEL_OK;
+}

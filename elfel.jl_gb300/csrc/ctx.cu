@@ -1,0 +1,239 @@
+// Context, device memory accounting, errors and the device scan.
+#include <stdarg.h>
+
+#include "common.cuh"
+
+namespace elfel {
+
+int fail(Ctx* c, int code, const char* fmt, ...) {
+  if (c) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    c->last_error = buf;
+  }
+  return code;
+}
+
+int dalloc(Ctx* c, void** p, size_t bytes) {
+  *p = nullptr;
+  if (bytes == 0) return ELFEL_OK;
+  if (c->budget > 0 && c->in_use + (int64_t)bytes > c->budget)
+    return fail(c, ELFEL_ERR_BUDGET, "device memory budget exceeded: in use %lld + request %zu > budget %lld",
+                (long long)c->in_use, bytes, (long long)c->budget);
+  cudaError_t e = cudaMallocAsync(p, bytes, c->stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(c, ELFEL_ERR_BUDGET, "cudaMallocAsync(%zu bytes): %s", bytes, cudaGetErrorString(e));
+  }
+  c->in_use += (int64_t)bytes;
+  if (c->in_use > c->peak) c->peak = c->in_use;
+  return ELFEL_OK;
+}
+
+void dfree(Ctx* c, void* p, size_t bytes) {
+  if (!p) return;
+  cudaFreeAsync(p, c->stream);
+  c->in_use -= (int64_t)bytes;
+}
+
+int red_scratch(Ctx* c, int nslots, int nblocks, RedSlot* slots) {
+  size_t per = (size_t)nblocks * sizeof(double) + 256;
+  size_t need = per * (size_t)nslots;
+  if (need > c->red_scratch_bytes) {
+    if (c->red_scratch) dfree(c, c->red_scratch, c->red_scratch_bytes);
+    c->red_scratch = nullptr;
+    c->red_scratch_bytes = 0;
+    ELFEL_TRY(dalloc(c, &c->red_scratch, need));
+    c->red_scratch_bytes = need;
+    ELFEL_CUDA(c, cudaMemsetAsync(c->red_scratch, 0, need, c->stream));
+  }
+  char* base = (char*)c->red_scratch;
+  for (int s = 0; s < nslots; ++s) {
+    slots[s].partials = (double*)(base + per * s);
+    slots[s].ticket = (unsigned int*)(base + per * s + (size_t)nblocks * sizeof(double));
+  }
+  return ELFEL_OK;
+}
+
+// ------------------------------------------------------------------ scan
+// Three-phase exclusive scan: per-block totals, recursive scan of the totals,
+// then a block-local scan with the block offset added.
+constexpr int kScanBlock = 512;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanBlock * kScanItems;
+
+template <typename TIn>
+__global__ void scan_block_totals_k(const TIn* in, int64_t n, int64_t* totals) {
+  __shared__ int64_t sh[kScanBlock / 32];
+  int64_t base = (int64_t)blockIdx.x * kScanTile;
+  int64_t s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    int64_t i = base + (int64_t)k * kScanBlock + threadIdx.x;
+    if (i < n) s += (int64_t)in[i];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int64_t t = 0;
+    for (int w = 0; w < kScanBlock / 32; ++w) t += sh[w];
+    totals[blockIdx.x] = t;
+  }
+}
+
+// Block-local exclusive scan of a tile; each thread owns kScanItems
+// consecutive items.  offsets = exclusive scan of the block totals.
+template <typename TIn>
+__global__ void scan_tile_k(const TIn* in, int64_t n, const int64_t* offsets, int64_t* out) {
+  __shared__ int64_t warp_tot[kScanBlock / 32];
+  int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  int64_t v[kScanItems];
+  int64_t run = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    int64_t i = base + k;
+    int64_t x = i < n ? (int64_t)in[i] : 0;
+    v[k] = run;
+    run += x;
+  }
+  // exclusive scan of the per-thread totals across the block
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int64_t incl = run;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int64_t t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) warp_tot[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    int64_t w = lane < kScanBlock / 32 ? warp_tot[lane] : 0;
+    int64_t wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int64_t t = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += t;
+    }
+    if (lane < kScanBlock / 32) warp_tot[lane] = wi - w;
+  }
+  __syncthreads();
+  int64_t excl = incl - run + warp_tot[wid] + offsets[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    int64_t i = base + k;
+    if (i < n) out[i] = v[k] + excl;
+  }
+}
+
+__global__ void write_total_k(const int64_t* offsets, int64_t nblocks, const int64_t* totals, int64_t* out_total) {
+  *out_total = offsets[nblocks - 1] + totals[nblocks - 1];
+}
+
+template <typename TIn>
+static int scan_impl(Ctx* c, const TIn* in, int64_t n, int64_t* out) {
+  if (n <= 0) {
+    ELFEL_CUDA(c, cudaMemsetAsync(out, 0, sizeof(int64_t), c->stream));
+    return ELFEL_OK;
+  }
+  int64_t nb = (n + kScanTile - 1) / kScanTile;
+  DBuf<int64_t> totals, offsets;
+  ELFEL_TRY(totals.alloc(c, (size_t)nb));
+  ELFEL_TRY(offsets.alloc(c, (size_t)nb + 1));
+  scan_block_totals_k<TIn><<<(unsigned)nb, kScanBlock, 0, c->stream>>>(in, n, totals.p);
+  ELFEL_LAUNCH_CHECK(c);
+  if (nb == 1) {
+    ELFEL_CUDA(c, cudaMemsetAsync(offsets.p, 0, sizeof(int64_t), c->stream));
+  } else {
+    ELFEL_TRY(scan_impl<int64_t>(c, totals.p, nb, offsets.p));
+  }
+  scan_tile_k<TIn><<<(unsigned)nb, kScanBlock, 0, c->stream>>>(in, n, offsets.p, out);
+  ELFEL_LAUNCH_CHECK(c);
+  write_total_k<<<1, 1, 0, c->stream>>>(offsets.p, nb, totals.p, out + n);
+  ELFEL_LAUNCH_CHECK(c);
+  totals.release(c);
+  offsets.release(c);
+  return ELFEL_OK;
+}
+
+int exclusive_scan_i64(Ctx* c, int64_t* data, int64_t n) {
+  // in-place: scan_tile reads its own items before writing them, and reads
+  // only its own tile, so in == out is safe.
+  return scan_impl<int64_t>(c, data, n, data);
+}
+
+int scan_counts_i32(Ctx* c, const int32_t* counts, int64_t n, int64_t* offsets) {
+  return scan_impl<int32_t>(c, counts, n, offsets);
+}
+
+}  // namespace elfel
+
+// ------------------------------------------------------------------ C ABI
+using namespace elfel;
+
+extern "C" int elfel_abi_version(void) { return ELFEL_ABI_VERSION; }
+
+extern "C" int elfel_ctx_create(int device, int64_t mem_budget_bytes, elfel_ctx** out) {
+  if (!out) return ELFEL_ERR_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+    cudaGetLastError();
+    return ELFEL_ERR_CUDA;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) return ELFEL_ERR_CUDA;
+  elfel_ctx* h = new elfel_ctx();
+  h->c.device = device;
+  h->c.budget = mem_budget_bytes;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) == cudaSuccess) h->c.sm_count = prop.multiProcessorCount;
+  if (cudaStreamCreateWithFlags(&h->c.stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete h;
+    return ELFEL_ERR_CUDA;
+  }
+  h->c.own_stream = h->c.stream;
+  *out = h;
+  return ELFEL_OK;
+}
+
+extern "C" int elfel_ctx_destroy(elfel_ctx* h) {
+  if (!h) return ELFEL_OK;
+  cudaSetDevice(h->c.device);
+  if (h->c.red_scratch) dfree(&h->c, h->c.red_scratch, h->c.red_scratch_bytes);
+  cudaStreamSynchronize(h->c.stream);
+  if (h->c.own_stream) cudaStreamDestroy(h->c.own_stream);
+  delete h;
+  return ELFEL_OK;
+}
+
+extern "C" const char* elfel_ctx_last_error(const elfel_ctx* h) {
+  return h ? h->c.last_error.c_str() : "null context";
+}
+
+extern "C" int elfel_ctx_memory(const elfel_ctx* h, int64_t* in_use, int64_t* peak) {
+  if (!h) return ELFEL_ERR_ARG;
+  if (in_use) *in_use = h->c.in_use;
+  if (peak) *peak = h->c.peak;
+  return ELFEL_OK;
+}
+
+extern "C" int elfel_ctx_set_stream(elfel_ctx* h, void* s) {
+  if (!h) return ELFEL_ERR_ARG;
+  Ctx* c = &h->c;
+  ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->stream = s ? (cudaStream_t)s : c->own_stream;
+  return ELFEL_OK;
+}
+
+extern "C" void* elfel_ctx_stream(const elfel_ctx* h) { return h ? (void*)h->c.stream : nullptr; }
+
+extern "C" int elfel_ctx_synchronize(elfel_ctx* h) {
+  if (!h) return ELFEL_ERR_ARG;
+  Ctx* c = &h->c;
+  ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+  return ELFEL_OK;
+}

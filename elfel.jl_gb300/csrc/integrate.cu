@@ -1,0 +1,503 @@
+// Element integration kernels: one thread per element, a CTA per batch of
+// kIntThreads elements.
+//   (a) the batch's connectivity is loaded into shared memory with coalesced
+//       loads, node coordinates are gathered as 16-byte double2 loads;
+//   (b) basis values / parametric gradients at the quadrature points are
+//       staged once per CTA in shared memory;
+//   (c) Jacobian, inverse, gradients and the element-matrix products run in
+//       registers; results are staged in shared memory and written out as one
+//       contiguous, coalesced record block per CTA.
+// Element records are consumed by reduce_values() through the slot map.
+//
+// Weak forms restated from the reference (Elfel.jl v0.4.0):
+//   heat        test/test_heat.jl:49-54
+//   elasticity  test/test_elasticity.jl:150-167
+//   Stokes TH   test/test_stokes.jl:645-652 (vector Laplacian form)
+// Geometry: src/FElements.jl:148-168 (J = sum_j x_j (x) gradNpar_j, det J),
+//           src/QPIterators.jl:132-140 (gradN = gradNpar / J).
+//
+// Straight-sided elements (T3 always; T6 when each midside node is exactly the
+// midpoint of its edge) have a constant Jacobian.  For them the quadrature sum
+// is reorganised with reference tensors precomputed from the same rule:
+//   ke_ij = kappa*det * sum_q w_q gradN_i(q).gradN_j(q)
+//         = c11*S11_ij + c22*S22_ij + c12*S12_ij,  S^{ab}_ij = sum_q w_q dN_i/dxi_a dN_j/dxi_b
+// (the tensor representation of Kirby & Logg's FFC).  Curved T6 elements take
+// the per-quadrature-point path, which mirrors the reference loop.
+#include "integrate.cuh"
+
+namespace elfel {
+
+// ------------------------------------------------------------------ tables
+static void bfun_host(int nn, double r, double s, double* N, double* G) {
+  if (nn == 3) {
+    N[0] = 1.0 - r - s; N[1] = r; N[2] = s;
+    G[0] = -1.0; G[1] = -1.0; G[2] = 1.0; G[3] = 0.0; G[4] = 0.0; G[5] = 1.0;
+  } else {
+    double t = 1.0 - r - s;
+    N[0] = t * (t + t - 1); N[1] = r * (r + r - 1); N[2] = s * (s + s - 1);
+    N[3] = 4 * r * t; N[4] = 4 * r * s; N[5] = 4 * s * t;
+    G[0] = -3 + 4 * r + 4 * s; G[1] = -3 + 4 * r + 4 * s;
+    G[2] = 4 * r - 1;          G[3] = 0.0;
+    G[4] = 0.0;                G[5] = 4 * s - 1;
+    G[6] = 4 - 8 * r - 4 * s;  G[7] = -4 * r;
+    G[8] = 4 * s;              G[9] = 4 * r;
+    G[10] = -4 * s;            G[11] = 4 - 4 * r - 8 * s;
+  }
+}
+
+int make_tables(int nn, int npts, const double* pc, const double* w, QPTab* t) {
+  if (npts < 1 || npts > kMaxQP || (nn != 3 && nn != 6)) return ELFEL_ERR_ARG;
+  memset(t, 0, sizeof(*t));
+  t->npts = npts;
+  t->nn = nn;
+  for (int q = 0; q < npts; ++q) {
+    t->w[q] = w[q];
+    double Np[3], Gp[6];
+    bfun_host(nn, pc[2 * q], pc[2 * q + 1], t->N[q], &t->G[q][0][0]);
+    bfun_host(3, pc[2 * q], pc[2 * q + 1], Np, Gp);
+    for (int j = 0; j < 3; ++j) t->Np[q][j] = Np[j];
+  }
+  // reference tensors for straight-sided elements
+  for (int i = 0; i < nn; ++i) {
+    double P = 0.0;
+    for (int q = 0; q < npts; ++q) P += t->w[q] * t->N[q][i];
+    t->P[i] = P;
+    for (int j = 0; j < nn; ++j) {
+      for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b) {
+          double s = 0.0;
+          for (int q = 0; q < npts; ++q) s += t->w[q] * t->G[q][i][a] * t->G[q][j][b];
+          t->S[a][b][i * 6 + j] = s;
+        }
+    }
+    for (int j = 0; j < 3; ++j)
+      for (int a = 0; a < 2; ++a) {
+        double s = 0.0;
+        for (int q = 0; q < npts; ++q) s += t->w[q] * t->Np[q][j] * t->G[q][i][a];
+        t->T[a][i * 3 + j] = s;
+      }
+    for (int j = 0; j < 3; ++j) {
+      double s = 0.0;
+      for (int q = 0; q < npts; ++q) s += t->w[q] * t->Np[q][j] * t->Np[q][j];
+      t->Mp[j] = s;
+    }
+  }
+  return ELFEL_OK;
+}
+
+// ------------------------------------------------------------------ helpers
+template <int NN>
+struct Geo {
+  double x[NN], y[NN];
+};
+
+template <int NN>
+__device__ __forceinline__ bool straight_sided(const Geo<NN>& g) {
+  if (NN == 3) return true;
+  return g.x[3] == 0.5 * (g.x[0] + g.x[1]) && g.y[3] == 0.5 * (g.y[0] + g.y[1]) &&
+         g.x[4] == 0.5 * (g.x[1] + g.x[2]) && g.y[4] == 0.5 * (g.y[1] + g.y[2]) &&
+         g.x[5] == 0.5 * (g.x[2] + g.x[0]) && g.y[5] == 0.5 * (g.y[2] + g.y[0]);
+}
+
+// Stage the element tables of a CTA in shared memory.
+struct SmemTab {
+  double w[kMaxQP];
+  double N[kMaxQP][6];
+  double G[kMaxQP][6][2];
+  double Np[kMaxQP][3];
+};
+
+__device__ __forceinline__ void stage_tables(const QPTab& t, SmemTab* s) {
+  for (int k = threadIdx.x; k < t.npts; k += blockDim.x) s->w[k] = t.w[k];
+  for (int k = threadIdx.x; k < t.npts * 6; k += blockDim.x) (&s->N[0][0])[k] = (&t.N[0][0])[k];
+  for (int k = threadIdx.x; k < t.npts * 12; k += blockDim.x) (&s->G[0][0][0])[k] = (&t.G[0][0][0])[k];
+  for (int k = threadIdx.x; k < t.npts * 3; k += blockDim.x) (&s->Np[0][0])[k] = (&t.Np[0][0])[k];
+}
+
+// Load a CTA's connectivity tile (coalesced) and gather this thread's nodes.
+template <int NN>
+__device__ __forceinline__ void load_geo(const int32_t* __restrict__ conn, const double2* __restrict__ xy, int64_t e0,
+                                         int64_t nel, int32_t* sconn, Geo<NN>& g, int32_t* nodes) {
+  const int64_t base = e0 * NN;
+  const int64_t lim = nel * NN;
+  for (int k = threadIdx.x; k < kIntThreads * NN; k += kIntThreads) {
+    int64_t gi = base + k;
+    sconn[k] = gi < lim ? __ldg(conn + gi) : 0;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < NN; ++j) {
+    int32_t n = sconn[threadIdx.x * NN + j];
+    if (nodes) nodes[j] = n;
+    double2 p = __ldg(xy + n);
+    g.x[j] = p.x;
+    g.y[j] = p.y;
+  }
+}
+
+// Write a CTA's records, staged as acc[k * (kIntThreads + 1) + t], to
+// out[(e0 + t) * rec + k] in one contiguous pass.
+__device__ __forceinline__ void write_records(const double* acc, int rec, int64_t e0, int64_t nel, double* out) {
+  __syncthreads();
+  const int64_t nvalid = min((int64_t)kIntThreads, nel - e0);
+  const int64_t total = nvalid * rec;
+  double* dst = out + e0 * rec;
+  for (int64_t L = threadIdx.x; L < total; L += kIntThreads) {
+    int t = (int)(L / rec), k = (int)(L - (int64_t)t * rec);
+    dst[L] = acc[k * (kIntThreads + 1) + t];
+  }
+}
+
+// ------------------------------------------------------------------ heat
+template <int NN>
+__global__ void __launch_bounds__(kIntThreads) heat_k(int64_t nel, const int32_t* __restrict__ conn,
+                                                     const double2* __restrict__ xy, const double* __restrict__ kappa,
+                                                     double Q, const __grid_constant__ QPTab tab,
+                                                     double* __restrict__ kstore, double* __restrict__ fstore) {
+  constexpr int NS = NN * (NN + 1) / 2;
+  constexpr int LD = kIntThreads + 1;
+  extern __shared__ double acc[];  // (NS + NN) * LD
+  __shared__ SmemTab st;
+  __shared__ int32_t sconn[kIntThreads * NN];
+  __shared__ double sS[3][NS];
+  stage_tables(tab, &st);
+  for (int k = threadIdx.x; k < NS; k += kIntThreads) {
+    int j = 0;
+    while ((j + 1) * (j + 2) / 2 <= k) ++j;
+    int i = k - j * (j + 1) / 2;
+    sS[0][k] = tab.S[0][0][i * 6 + j];
+    sS[1][k] = tab.S[1][1][i * 6 + j];
+    sS[2][k] = tab.S[0][1][i * 6 + j] + tab.S[1][0][i * 6 + j];
+  }
+  const int64_t e0 = (int64_t)blockIdx.x * kIntThreads;
+  Geo<NN> g;
+  load_geo<NN>(conn, xy, e0, nel, sconn, g, nullptr);  // contains __syncthreads
+  const int t = threadIdx.x;
+  const int64_t e = e0 + t;
+  double* fa = acc + NS * LD;
+  if (e < nel) {
+    const double kap = kappa[e];
+    if (straight_sided<NN>(g)) {
+      const double J11 = g.x[1] - g.x[0], J12 = g.x[2] - g.x[0];
+      const double J21 = g.y[1] - g.y[0], J22 = g.y[2] - g.y[0];
+      const double det = J11 * J22 - J21 * J12;
+      const double s = kap / det;
+      const double c11 = (J22 * J22 + J12 * J12) * s;
+      const double c22 = (J21 * J21 + J11 * J11) * s;
+      const double c12 = -(J22 * J21 + J12 * J11) * s;
+#pragma unroll
+      for (int k = 0; k < NS; ++k) acc[k * LD + t] = c11 * sS[0][k] + c22 * sS[1][k] + c12 * sS[2][k];
+      const double qd = Q * det;
+#pragma unroll
+      for (int j = 0; j < NN; ++j) fa[j * LD + t] = qd * tab.P[j];
+    } else {
+      double ke[NS], fe[NN];
+#pragma unroll
+      for (int k = 0; k < NS; ++k) ke[k] = 0.0;
+#pragma unroll
+      for (int j = 0; j < NN; ++j) fe[j] = 0.0;
+      for (int q = 0; q < tab.npts; ++q) {
+        double J11 = 0, J12 = 0, J21 = 0, J22 = 0;
+#pragma unroll
+        for (int j = 0; j < NN; ++j) {
+          J11 += g.x[j] * st.G[q][j][0];
+          J12 += g.x[j] * st.G[q][j][1];
+          J21 += g.y[j] * st.G[q][j][0];
+          J22 += g.y[j] * st.G[q][j][1];
+        }
+        const double det = J11 * J22 - J21 * J12;
+        const double rd = 1.0 / det;
+        double gx[NN], gy[NN];
+#pragma unroll
+        for (int j = 0; j < NN; ++j) {
+          const double a = st.G[q][j][0], b = st.G[q][j][1];
+          gx[j] = (a * J22 - b * J21) * rd;
+          gy[j] = (-a * J12 + b * J11) * rd;
+        }
+        const double JxW = det * st.w[q];
+        const double c = kap * JxW;
+#pragma unroll
+        for (int j = 0; j < NN; ++j) {
+#pragma unroll
+          for (int i = 0; i <= j; ++i) ke[j * (j + 1) / 2 + i] += (gx[i] * gx[j] + gy[i] * gy[j]) * c;
+          fe[j] += st.N[q][j] * Q * JxW;
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < NS; ++k) acc[k * LD + t] = ke[k];
+#pragma unroll
+      for (int j = 0; j < NN; ++j) fa[j * LD + t] = fe[j];
+    }
+  }
+  write_records(acc, NS, e0, nel, kstore);
+  __syncthreads();
+  write_records(fa, NN, e0, nel, fstore);
+}
+
+int launch_heat(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* xy, const double* kappa, double Q,
+                const QPTab& tab, double* kstore, double* fstore) {
+  if (nel == 0) return ELFEL_OK;
+  const unsigned grid = grid_for(nel, kIntThreads);
+  if (nn == 3) {
+    const size_t sm = (size_t)(6 + 3) * (kIntThreads + 1) * sizeof(double);
+    heat_k<3><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, (const double2*)xy, kappa, Q, tab, kstore, fstore);
+  } else {
+    const size_t sm = (size_t)(21 + 6) * (kIntThreads + 1) * sizeof(double);
+    heat_k<6><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, (const double2*)xy, kappa, Q, tab, kstore, fstore);
+  }
+  ELFEL_LAUNCH_CHECK(c);
+  return ELFEL_OK;
+}
+
+// ------------------------------------------------------------------ elasticity
+// 2-component vector space; DOF k of the element = node k/2, component k%2.
+// B(g,0) = (g1, 0, g2), B(g,1) = (0, g2, g1);  ke_ij += dot(D*B_j, B_i) * JxW.
+template <int NN>
+__global__ void __launch_bounds__(kIntThreads) elast_k(int64_t nel, const int32_t* __restrict__ conn,
+                                                      const double2* __restrict__ xy, const Mat3 D,
+                                                      const double* __restrict__ bforce,
+                                                      const __grid_constant__ QPTab tab, double* __restrict__ kstore,
+                                                      double* __restrict__ fstore) {
+  constexpr int ND = 2 * NN;
+  constexpr int NS = ND * (ND + 1) / 2;
+  constexpr int LD = kIntThreads + 1;
+  extern __shared__ double acc[];  // (NS + ND) * LD
+  __shared__ SmemTab st;
+  __shared__ int32_t sconn[kIntThreads * NN];
+  stage_tables(tab, &st);
+  const int64_t e0 = (int64_t)blockIdx.x * kIntThreads;
+  Geo<NN> g;
+  load_geo<NN>(conn, xy, e0, nel, sconn, g, nullptr);
+  const int t = threadIdx.x;
+  const int64_t e = e0 + t;
+  double* fa = acc + NS * LD;
+  if (e < nel) {
+    for (int k = 0; k < NS; ++k) acc[k * LD + t] = 0.0;
+    for (int k = 0; k < ND; ++k) fa[k * LD + t] = 0.0;
+    double b0 = 0.0, b1 = 0.0;
+    if (bforce) {
+      b0 = bforce[2 * e];
+      b1 = bforce[2 * e + 1];
+    }
+    for (int q = 0; q < tab.npts; ++q) {
+      double J11 = 0, J12 = 0, J21 = 0, J22 = 0;
+#pragma unroll
+      for (int j = 0; j < NN; ++j) {
+        J11 += g.x[j] * st.G[q][j][0];
+        J12 += g.x[j] * st.G[q][j][1];
+        J21 += g.y[j] * st.G[q][j][0];
+        J22 += g.y[j] * st.G[q][j][1];
+      }
+      const double det = J11 * J22 - J21 * J12;
+      const double rd = 1.0 / det;
+      double gx[NN], gy[NN];
+#pragma unroll
+      for (int j = 0; j < NN; ++j) {
+        const double a = st.G[q][j][0], b = st.G[q][j][1];
+        gx[j] = (a * J22 - b * J21) * rd;
+        gy[j] = (-a * J12 + b * J11) * rd;
+      }
+      const double JxW = det * st.w[q];
+#pragma unroll
+      for (int j = 0; j < ND; ++j) {
+        const int nj = j >> 1;
+        double B0, B1, B2;
+        if ((j & 1) == 0) { B0 = gx[nj]; B1 = 0.0; B2 = gy[nj]; }
+        else { B0 = 0.0; B1 = gy[nj]; B2 = gx[nj]; }
+        const double d0 = D.a[0][0] * B0 + D.a[0][1] * B1 + D.a[0][2] * B2;
+        const double d1 = D.a[1][0] * B0 + D.a[1][1] * B1 + D.a[1][2] * B2;
+        const double d2 = D.a[2][0] * B0 + D.a[2][1] * B1 + D.a[2][2] * B2;
+#pragma unroll
+        for (int i = 0; i <= j; ++i) {
+          const int ni = i >> 1;
+          double v;
+          if ((i & 1) == 0) v = d0 * gx[ni] + d2 * gy[ni];
+          else v = d1 * gy[ni] + d2 * gx[ni];
+          acc[(j * (j + 1) / 2 + i) * LD + t] += v * JxW;
+        }
+      }
+      if (bforce) {
+#pragma unroll
+        for (int a = 0; a < NN; ++a) {
+          fa[(2 * a) * LD + t] += st.N[q][a] * b0 * JxW;
+          fa[(2 * a + 1) * LD + t] += st.N[q][a] * b1 * JxW;
+        }
+      }
+    }
+  }
+  write_records(acc, NS, e0, nel, kstore);
+  __syncthreads();
+  write_records(fa, ND, e0, nel, fstore);
+}
+
+int launch_elasticity(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* xy, const Mat3& D,
+                      const double* bforce, const QPTab& tab, double* kstore, double* fstore) {
+  if (nel == 0) return ELFEL_OK;
+  const unsigned grid = grid_for(nel, kIntThreads);
+  if (nn == 3) {
+    const size_t sm = (size_t)(21 + 6) * (kIntThreads + 1) * sizeof(double);
+    elast_k<3><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, (const double2*)xy, D, bforce, tab, kstore, fstore);
+  } else {
+    const size_t sm = (size_t)(78 + 12) * (kIntThreads + 1) * sizeof(double);
+    ELFEL_CUDA(c, cudaFuncSetAttribute(elast_k<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    elast_k<6><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, (const double2*)xy, D, bforce, tab, kstore, fstore);
+  }
+  ELFEL_LAUNCH_CHECK(c);
+  return ELFEL_OK;
+}
+
+// Traction on element edges: consistent nodal loads sum_q w_q N_i(s_q) t |dx/ds|
+// with the 3-point Gauss rule on the edge (exact for the quadratic edge).
+// Edge k of a triangle runs from vertex k to vertex (k+1)%3; for T6 the
+// midside node of that edge is node 3+k.  Output: ntrac records of 2*nen values
+// in (edge node, component) order.
+__global__ void traction_k(int64_t ntrac, const int32_t* __restrict__ edges /* ntrac x 2: element, local edge */,
+                           const int32_t* __restrict__ conn, int nn, const double2* __restrict__ xy, double t0,
+                           double t1, double* __restrict__ out) {
+  const double gs[3] = {-0.774596669241483377, 0.0, 0.774596669241483377};
+  const double gw[3] = {5.0 / 9.0, 8.0 / 9.0, 5.0 / 9.0};
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < ntrac; k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = edges[2 * k];
+    const int le = edges[2 * k + 1];
+    const int nen = nn == 6 ? 3 : 2;
+    double2 p[3];
+    p[0] = xy[conn[e * nn + le]];
+    p[1] = xy[conn[e * nn + (le + 1) % 3]];
+    if (nen == 3) p[2] = xy[conn[e * nn + 3 + le]];
+    double f[3] = {0.0, 0.0, 0.0};
+    for (int q = 0; q < 3; ++q) {
+      const double s = gs[q];
+      double N[3], dN[3];
+      if (nen == 2) {
+        N[0] = 0.5 * (1 - s); N[1] = 0.5 * (1 + s); N[2] = 0;
+        dN[0] = -0.5; dN[1] = 0.5; dN[2] = 0;
+      } else {
+        N[0] = 0.5 * s * (s - 1); N[1] = 0.5 * s * (s + 1); N[2] = 1 - s * s;
+        dN[0] = s - 0.5; dN[1] = s + 0.5; dN[2] = -2 * s;
+      }
+      double tx = 0, ty = 0;
+      for (int a = 0; a < nen; ++a) {
+        tx += dN[a] * p[a].x;
+        ty += dN[a] * p[a].y;
+      }
+      const double jac = sqrt(tx * tx + ty * ty);
+      for (int a = 0; a < nen; ++a) f[a] += gw[q] * N[a] * jac;
+    }
+    for (int a = 0; a < nen; ++a) {
+      out[k * 2 * nen + 2 * a] = f[a] * t0;
+      out[k * 2 * nen + 2 * a + 1] = f[a] * t1;
+    }
+  }
+}
+
+int launch_traction(Ctx* c, int64_t ntrac, const int32_t* edges, const int32_t* conn, int nn, const double* xy,
+                    double t0, double t1, double* out) {
+  if (ntrac == 0) return ELFEL_OK;
+  traction_k<<<grid_for(ntrac, 128), 128, 0, c->stream>>>(ntrac, edges, conn, nn, (const double2*)xy, t0, t1, out);
+  ELFEL_LAUNCH_CHECK(c);
+  return ELFEL_OK;
+}
+
+// ------------------------------------------------------------------ Stokes
+// Velocity: vector T6 (12 DOFs, node-major / component-minor), pressure T3.
+// Record: kuu upper triangle (78) | kup 12x3 column-major (36).
+// kuu_ij += (mu*JxW) * dot(gradNu_i, gradNu_j) when comp(i) == comp(j), else 0
+// kup_ij += (-JxW * Np_j) * gradNu_i[comp(i)].
+// Also the pressure mass diagonal per element: sum_q w_q det Np_j^2.
+__global__ void __launch_bounds__(kIntThreads) stokes_k(int64_t nel, const int32_t* __restrict__ conn,
+                                                       const double2* __restrict__ xy, double mu,
+                                                       const __grid_constant__ QPTab tab, double* __restrict__ kstore,
+                                                       double* __restrict__ pmass) {
+  constexpr int NN = 6;
+  constexpr int NS = 78;
+  constexpr int NR = NS + 36;
+  constexpr int LD = kIntThreads + 1;
+  extern __shared__ double acc[];  // (NR + 3) * LD
+  __shared__ SmemTab st;
+  __shared__ int32_t sconn[kIntThreads * NN];
+  stage_tables(tab, &st);
+  const int64_t e0 = (int64_t)blockIdx.x * kIntThreads;
+  Geo<NN> g;
+  load_geo<NN>(conn, xy, e0, nel, sconn, g, nullptr);
+  const int t = threadIdx.x;
+  const int64_t e = e0 + t;
+  double* pa = acc + NR * LD;
+  if (e < nel) {
+    double kuu[21];  // scalar Laplacian block (upper triangle), shared by both components
+    double kup[12][3];
+    double mp[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int k = 0; k < 21; ++k) kuu[k] = 0.0;
+#pragma unroll
+    for (int a = 0; a < 12; ++a) kup[a][0] = kup[a][1] = kup[a][2] = 0.0;
+    for (int q = 0; q < tab.npts; ++q) {
+      double J11 = 0, J12 = 0, J21 = 0, J22 = 0;
+#pragma unroll
+      for (int j = 0; j < NN; ++j) {
+        J11 += g.x[j] * st.G[q][j][0];
+        J12 += g.x[j] * st.G[q][j][1];
+        J21 += g.y[j] * st.G[q][j][0];
+        J22 += g.y[j] * st.G[q][j][1];
+      }
+      const double det = J11 * J22 - J21 * J12;
+      const double rd = 1.0 / det;
+      double gx[NN], gy[NN];
+#pragma unroll
+      for (int j = 0; j < NN; ++j) {
+        const double a = st.G[q][j][0], b = st.G[q][j][1];
+        gx[j] = (a * J22 - b * J21) * rd;
+        gy[j] = (-a * J12 + b * J11) * rd;
+      }
+      const double JxW = det * st.w[q];
+      const double c = mu * JxW;
+#pragma unroll
+      for (int j = 0; j < NN; ++j)
+#pragma unroll
+        for (int i = 0; i <= j; ++i) kuu[j * (j + 1) / 2 + i] += c * (gx[i] * gx[j] + gy[i] * gy[j]);
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const double s = -JxW * st.Np[q][j];
+#pragma unroll
+        for (int a = 0; a < NN; ++a) {
+          kup[2 * a][j] += s * gx[a];
+          kup[2 * a + 1][j] += s * gy[a];
+        }
+        mp[j] += JxW * st.Np[q][j] * st.Np[q][j];
+      }
+    }
+    // expand the scalar block into the 12x12 upper triangle (cross-component = 0)
+#pragma unroll
+    for (int J = 0; J < 12; ++J)
+#pragma unroll
+      for (int I = 0; I <= J; ++I) {
+        double v = 0.0;
+        if ((I & 1) == (J & 1)) {
+          const int i = I >> 1, j = J >> 1;
+          v = kuu[j * (j + 1) / 2 + i];
+        }
+        acc[(J * (J + 1) / 2 + I) * LD + t] = v;
+      }
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int a = 0; a < 12; ++a) acc[(NS + a + 12 * j) * LD + t] = kup[a][j];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) pa[j * LD + t] = mp[j];
+  }
+  write_records(acc, NR, e0, nel, kstore);
+  __syncthreads();
+  write_records(pa, 3, e0, nel, pmass);
+}
+
+int launch_stokes(Ctx* c, int64_t nel, const int32_t* conn, const double* xy, double mu, const QPTab& tab,
+                  double* kstore, double* pmass) {
+  if (nel == 0) return ELFEL_OK;
+  const size_t sm = (size_t)(78 + 36 + 3) * (kIntThreads + 1) * sizeof(double);
+  ELFEL_CUDA(c, cudaFuncSetAttribute(stokes_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  stokes_k<<<grid_for(nel, kIntThreads), kIntThreads, sm, c->stream>>>(nel, conn, (const double2*)xy, mu, tab,
+                                                                        kstore, pmass);
+  ELFEL_LAUNCH_CHECK(c);
+  return ELFEL_OK;
+}
+
+}  // namespace elfel

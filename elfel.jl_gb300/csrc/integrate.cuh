@@ -1,0 +1,43 @@
+// Element-integration kernels and their quadrature tables.
+#pragma once
+#include "common.cuh"
+
+namespace elfel {
+
+constexpr int kIntThreads = 128;  // elements per CTA
+constexpr int kMaxQP = 16;
+
+// Quadrature-point tables of one element type, passed by value to kernels.
+// Values and parametric gradients follow src/FElements.jl:239-288 and are
+// evaluated at the rule's points as QPIterator's __bfundata does
+// (src/QPIterators.jl:14-50).
+struct QPTab {
+  int npts;
+  int nn;
+  double w[kMaxQP];
+  double N[kMaxQP][6];
+  double G[kMaxQP][6][2];
+  double Np[kMaxQP][3];  // T3 basis (Taylor-Hood pressure) at the same points
+  // reference tensors for straight-sided elements (index i*6 + j)
+  double S[2][2][36];  // sum_q w_q G_i,a G_j,b
+  double T[2][18];     // sum_q w_q Np_j G_i,a      (index i*3 + j)
+  double P[6];         // sum_q w_q N_i
+  double Mp[3];        // sum_q w_q Np_j^2
+};
+
+struct Mat3 {
+  double a[3][3];
+};
+
+int make_tables(int nn, int npts, const double* pc, const double* w, QPTab* t);
+
+int launch_heat(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* xy, const double* kappa, double Q,
+                const QPTab& tab, double* kstore, double* fstore);
+int launch_elasticity(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* xy, const Mat3& D,
+                      const double* bforce, const QPTab& tab, double* kstore, double* fstore);
+int launch_traction(Ctx* c, int64_t ntrac, const int32_t* edges, const int32_t* conn, int nn, const double* xy,
+                    double t0, double t1, double* out);
+int launch_stokes(Ctx* c, int64_t nel, const int32_t* conn, const double* xy, double mu, const QPTab& tab,
+                  double* kstore, double* pmass);
+
+}  // namespace elfel

@@ -1,0 +1,270 @@
+// Device construction of the CSC pattern and of the per-nonzero contributor
+// lists (the "slot -> nonzero" map), with the semantics of
+// SparseArrays.sparse(I, J, V, m, n) as called by finish! of
+// SysmatAssemblerSparse (Elfel.jl src/Assemblers.jl:121-123):
+//   * one slot per appended triplet, ordered as the assemble! calls append them;
+//   * entries with equal (row, col) are summed in that slot order;
+//   * explicitly assembled zeros stay in the pattern;
+//   * rows ascend within each column.
+//
+// Steps (all deterministic; integer atomics only count and bucket):
+//   1. column counts                           (int32 atomics)
+//   2. exclusive scan -> column starts
+//   3. bucket each slot's key (row << 32 | slot) into its column
+//   4. sort each column's keys (one warp per column, bitonic network)
+//   5. count distinct rows per column, scan -> colptr
+//   6. emit rowval, the first contribution of each nonzero (cptr) and the
+//      storage index of every contribution (contrib), in sorted order.
+#include "sysmat.cuh"
+
+namespace elfel {
+
+constexpr int kSortThreads = 256;           // 8 warps, one column each
+constexpr int kSortCap = 256;               // keys per warp sorted in shared memory
+constexpr uint64_t kKeyInf = ~0ull;
+
+__global__ void count_cols_k(SlotGen g, int64_t n, int32_t* colcnt, int64_t ncol, int64_t nrow, int* bad) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
+    int32_t r, c;
+    int64_t st;
+    slot_rc(g, s, r, c, st);
+    if (r < 0 || r >= nrow || c < 0 || c >= ncol) {
+      atomicExch(bad, 1);
+      continue;
+    }
+    atomicAdd(&colcnt[c], 1);
+  }
+}
+
+__global__ void bucket_k(SlotGen g, int64_t n, const int64_t* colstart, int32_t* cursor, uint64_t* keys) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
+    int32_t r, c;
+    int64_t st;
+    slot_rc(g, s, r, c, st);
+    int32_t pos = atomicAdd(&cursor[c], 1);
+    keys[colstart[c] + pos] = ((uint64_t)(uint32_t)r << 32) | (uint64_t)(uint32_t)s;
+  }
+}
+
+__device__ __forceinline__ void cmpswap(uint64_t* a, int64_t i, int64_t j) {
+  uint64_t x = a[i], y = a[j];
+  if (x > y) {
+    a[i] = y;
+    a[j] = x;
+  }
+}
+
+// Bitonic network in its "flip" form: every comparator puts the smaller key at
+// the lower index, so any length n sorts correctly when comparators that reach
+// past n are skipped (those positions behave as +infinity).  One warp.
+__device__ void warp_sort(uint64_t* a, int64_t n, int lane) {
+  if (n < 2) return;
+  int64_t npow = 1;
+  while (npow < n) npow <<= 1;
+  const int64_t half_pairs = npow >> 1;
+  for (int64_t size = 2; size <= npow; size <<= 1) {
+    const int64_t h = size >> 1;
+    for (int64_t p = lane; p < half_pairs; p += 32) {
+      int64_t blk = p / h, off = p - blk * h;
+      int64_t i = blk * size + off;
+      int64_t j = blk * size + size - 1 - off;
+      if (j < n) cmpswap(a, i, j);
+    }
+    __syncwarp();
+    for (int64_t stride = h >> 1; stride > 0; stride >>= 1) {
+      for (int64_t p = lane; p < half_pairs; p += 32) {
+        int64_t blk = p / stride, off = p - blk * stride;
+        int64_t i = blk * 2 * stride + off;
+        int64_t j = i + stride;
+        if (j < n) cmpswap(a, i, j);
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// Sort every column's keys by (row, slot) and count its distinct rows.
+__global__ void __launch_bounds__(kSortThreads) sort_cols_k(const int64_t* colstart, int64_t ncol, uint64_t* keys,
+                                                           int32_t* nnzcnt) {
+  __shared__ uint64_t sh[kSortThreads / 32][kSortCap];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t warps = (int64_t)gridDim.x * (kSortThreads / 32);
+  for (int64_t col = (int64_t)blockIdx.x * (kSortThreads / 32) + wid; col < ncol; col += warps) {
+    const int64_t b = colstart[col], n = colstart[col + 1] - b;
+    uint64_t* a;
+    if (n <= kSortCap) {
+      for (int64_t t = lane; t < n; t += 32) sh[wid][t] = keys[b + t];
+      __syncwarp();
+      a = sh[wid];
+    } else {
+      a = keys + b;  // long column: sort in place in global memory
+    }
+    warp_sort(a, n, lane);
+    // distinct rows
+    int32_t cnt = 0;
+    for (int64_t t0 = 0; t0 < n; t0 += 32) {
+      int64_t t = t0 + lane;
+      bool first = false;
+      if (t < n) first = (t == 0) || ((a[t] >> 32) != (a[t - 1] >> 32));
+      cnt += __popc(__ballot_sync(0xffffffffu, first));
+    }
+    if (n <= kSortCap)
+      for (int64_t t = lane; t < n; t += 32) keys[b + t] = a[t];
+    if (lane == 0) nnzcnt[col] = cnt;
+    __syncwarp();
+  }
+}
+
+__global__ void emit_k(SlotGen g, const int64_t* colstart, const int64_t* colptr, int64_t ncol, const uint64_t* keys,
+                       int32_t* rowval, int32_t* cptr, int32_t* contrib) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x / 32);
+  for (int64_t col = (int64_t)blockIdx.x * (blockDim.x / 32) + wid; col < ncol; col += warps) {
+    const int64_t b = colstart[col], n = colstart[col + 1] - b;
+    int64_t k = colptr[col];
+    for (int64_t t0 = 0; t0 < n; t0 += 32) {
+      int64_t t = t0 + lane;
+      bool first = false;
+      uint64_t key = 0;
+      if (t < n) {
+        key = keys[b + t];
+        first = (t == 0) || ((key >> 32) != (keys[b + t - 1] >> 32));
+        int32_t r, c;
+        int64_t st;
+        slot_rc(g, (int64_t)(key & 0xffffffffull), r, c, st);
+        contrib[b + t] = (int32_t)st;
+      }
+      unsigned m = __ballot_sync(0xffffffffu, first);
+      if (first) {
+        int64_t kk = k + __popc(m & ((1u << lane) - 1u));
+        rowval[kk] = (int32_t)(key >> 32);
+        cptr[kk] = (int32_t)(b + t);
+      }
+      k += __popc(m);
+    }
+  }
+}
+
+__global__ void set_last_k(int32_t* cptr, int64_t nnz, int64_t total) { cptr[nnz] = (int32_t)total; }
+
+int build_pattern(Ctx* c, const SlotGen& g, int64_t nrow, int64_t ncol, Pattern* P) {
+  P->release(c);
+  const int64_t M = g.total();
+  if (M >= (int64_t)0x7fffffff)
+    return fail(c, ELFEL_ERR_ARG, "too many assembled entries (%lld): the device pattern holds < 2^31", (long long)M);
+  if (nrow >= (int64_t)0x7fffffff || ncol >= (int64_t)0x7fffffff)
+    return fail(c, ELFEL_ERR_ARG, "matrix dimension >= 2^31");
+  P->nrow = nrow;
+  P->ncol = ncol;
+  P->nslots = M;
+  cudaStream_t st = c->stream;
+  DBuf<int32_t> colcnt, cursor;
+  DBuf<int64_t> colstart;
+  DBuf<uint64_t> keys;
+  DBuf<int> bad;
+  ELFEL_TRY(colcnt.alloc(c, (size_t)ncol + 1));
+  ELFEL_TRY(cursor.alloc(c, (size_t)ncol + 1));
+  ELFEL_TRY(colstart.alloc(c, (size_t)ncol + 1));
+  ELFEL_TRY(bad.alloc(c, 1));
+  ELFEL_CUDA(c, cudaMemsetAsync(colcnt.p, 0, sizeof(int32_t) * (ncol + 1), st));
+  ELFEL_CUDA(c, cudaMemsetAsync(cursor.p, 0, sizeof(int32_t) * (ncol + 1), st));
+  ELFEL_CUDA(c, cudaMemsetAsync(bad.p, 0, sizeof(int), st));
+  const unsigned gs = grid_for(M, 256, (int64_t)c->sm_count * 16);
+  if (M > 0) {
+    count_cols_k<<<gs, 256, 0, st>>>(g, M, colcnt.p, ncol, nrow, bad.p);
+    ELFEL_LAUNCH_CHECK(c);
+  }
+  int hbad = 0;
+  ELFEL_CUDA(c, cudaMemcpyAsync(&hbad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  ELFEL_CUDA(c, cudaStreamSynchronize(st));
+  if (hbad) return fail(c, ELFEL_ERR_ARG, "assembled row or column number out of range (1..%lld, 1..%lld)",
+                        (long long)nrow, (long long)ncol);
+  ELFEL_TRY(scan_counts_i32(c, colcnt.p, ncol, colstart.p));
+  ELFEL_TRY(keys.alloc(c, (size_t)(M > 0 ? M : 1)));
+  if (M > 0) {
+    bucket_k<<<gs, 256, 0, st>>>(g, M, colstart.p, cursor.p, keys.p);
+    ELFEL_LAUNCH_CHECK(c);
+  }
+  cursor.release(c);
+  // sort + distinct counts (reuse colcnt as per-column nonzero counts)
+  const unsigned gsort = grid_for(ncol, kSortThreads / 32, (int64_t)c->sm_count * 32);
+  if (ncol > 0) {
+    sort_cols_k<<<gsort, kSortThreads, 0, st>>>(colstart.p, ncol, keys.p, colcnt.p);
+    ELFEL_LAUNCH_CHECK(c);
+  }
+  ELFEL_TRY(P->colptr.alloc(c, (size_t)ncol + 1));
+  ELFEL_TRY(scan_counts_i32(c, colcnt.p, ncol, P->colptr.p));
+  int64_t nnz = 0;
+  ELFEL_CUDA(c, cudaMemcpyAsync(&nnz, P->colptr.p + ncol, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  ELFEL_CUDA(c, cudaStreamSynchronize(st));
+  P->nnz = nnz;
+  ELFEL_TRY(P->rowval.alloc(c, (size_t)(nnz > 0 ? nnz : 1)));
+  ELFEL_TRY(P->cptr.alloc(c, (size_t)nnz + 1));
+  ELFEL_TRY(P->contrib.alloc(c, (size_t)(M > 0 ? M : 1)));
+  if (ncol > 0) {
+    emit_k<<<gsort, kSortThreads, 0, st>>>(g, colstart.p, P->colptr.p, ncol, keys.p, P->rowval.p, P->cptr.p,
+                                           P->contrib.p);
+    ELFEL_LAUNCH_CHECK(c);
+  }
+  set_last_k<<<1, 1, 0, st>>>(P->cptr.p, nnz, M);
+  ELFEL_LAUNCH_CHECK(c);
+  keys.release(c);
+  colcnt.release(c);
+  colstart.release(c);
+  bad.release(c);
+  return ELFEL_OK;
+}
+
+// One thread per nonzero; its contributions are summed left to right, in the
+// order the reference's sparse() adds duplicates.
+__global__ void reduce_k(const int32_t* __restrict__ cptr, const int32_t* __restrict__ contrib,
+                         const double* __restrict__ store, int64_t nnz, double* __restrict__ out) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nnz; k += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t b = cptr[k], e = cptr[k + 1];
+    double s = store[contrib[b]];
+    for (int32_t t = b + 1; t < e; ++t) s += store[contrib[t]];
+    out[k] = s;
+  }
+}
+
+int reduce_values(Ctx* c, const Pattern& P, const double* store, double* vals_out) {
+  if (P.nnz == 0) return ELFEL_OK;
+  reduce_k<<<grid_for(P.nnz, 256, (int64_t)c->sm_count * 16), 256, 0, c->stream>>>(P.cptr.p, P.contrib.p, store,
+                                                                                   P.nnz, vals_out);
+  ELFEL_LAUNCH_CHECK(c);
+  return ELFEL_OK;
+}
+
+__global__ void to_index32_k(const int64_t* src, int64_t n, int64_t limit, int32_t* dst, int* bad) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t v = src[i];
+    if (v < 1 || v > limit) {
+      atomicExch(bad, 1);
+      dst[i] = 0;
+    } else {
+      dst[i] = (int32_t)(v - 1);
+    }
+  }
+}
+
+int to_index32(Ctx* c, const int64_t* src_host, int64_t n, int64_t limit, DBuf<int32_t>* dst, const char* what) {
+  ELFEL_TRY(dst->alloc(c, (size_t)(n > 0 ? n : 1)));
+  if (n == 0) return ELFEL_OK;
+  DBuf<int64_t> tmp;
+  DBuf<int> bad;
+  ELFEL_TRY(tmp.alloc(c, (size_t)n));
+  ELFEL_TRY(bad.alloc(c, 1));
+  ELFEL_CUDA(c, cudaMemsetAsync(bad.p, 0, sizeof(int), c->stream));
+  ELFEL_CUDA(c, cudaMemcpyAsync(tmp.p, src_host, sizeof(int64_t) * n, cudaMemcpyHostToDevice, c->stream));
+  to_index32_k<<<grid_for(n, 256, (int64_t)c->sm_count * 16), 256, 0, c->stream>>>(tmp.p, n, limit, dst->p, bad.p);
+  ELFEL_LAUNCH_CHECK(c);
+  int hbad = 0;
+  ELFEL_CUDA(c, cudaMemcpyAsync(&hbad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+  tmp.release(c);
+  bad.release(c);
+  if (hbad) return fail(c, ELFEL_ERR_ARG, "%s: entry outside 1..%lld", what, (long long)limit);
+  return ELFEL_OK;
+}
+
+}  // namespace elfel

@@ -1,0 +1,980 @@
+// Device solve of the lifted free-free system of the reference's solve!
+// (Elfel.jl test/test_heat.jl:73-76):
+//     T[1:nu] = K[1:nu,1:nu] \ (F[1:nu] - (K*T)[1:nu])
+// The free DOFs are numbered first (numberdofs!, src/FESpaces.jl:250-259), so
+// the free-free block is the leading nu x nu block of K.  The direct solve of
+// the reference is replaced by
+//   ELFEL_PCG64        Jacobi-preconditioned CG, FP64 throughout;
+//   ELFEL_PCG32_IR     Jacobi CG on an FP32 copy of K with FP64 residual
+//                      replacement ("reliable updates", Sleijpen & van der
+//                      Vorst 1996; used for mixed precision by Clark et al.
+//                      2010): the solution is accumulated in FP64, and each
+//                      time the FP32 recurrence residual has dropped by a
+//                      factor delta the true residual b - K x is recomputed in
+//                      FP64 and replaces it; convergence is judged on that
+//                      FP64 residual;
+//   ELFEL_MINRES64     MINRES (Paige & Saunders 1975) with a symmetric positive
+//                      diagonal preconditioner: |K_ii| on rows with a diagonal,
+//                      the pressure mass-matrix diagonal on Stokes pressure rows;
+//   ELFEL_MINRES32_IR  the same MINRES in FP32 inside FP64 iterative refinement.
+// All reductions are deterministic (per-block partials summed in block order).
+// Iterations are launched as CUDA graphs of kGraphIters iterations; kernels of
+// a finished (or paused) iteration exit at once, so the graph needs no host
+// decision per iteration.
+#include <math.h>
+
+#include <chrono>
+
+#include "solve.cuh"
+
+namespace elfel {
+
+constexpr int kBlk = 256;
+constexpr int kGraphIters = 16;
+
+// device scalar slots
+enum {
+  S_PQ = 0, S_RZ, S_RR, S_BETA, S_BN2, S_TOL2, S_RMAX, S_DELTA,
+  // MINRES
+  S_GAM, S_GAMP, S_GAMN, S_DEL, S_C, S_CP, S_S, S_SP, S_ETA, S_ETA0, S_A1, S_A2, S_A3, S_CN,
+  S_COUNT
+};
+// device int flags
+enum { F_DONE = 0, F_RU, F_ITER, F_MAXIT, F_ROT, F_CONV, F_COUNT };
+
+struct Red4 {
+  double* partials;  // nblocks x 4
+  unsigned* ticket;
+};
+
+struct Csr {
+  int64_t nrows = 0, nnz = 0;
+  DBuf<int32_t> rowptr, col, map;
+  DBuf<double> v64;
+  DBuf<float> v32;
+  void release(Ctx* c) {
+    rowptr.release(c); col.release(c); map.release(c); v64.release(c); v32.release(c);
+    nrows = nnz = 0;
+  }
+};
+
+struct SolverData {
+  int64_t nu = -1;
+  const void* pattern_id = nullptr;
+  int64_t pattern_nnz = -1;
+  uint64_t values_version = ~0ull;
+  int group = 4;  // lanes per row in the SpMV
+  Csr ff, fd;
+  DBuf<double> dinv64;
+  DBuf<float> dinv32;
+  DBuf<double> b64, x64, r64, T64, y64;
+  DBuf<double> v64[3], w64[3], z64, p64, q64;
+  DBuf<float> r32, p32, q32, z32, xa32;
+  DBuf<float> v32[3], w32[3], zz32, b32, x32;
+  DBuf<double> scal;
+  DBuf<int> flags;
+  DBuf<double> red;  // 3 reduction areas
+  DBuf<unsigned> tickets;
+  cudaGraphExec_t g_pcg64 = nullptr, g_pcg32 = nullptr, g_minres64 = nullptr, g_minres32 = nullptr;
+  void release(Ctx* c) {
+    ff.release(c); fd.release(c); dinv64.release(c); dinv32.release(c);
+    b64.release(c); x64.release(c); r64.release(c); T64.release(c); y64.release(c);
+    for (int i = 0; i < 3; ++i) { v64[i].release(c); w64[i].release(c); v32[i].release(c); w32[i].release(c); }
+    z64.release(c); p64.release(c); q64.release(c);
+    r32.release(c); p32.release(c); q32.release(c); z32.release(c); xa32.release(c); zz32.release(c);
+    b32.release(c); x32.release(c);
+    scal.release(c); flags.release(c); red.release(c); tickets.release(c);
+    for (cudaGraphExec_t* g : {&g_pcg64, &g_pcg32, &g_minres64, &g_minres32})
+      if (*g) { cudaGraphExecDestroy(*g); *g = nullptr; }
+  }
+};
+
+void solver_release(Ctx* c, elfel_sysmat* m) {
+  if (m->solver) {
+    m->solver->release(c);
+    delete m->solver;
+    m->solver = nullptr;
+  }
+}
+
+// ------------------------------------------------------------------ reductions
+// Sum NV per-thread values over the grid; the last block gets the totals.
+template <int NV>
+__device__ __forceinline__ bool grid_sums(double (&v)[NV], Red4 red, double (&tot)[NV]) {
+  __shared__ double sh[NV][kBlk / 32];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int a = 0; a < NV; ++a) {
+    double x = v[a];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[a][wid] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int a = 0; a < NV; ++a) {
+      double s = 0.0;
+#pragma unroll
+      for (int w = 0; w < kBlk / 32; ++w) s += sh[a][w];
+      red.partials[blockIdx.x * 4 + a] = s;
+    }
+    __threadfence();
+    unsigned t = atomicAdd(red.ticket, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    volatile double* pp = red.partials;
+#pragma unroll
+    for (int a = 0; a < NV; ++a) {
+      double s = 0.0;
+      for (unsigned b = 0; b < gridDim.x; ++b) s += pp[b * 4 + a];
+      tot[a] = s;
+    }
+    *red.ticket = 0u;
+  }
+  return threadIdx.x == 0;
+}
+
+// ------------------------------------------------------------------ SpMV
+// y = A x on rows [0, n); G lanes per row; returns per-thread partial of y.w
+// (w = x when wdot == nullptr).  Row loop is warp-uniform so the group
+// shuffles always see the whole warp.
+template <typename T, int G>
+__device__ __forceinline__ double spmv_rows(int64_t n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                            const T* __restrict__ v, const T* __restrict__ x, T* __restrict__ y,
+                                            const T* __restrict__ wdot) {
+  constexpr int RPW = 32 / G;  // rows per warp step
+  const int lane = threadIdx.x & 31;
+  const int g = lane / G, lg = lane % G;
+  const int64_t warp = ((int64_t)blockIdx.x * kBlk + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * kBlk) >> 5;
+  T part = 0;
+  for (int64_t r0 = warp * RPW; r0 < n; r0 += nwarps * RPW) {
+    const int64_t r = r0 + g;
+    T s = 0;
+    if (r < n) {
+      const int32_t b = rp[r], e = rp[r + 1];
+      for (int32_t k = b + lg; k < e; k += G) s += v[k] * __ldg(x + ci[k]);
+    }
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
+    if (r < n && lg == 0) {
+      y[r] = s;
+      part += s * (wdot ? wdot[r] : x[r]);
+    }
+  }
+  return (double)part;
+}
+
+template <typename T, int G>
+__global__ void __launch_bounds__(kBlk) spmv_dot_k(int64_t n, const int32_t* __restrict__ rp,
+                                                  const int32_t* __restrict__ ci, const T* __restrict__ v,
+                                                  const T* __restrict__ x, T* __restrict__ y, Red4 red,
+                                                  double* scal, int slot, const int* flags) {
+  if (flags[F_DONE] || flags[F_RU]) {
+    // F_RU = 1: requested by the previous update; p has been advanced once by
+    // cg_p_k since.  Mark it 2 so the rest of the graph skips until the host
+    // has replaced the residual.
+    if (flags[F_RU] == 1 && blockIdx.x == 0 && threadIdx.x == 0) ((volatile int*)flags)[F_RU] = 2;
+    return;
+  }
+  double p[1] = {spmv_rows<T, G>(n, rp, ci, v, x, y, nullptr)};
+  double t[1];
+  if (grid_sums<1>(p, red, t)) scal[slot] = t[0];
+}
+
+// r = b - A_ff x - A_fd t (FP64), rr partial; used for the lifted rhs and
+// for the true residual.  t may be null (no data columns).
+template <int G>
+__global__ void __launch_bounds__(kBlk) resid64_k(int64_t n, const int32_t* __restrict__ rp,
+                                                 const int32_t* __restrict__ ci, const double* __restrict__ v,
+                                                 const double* __restrict__ x, const int32_t* __restrict__ rpd,
+                                                 const int32_t* __restrict__ cid, const double* __restrict__ vd,
+                                                 const double* __restrict__ t, int64_t nu,
+                                                 const double* __restrict__ b, double* __restrict__ r, Red4 red,
+                                                 double* scal, int slot) {
+  constexpr int RPW = 32 / G;
+  const int lane = threadIdx.x & 31;
+  const int g = lane / G, lg = lane % G;
+  const int64_t warp = ((int64_t)blockIdx.x * kBlk + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * kBlk) >> 5;
+  double part = 0.0;
+  for (int64_t r0 = warp * RPW; r0 < n; r0 += nwarps * RPW) {
+    const int64_t row = r0 + g;
+    double s = 0.0;
+    if (row < n) {
+      const int32_t bb = rp[row], e = rp[row + 1];
+      for (int32_t k = bb + lg; k < e; k += G) s += v[k] * x[ci[k]];
+      if (t) {
+        const int32_t bd = rpd[row], ed = rpd[row + 1];
+        for (int32_t k = bd + lg; k < ed; k += G) s += vd[k] * t[cid[k] - nu];
+      }
+    }
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
+    if (row < n && lg == 0) {
+      const double rv = b[row] - s;
+      r[row] = rv;
+      part += rv * rv;
+    }
+  }
+  double p[1] = {part};
+  double tt[1];
+  if (grid_sums<1>(p, red, tt)) scal[slot] = tt[0];
+}
+
+// ------------------------------------------------------------------ PCG
+template <typename T, bool ACC>
+__global__ void __launch_bounds__(kBlk) cg_update_k(int64_t n, T* __restrict__ x, T* __restrict__ r,
+                                                   const T* __restrict__ p, const T* __restrict__ q,
+                                                   T* __restrict__ z, const T* __restrict__ dinv, Red4 red,
+                                                   double* scal, int* flags) {
+  if (flags[F_DONE] || flags[F_RU]) return;
+  const T alpha = (T)(scal[S_RZ] / scal[S_PQ]);
+  T prz = 0, prr = 0;
+  for (int64_t i = blockIdx.x * (int64_t)kBlk + threadIdx.x; i < n; i += (int64_t)gridDim.x * kBlk) {
+    const T pi = p[i];
+    x[i] += alpha * pi;
+    const T ri = r[i] - alpha * q[i];
+    r[i] = ri;
+    const T zi = dinv[i] * ri;
+    z[i] = zi;
+    prz += ri * zi;
+    prr += ri * ri;
+  }
+  double v[2] = {(double)prz, (double)prr};
+  double t[2];
+  if (grid_sums<2>(v, red, t)) {
+    const double rz = t[0], rr = t[1];
+    scal[S_BETA] = rz / scal[S_RZ];
+    scal[S_RZ] = rz;
+    scal[S_RR] = rr;
+    const int it = ++flags[F_ITER];
+    const bool conv = rr <= scal[S_TOL2] * scal[S_BN2];
+    if (!ACC) {
+      if (conv || it >= flags[F_MAXIT]) {
+        flags[F_DONE] = 1;
+        flags[F_CONV] = conv ? 1 : 0;
+      }
+    } else {
+      // FP32 recurrence: ask for an FP64 residual replacement when the
+      // residual dropped by delta since the last one, or looks converged.
+      const double rn = sqrt(rr);
+      if (rn > scal[S_RMAX]) scal[S_RMAX] = rn;
+      if (conv || it >= flags[F_MAXIT] || rn < scal[S_DELTA] * scal[S_RMAX]) flags[F_RU] = 1;
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBlk) cg_p_k(int64_t n, T* __restrict__ p, const T* __restrict__ z,
+                                              const double* scal, const int* flags) {
+  // runs once more after a replacement request (F_RU = 1), so that p is the
+  // recurrence's next direction when the residual gets replaced
+  if (flags[F_DONE] || flags[F_RU] == 2) return;
+  const T beta = (T)scal[S_BETA];
+  for (int64_t i = blockIdx.x * (int64_t)kBlk + threadIdx.x; i < n; i += (int64_t)gridDim.x * kBlk)
+    p[i] = z[i] + beta * p[i];
+}
+
+// z = dinv r, p = z, rz = r.z, and the initial scalars.
+template <typename T>
+__global__ void __launch_bounds__(kBlk) cg_start_k(int64_t n, const T* __restrict__ r, T* __restrict__ z,
+                                                  T* __restrict__ p, const T* __restrict__ dinv, Red4 red,
+                                                  double* scal, int* flags, int set_p) {
+  T prz = 0;
+  for (int64_t i = blockIdx.x * (int64_t)kBlk + threadIdx.x; i < n; i += (int64_t)gridDim.x * kBlk) {
+    const T zi = dinv[i] * r[i];
+    z[i] = zi;
+    if (set_p) p[i] = zi;
+    prz += r[i] * zi;
+  }
+  double v[1] = {(double)prz};
+  double t[1];
+  if (grid_sums<1>(v, red, t)) {
+    scal[S_RZ] = t[0];
+    flags[F_RU] = 0;
+  }
+}
+
+// x64 += xacc, xacc = 0
+__global__ void fold_k(int64_t n, double* __restrict__ x, float* __restrict__ xa) {
+  for (int64_t i = blockIdx.x * (int64_t)kBlk + threadIdx.x; i < n; i += (int64_t)gridDim.x * kBlk) {
+    x[i] += (double)xa[i];
+    xa[i] = 0.0f;
+  }
+}
+
+__global__ void demote_k(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+  for (int64_t i = blockIdx.x * (int64_t)kBlk + threadIdx.x; i < n; i += (int64_t)gridDim.x * kBlk)
+    b[i] = (float)a[i];
+}
+
+__global__ void add_scaled_k(int64_t n, double* __restrict__ x, const float* __restrict__ d) {
+  for (int64_t i = blockIdx.x * (int64_t)kBlk + threadIdx.x; i < n; i += (int64_t)gridDim.x * kBlk)
+    x[i] += (double)d[i];
+}
+
+// ------------------------------------------------------------------ MINRES
+// Preconditioned MINRES with diagonal M (minv = M^-1); three-term buffers are
+// addressed by a rotation counter in flags[F_ROT].
+//   step 1 (spmv): q = A z_j,  delta = q.z_j
+//   step 2 (vec):  v_{j+1} = q - (delta/gam) v_j - (gam/gamp) v_{j-1};
+//                  z_{j+1} = minv v_{j+1}; gamn^2 = z_{j+1}.v_{j+1};
+//                  last block: Givens rotation scalars
+//   step 3 (upd):  w_{j+1} = (z_j - a3 w_{j-1} - a2 w_j)/a1;  x += c_{j+1} eta w_{j+1}
+// where z_j denotes the normalised z (z/gam), stored in zbuf[rot].
+template <typename T, int G>
+__global__ void __launch_bounds__(kBlk) mr_spmv_k(int64_t n, const int32_t* __restrict__ rp,
+                                                 const int32_t* __restrict__ ci, const T* __restrict__ v,
+                                                 T* const* zb, T* __restrict__ q, Red4 red, double* scal,
+                                                 const int* flags) {
+  if (flags[F_DONE]) return;
+  const int rot = flags[F_ROT];
+  const T* z = zb[rot % 3];
+  double p[1] = {spmv_rows<T, G>(n, rp, ci, v, z, q, nullptr)};
+  double t[1];
+  if (grid_sums<1>(p, red, t)) scal[S_DEL] = t[0];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBlk) mr_vec_k(int64_t n, const T* __restrict__ q, T* const* vb, T* const* zb,
+                                                const T* __restrict__ minv, Red4 red, double* scal, int* flags) {
+  if (flags[F_DONE]) return;
+  const int rot = flags[F_ROT];
+  T* vj = vb[rot % 3];
+  T* vjm = vb[(rot + 2) % 3];
+  T* vn = vb[(rot + 1) % 3];
+  T* zn = zb[(rot + 1) % 3];
+  const double gam = scal[S_GAM], gamp = scal[S_GAMP];
+  const T a = (T)(scal[S_DEL] / gam), bcoef = (T)(gamp > 0.0 ? gam / gamp : 0.0);
+  T pz = 0;
+  for (int64_t i = blockIdx.x * (int64_t)kBlk + threadIdx.x; i < n; i += (int64_t)gridDim.x * kBlk) {
+    const T vv = q[i] - a * vj[i] - bcoef * vjm[i];
+    vn[i] = vv;
+    const T zz = minv[i] * vv;
+    zn[i] = zz;
+    pz += zz * vv;
+  }
+  double v[1] = {(double)pz};
+  double t[1];
+  if (grid_sums<1>(v, red, t)) {
+    const double gamn = sqrt(fmax(t[0], 0.0));
+    const double delta = scal[S_DEL];
+    const double c = scal[S_C], cp = scal[S_CP], s = scal[S_S], sp = scal[S_SP], g = scal[S_GAM];
+    const double a0 = c * delta - cp * s * g;
+    const double a1 = sqrt(a0 * a0 + gamn * gamn);
+    const double a2 = s * delta + cp * c * g;
+    const double a3 = sp * g;
+    const double cn = a0 / a1, sn = gamn / a1;
+    scal[S_A1] = a1;
+    scal[S_A2] = a2;
+    scal[S_A3] = a3;
+    scal[S_CN] = cn;
+    scal[S_CP] = c;
+    scal[S_C] = cn;
+    scal[S_SP] = s;
+    scal[S_S] = sn;
+    scal[S_GAMP] = g;
+    scal[S_GAMN] = gamn;
+    (void)sp;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBlk) mr_upd_k(int64_t n, T* const* zb, T* const* wb, T* __restrict__ x,
+                                                double* scal, int* flags) {
+  if (flags[F_DONE]) return;
+  const int rot = flags[F_ROT];
+  const T* z = zb[rot % 3];
+  T* zn = zb[(rot + 1) % 3];
+  const T* wj = wb[rot % 3];
+  const T* wjm = wb[(rot + 2) % 3];
+  T* wn = wb[(rot + 1) % 3];
+  const double a1 = scal[S_A1];
+  const T a2 = (T)scal[S_A2], a3 = (T)scal[S_A3];
+  const T ia1 = (T)(1.0 / a1);
+  const T ce = (T)(scal[S_CN] * scal[S_ETA]);
+  const double gamn = scal[S_GAMN];
+  const T ig = (T)(gamn > 0.0 ? 1.0 / gamn : 0.0);
+  for (int64_t i = blockIdx.x * (int64_t)kBlk + threadIdx.x; i < n; i += (int64_t)gridDim.x * kBlk) {
+    const T w = (z[i] - a3 * wjm[i] - a2 * wj[i]) * ia1;
+    wn[i] = w;
+    x[i] += ce * w;
+    zn[i] *= ig;  // normalise the next z for the next step
+  }
+}
+
+// Advance the MINRES scalars once all blocks of mr_upd_k are done.
+__global__ void mr_tail_k(double* scal, int* flags) {
+  if (flags[F_DONE]) return;
+  scal[S_ETA] = -scal[S_S] * scal[S_ETA];
+  scal[S_GAM] = scal[S_GAMN];
+  flags[F_ROT] = flags[F_ROT] + 1;
+  const int it = ++flags[F_ITER];
+  const bool conv = fabs(scal[S_ETA]) <= sqrt(scal[S_TOL2]) * scal[S_ETA0];
+  if (conv || it >= flags[F_MAXIT] || scal[S_GAMN] == 0.0) {
+    flags[F_DONE] = 1;
+    flags[F_CONV] = (conv || scal[S_GAMN] == 0.0) ? 1 : 0;
+  }
+}
+
+// MINRES start: v1 = r (in vb[0]), z1 = minv r, gam = sqrt(z.v), z normalised.
+template <typename T>
+__global__ void __launch_bounds__(kBlk) mr_start_k(int64_t n, const T* __restrict__ r, T* const* vb, T* const* zb,
+                                                  T* const* wb, const T* __restrict__ minv, T* __restrict__ x,
+                                                  Red4 red, double* scal, int* flags) {
+  T pz = 0;
+  for (int64_t i = blockIdx.x * (int64_t)kBlk + threadIdx.x; i < n; i += (int64_t)gridDim.x * kBlk) {
+    const T ri = r[i];
+    vb[0][i] = ri;
+    vb[1][i] = 0;
+    vb[2][i] = 0;
+    wb[0][i] = 0;
+    wb[1][i] = 0;
+    wb[2][i] = 0;
+    const T zi = minv[i] * ri;
+    zb[0][i] = zi;
+    pz += zi * ri;
+    x[i] = 0;
+  }
+  double v[1] = {(double)pz};
+  double t[1];
+  if (grid_sums<1>(v, red, t)) {
+    const double g = sqrt(fmax(t[0], 0.0));
+    scal[S_GAM] = g;
+    scal[S_GAMP] = 0.0;
+    scal[S_ETA] = g;
+    scal[S_ETA0] = g;
+    scal[S_C] = 1.0;
+    scal[S_CP] = 1.0;
+    scal[S_S] = 0.0;
+    scal[S_SP] = 0.0;
+    flags[F_ROT] = 0;
+    flags[F_ITER] = 0;
+    flags[F_DONE] = g == 0.0 ? 1 : 0;
+    flags[F_CONV] = g == 0.0 ? 1 : 0;
+  }
+}
+
+template <typename T>
+__global__ void scale_k(int64_t n, T* const* zb, const double* scal) {
+  const double g = scal[S_GAM];
+  const T ig = (T)(g > 0.0 ? 1.0 / g : 0.0);
+  for (int64_t i = blockIdx.x * (int64_t)kBlk + threadIdx.x; i < n; i += (int64_t)gridDim.x * kBlk) zb[0][i] *= ig;
+}
+
+// ------------------------------------------------------------------ setup
+__global__ void split_count_k(int64_t nu, const int64_t* rowptr, const int32_t* col, int32_t* nff, int32_t* nfd) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nu; r += (int64_t)gridDim.x * blockDim.x) {
+    int32_t a = 0, b = 0;
+    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) (col[k] < nu) ? ++a : ++b;
+    nff[r] = a;
+    nfd[r] = b;
+  }
+}
+
+__global__ void split_copy_k(int64_t nu, const int64_t* rowptr, const int32_t* col, const int32_t* cptr,
+                             const int32_t* contrib, const int64_t* pff, const int64_t* pfd, int32_t* cff,
+                             int32_t* mff, int32_t* cfd, int32_t* mfd) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nu; r += (int64_t)gridDim.x * blockDim.x) {
+    int64_t a = pff[r], b = pfd[r];
+    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) {
+      const int32_t cc = col[k];
+      const int32_t src = contrib[cptr[k]];
+      if (cc < nu) { cff[a] = cc; mff[a] = src; ++a; }
+      else { cfd[b] = cc; mfd[b] = src; ++b; }
+    }
+  }
+}
+
+__global__ void col_of_k(const int64_t* colptr, int64_t ncol, int32_t* colof) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < ncol; j += (int64_t)gridDim.x * blockDim.x)
+    for (int64_t k = colptr[j]; k < colptr[j + 1]; ++k) colof[k] = (int32_t)j;
+}
+
+__global__ void to32_k(int64_t n, const int64_t* a, int32_t* b) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (int32_t)a[i];
+}
+
+__global__ void gather_vals_k(int64_t n, const int32_t* map, const double* src, double* d64, float* d32) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = src[map[i]];
+    d64[i] = v;
+    if (d32) d32[i] = (float)v;
+  }
+}
+
+// Preconditioner diagonal: 1/K_ii where K_ii != 0, else 1/aux_i where aux_i > 0
+// (pressure mass diagonal), else 1.  abs_diag selects |K_ii| (MINRES needs SPD M).
+__global__ void diag_k(int64_t nu, const int32_t* rp, const int32_t* ci, const double* v, const double* aux,
+                       int abs_diag, double* d64, float* d32) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nu; r += (int64_t)gridDim.x * blockDim.x) {
+    double d = 0.0;
+    int32_t lo = rp[r], hi = rp[r + 1] - 1;
+    while (lo <= hi) {
+      int32_t mid = (lo + hi) >> 1;
+      if (ci[mid] == r) { d = v[mid]; break; }
+      if (ci[mid] < r) lo = mid + 1; else hi = mid - 1;
+    }
+    if (abs_diag) d = fabs(d);
+    double inv;
+    if (d != 0.0) inv = 1.0 / d;
+    else if (aux && aux[r] > 0.0) inv = 1.0 / aux[r];
+    else inv = 1.0;
+    d64[r] = inv;
+    d32[r] = (float)inv;
+  }
+}
+
+static int pick_group(int64_t nnz, int64_t n) {
+  const double avg = n > 0 ? (double)nnz / (double)n : 0.0;
+  if (avg <= 3) return 2;
+  if (avg <= 10) return 4;
+  if (avg <= 24) return 8;
+  if (avg <= 48) return 16;
+  return 32;
+}
+
+// Reduction-carrying kernels use at most kSMs*4 blocks (the partials area size).
+static unsigned vec_grid(Ctx* c, int64_t n) {
+  (void)c;
+  return grid_for(n, kBlk, (int64_t)kSMs * 4);
+}
+
+static Red4 red_area(SolverData* S, int k) {
+  Red4 r;
+  r.partials = S->red.p + (size_t)k * kSMs * 4 * 4;
+  r.ticket = S->tickets.p + k;
+  return r;
+}
+
+static int build_solver(elfel_sysmat* m, int64_t nu) {
+  Ctx* c = &m->h->c;
+  if (!m->solver) m->solver = new SolverData();
+  SolverData* S = m->solver;
+  if (S->nu == nu && S->pattern_id == (const void*)m->P.rowval.p && S->pattern_nnz == m->P.nnz) return ELFEL_OK;
+  S->release(c);
+  const int64_t n = m->nrow;
+  // Full CSR of K through the pattern builder: slots = CSC nonzeros, with
+  // row and column roles swapped so that the CSC of K^T (= CSR of K) comes out.
+  DBuf<int32_t> colof;
+  ELFEL_TRY(colof.alloc(c, (size_t)(m->P.nnz > 0 ? m->P.nnz : 1)));
+  if (m->P.ncol > 0) {
+    col_of_k<<<grid_for(m->P.ncol, 256, (int64_t)c->sm_count * 16), 256, 0, c->stream>>>(m->P.colptr.p, m->P.ncol,
+                                                                                        colof.p);
+    ELFEL_LAUNCH_CHECK(c);
+  }
+  SlotGen g;
+  g.I = colof.p;        // "row" of the transposed matrix = column of K
+  g.J = m->P.rowval.p;  // "column" of the transposed matrix = row of K
+  g.ncoo = m->P.nnz;
+  Pattern R;
+  ELFEL_TRY(build_pattern(c, g, m->ncol, m->nrow, &R));
+  colof.release(c);
+  // split the first nu rows into free (col < nu) and data (col >= nu) parts
+  DBuf<int32_t> nff, nfd;
+  DBuf<int64_t> pff, pfd;
+  ELFEL_TRY(nff.alloc(c, (size_t)nu + 1));
+  ELFEL_TRY(nfd.alloc(c, (size_t)nu + 1));
+  ELFEL_TRY(pff.alloc(c, (size_t)nu + 1));
+  ELFEL_TRY(pfd.alloc(c, (size_t)nu + 1));
+  const unsigned gr = grid_for(nu, 256, (int64_t)c->sm_count * 16);
+  if (nu > 0) {
+    split_count_k<<<gr, 256, 0, c->stream>>>(nu, R.colptr.p, R.rowval.p, nff.p, nfd.p);
+    ELFEL_LAUNCH_CHECK(c);
+  }
+  ELFEL_TRY(scan_counts_i32(c, nff.p, nu, pff.p));
+  ELFEL_TRY(scan_counts_i32(c, nfd.p, nu, pfd.p));
+  int64_t tff = 0, tfd = 0;
+  ELFEL_CUDA(c, cudaMemcpyAsync(&tff, pff.p + nu, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+  ELFEL_CUDA(c, cudaMemcpyAsync(&tfd, pfd.p + nu, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+  ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+  S->ff.nrows = S->fd.nrows = nu;
+  S->ff.nnz = tff;
+  S->fd.nnz = tfd;
+  ELFEL_TRY(S->ff.rowptr.alloc(c, (size_t)nu + 1));
+  ELFEL_TRY(S->fd.rowptr.alloc(c, (size_t)nu + 1));
+  ELFEL_TRY(S->ff.col.alloc(c, (size_t)(tff > 0 ? tff : 1)));
+  ELFEL_TRY(S->ff.map.alloc(c, (size_t)(tff > 0 ? tff : 1)));
+  ELFEL_TRY(S->fd.col.alloc(c, (size_t)(tfd > 0 ? tfd : 1)));
+  ELFEL_TRY(S->fd.map.alloc(c, (size_t)(tfd > 0 ? tfd : 1)));
+  ELFEL_TRY(S->ff.v64.alloc(c, (size_t)(tff > 0 ? tff : 1)));
+  ELFEL_TRY(S->ff.v32.alloc(c, (size_t)(tff > 0 ? tff : 1)));
+  ELFEL_TRY(S->fd.v64.alloc(c, (size_t)(tfd > 0 ? tfd : 1)));
+  to32_k<<<grid_for(nu + 1, 256), 256, 0, c->stream>>>(nu + 1, pff.p, S->ff.rowptr.p);
+  to32_k<<<grid_for(nu + 1, 256), 256, 0, c->stream>>>(nu + 1, pfd.p, S->fd.rowptr.p);
+  if (nu > 0)
+    split_copy_k<<<gr, 256, 0, c->stream>>>(nu, R.colptr.p, R.rowval.p, R.cptr.p, R.contrib.p, pff.p, pfd.p,
+                                            S->ff.col.p, S->ff.map.p, S->fd.col.p, S->fd.map.p);
+  ELFEL_LAUNCH_CHECK(c);
+  R.release(c);
+  nff.release(c); nfd.release(c); pff.release(c); pfd.release(c);
+  const size_t vn = (size_t)(nu > 0 ? nu : 1);
+  ELFEL_TRY(S->dinv64.alloc(c, vn));
+  ELFEL_TRY(S->dinv32.alloc(c, vn));
+  for (DBuf<double>* b : {&S->b64, &S->x64, &S->r64, &S->z64, &S->p64, &S->q64, &S->y64}) ELFEL_TRY(b->alloc(c, vn));
+  for (DBuf<float>* b : {&S->r32, &S->p32, &S->q32, &S->z32, &S->xa32, &S->zz32, &S->b32, &S->x32})
+    ELFEL_TRY(b->alloc(c, vn));
+  ELFEL_TRY(S->T64.alloc(c, (size_t)(n > 0 ? n : 1)));
+  ELFEL_TRY(S->scal.alloc(c, S_COUNT));
+  ELFEL_TRY(S->flags.alloc(c, F_COUNT));
+  ELFEL_TRY(S->red.alloc(c, (size_t)3 * kSMs * 4 * 4));
+  ELFEL_TRY(S->tickets.alloc(c, 4));
+  ELFEL_CUDA(c, cudaMemsetAsync(S->tickets.p, 0, sizeof(unsigned) * 4, c->stream));
+  ELFEL_CUDA(c, cudaMemsetAsync(S->scal.p, 0, sizeof(double) * S_COUNT, c->stream));
+  ELFEL_CUDA(c, cudaMemsetAsync(S->flags.p, 0, sizeof(int) * F_COUNT, c->stream));
+  S->group = pick_group(tff, nu);
+  S->nu = nu;
+  S->pattern_id = m->P.rowval.p;
+  S->pattern_nnz = m->P.nnz;
+  S->values_version = ~0ull;
+  ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+  return ELFEL_OK;
+}
+
+static int refresh_values(elfel_sysmat* m, int abs_diag) {
+  Ctx* c = &m->h->c;
+  SolverData* S = m->solver;
+  const int64_t nu = S->nu;
+  if (S->ff.nnz)
+    gather_vals_k<<<grid_for(S->ff.nnz, 256, (int64_t)c->sm_count * 16), 256, 0, c->stream>>>(
+        S->ff.nnz, S->ff.map.p, m->vals.p, S->ff.v64.p, S->ff.v32.p);
+  if (S->fd.nnz)
+    gather_vals_k<<<grid_for(S->fd.nnz, 256, (int64_t)c->sm_count * 16), 256, 0, c->stream>>>(
+        S->fd.nnz, S->fd.map.p, m->vals.p, S->fd.v64.p, nullptr);
+  const double* aux = (m->fused && m->F.physics == ELFEL_STOKES) ? m->F.pmass_diag.p : nullptr;
+  if (nu > 0)
+    diag_k<<<grid_for(nu, 256, (int64_t)c->sm_count * 16), 256, 0, c->stream>>>(
+        nu, S->ff.rowptr.p, S->ff.col.p, S->ff.v64.p, aux, abs_diag, S->dinv64.p, S->dinv32.p);
+  ELFEL_LAUNCH_CHECK(c);
+  S->values_version = m->values_version;
+  return ELFEL_OK;
+}
+
+// Launch helpers dispatching on the group size.
+template <typename T>
+static void launch_spmv_dot(Ctx* c, SolverData* S, const T* v, const T* x, T* y, Red4 red, int slot) {
+  const unsigned grid = vec_grid(c, S->nu * S->group);
+  const int64_t n = S->nu;
+  const int32_t *rp = S->ff.rowptr.p, *ci = S->ff.col.p;
+  double* sc = S->scal.p;
+  const int* fl = S->flags.p;
+  switch (S->group) {
+    case 2: spmv_dot_k<T, 2><<<grid, kBlk, 0, c->stream>>>(n, rp, ci, v, x, y, red, sc, slot, fl); break;
+    case 4: spmv_dot_k<T, 4><<<grid, kBlk, 0, c->stream>>>(n, rp, ci, v, x, y, red, sc, slot, fl); break;
+    case 8: spmv_dot_k<T, 8><<<grid, kBlk, 0, c->stream>>>(n, rp, ci, v, x, y, red, sc, slot, fl); break;
+    case 16: spmv_dot_k<T, 16><<<grid, kBlk, 0, c->stream>>>(n, rp, ci, v, x, y, red, sc, slot, fl); break;
+    default: spmv_dot_k<T, 32><<<grid, kBlk, 0, c->stream>>>(n, rp, ci, v, x, y, red, sc, slot, fl); break;
+  }
+}
+
+template <typename T>
+static void launch_mr_spmv(Ctx* c, SolverData* S, const T* v, T* const* zb, T* q, Red4 red) {
+  const unsigned grid = vec_grid(c, S->nu * S->group);
+  const int64_t n = S->nu;
+  const int32_t *rp = S->ff.rowptr.p, *ci = S->ff.col.p;
+  double* sc = S->scal.p;
+  const int* fl = S->flags.p;
+  switch (S->group) {
+    case 2: mr_spmv_k<T, 2><<<grid, kBlk, 0, c->stream>>>(n, rp, ci, v, zb, q, red, sc, fl); break;
+    case 4: mr_spmv_k<T, 4><<<grid, kBlk, 0, c->stream>>>(n, rp, ci, v, zb, q, red, sc, fl); break;
+    case 8: mr_spmv_k<T, 8><<<grid, kBlk, 0, c->stream>>>(n, rp, ci, v, zb, q, red, sc, fl); break;
+    case 16: mr_spmv_k<T, 16><<<grid, kBlk, 0, c->stream>>>(n, rp, ci, v, zb, q, red, sc, fl); break;
+    default: mr_spmv_k<T, 32><<<grid, kBlk, 0, c->stream>>>(n, rp, ci, v, zb, q, red, sc, fl); break;
+  }
+}
+
+// r = b - A x (with the data-column part when t != null); scal[slot] = r.r
+static int launch_resid(Ctx* c, SolverData* S, const double* x, const double* t, const double* b, double* r,
+                        Red4 red, int slot) {
+  const unsigned grid = vec_grid(c, S->nu * S->group);
+  const int64_t n = S->nu;
+  const Csr &A = S->ff, &D = S->fd;
+#define RES_ARGS                                                                                                  \
+  n, A.rowptr.p, A.col.p, A.v64.p, x, D.rowptr.p, D.col.p, D.v64.p, t, S->nu, b, r, red, S->scal.p, slot
+  switch (S->group) {
+    case 2: resid64_k<2><<<grid, kBlk, 0, c->stream>>>(RES_ARGS); break;
+    case 4: resid64_k<4><<<grid, kBlk, 0, c->stream>>>(RES_ARGS); break;
+    case 8: resid64_k<8><<<grid, kBlk, 0, c->stream>>>(RES_ARGS); break;
+    case 16: resid64_k<16><<<grid, kBlk, 0, c->stream>>>(RES_ARGS); break;
+    default: resid64_k<32><<<grid, kBlk, 0, c->stream>>>(RES_ARGS); break;
+  }
+#undef RES_ARGS
+  ELFEL_LAUNCH_CHECK(c);
+  return ELFEL_OK;
+}
+
+static int read_flags(Ctx* c, SolverData* S, int* h) {
+  ELFEL_CUDA(c, cudaMemcpyAsync(h, S->flags.p, sizeof(int) * F_COUNT, cudaMemcpyDeviceToHost, c->stream));
+  ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+  return ELFEL_OK;
+}
+
+static int set_scal(Ctx* c, SolverData* S, int idx, double v) {
+  ELFEL_CUDA(c, cudaMemcpyAsync(S->scal.p + idx, &v, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+  return ELFEL_OK;
+}
+
+// Capture kGraphIters iterations of a kernel sequence into an executable graph.
+template <typename F>
+static int capture(Ctx* c, cudaGraphExec_t* out, F&& body) {
+  if (*out) return ELFEL_OK;
+  cudaGraph_t g;
+  ELFEL_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  for (int k = 0; k < kGraphIters; ++k) body();
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  if (e != cudaSuccess) return fail(c, ELFEL_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(c, ELFEL_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+  return ELFEL_OK;
+}
+
+// ------------------------------------------------------------------ drivers
+static int run_pcg64(elfel_sysmat* m, double rtol, int maxit, elfel_solve_stats* st) {
+  Ctx* c = &m->h->c;
+  SolverData* S = m->solver;
+  const int64_t nu = S->nu;
+  const unsigned vg = vec_grid(c, nu);
+  // x = 0, r = b
+  ELFEL_CUDA(c, cudaMemsetAsync(S->x64.p, 0, sizeof(double) * nu, c->stream));
+  ELFEL_CUDA(c, cudaMemcpyAsync(S->r64.p, S->b64.p, sizeof(double) * nu, cudaMemcpyDeviceToDevice, c->stream));
+  int hf[F_COUNT] = {0, 0, 0, maxit, 0, 0};
+  ELFEL_CUDA(c, cudaMemcpyAsync(S->flags.p, hf, sizeof(hf), cudaMemcpyHostToDevice, c->stream));
+  cg_start_k<double><<<vg, kBlk, 0, c->stream>>>(nu, S->r64.p, S->z64.p, S->p64.p, S->dinv64.p, red_area(S, 0),
+                                                 S->scal.p, S->flags.p, 1);
+  ELFEL_LAUNCH_CHECK(c);
+  ELFEL_TRY(capture(c, &S->g_pcg64, [&]() {
+    launch_spmv_dot<double>(c, S, S->ff.v64.p, S->p64.p, S->q64.p, red_area(S, 0), S_PQ);
+    cg_update_k<double, false><<<vg, kBlk, 0, c->stream>>>(nu, S->x64.p, S->r64.p, S->p64.p, S->q64.p, S->z64.p,
+                                                            S->dinv64.p, red_area(S, 1), S->scal.p, S->flags.p);
+    cg_p_k<double><<<vg, kBlk, 0, c->stream>>>(nu, S->p64.p, S->z64.p, S->scal.p, S->flags.p);
+  }));
+  while (true) {
+    ELFEL_CUDA(c, cudaGraphLaunch(S->g_pcg64, c->stream));
+    ELFEL_TRY(read_flags(c, S, hf));
+    if (hf[F_DONE]) break;
+  }
+  st->iterations = hf[F_ITER];
+  st->refinements = 0;
+  // true residual
+  ELFEL_TRY(launch_resid(c, S, S->x64.p, nullptr, S->b64.p, S->r64.p, red_area(S, 2), S_RR));
+  return ELFEL_OK;
+}
+
+static int run_pcg32(elfel_sysmat* m, double rtol, int maxit, elfel_solve_stats* st) {
+  Ctx* c = &m->h->c;
+  SolverData* S = m->solver;
+  const int64_t nu = S->nu;
+  const unsigned vg = vec_grid(c, nu);
+  ELFEL_CUDA(c, cudaMemsetAsync(S->x64.p, 0, sizeof(double) * nu, c->stream));
+  ELFEL_CUDA(c, cudaMemsetAsync(S->xa32.p, 0, sizeof(float) * nu, c->stream));
+  ELFEL_CUDA(c, cudaMemcpyAsync(S->r64.p, S->b64.p, sizeof(double) * nu, cudaMemcpyDeviceToDevice, c->stream));
+  demote_k<<<vg, kBlk, 0, c->stream>>>(nu, S->r64.p, S->r32.p);
+  int hf[F_COUNT] = {0, 0, 0, maxit, 0, 0};
+  ELFEL_CUDA(c, cudaMemcpyAsync(S->flags.p, hf, sizeof(hf), cudaMemcpyHostToDevice, c->stream));
+  cg_start_k<float><<<vg, kBlk, 0, c->stream>>>(nu, S->r32.p, S->z32.p, S->p32.p, S->dinv32.p, red_area(S, 0),
+                                                S->scal.p, S->flags.p, 1);
+  ELFEL_LAUNCH_CHECK(c);
+  ELFEL_TRY(capture(c, &S->g_pcg32, [&]() {
+    launch_spmv_dot<float>(c, S, S->ff.v32.p, S->p32.p, S->q32.p, red_area(S, 0), S_PQ);
+    cg_update_k<float, true><<<vg, kBlk, 0, c->stream>>>(nu, S->xa32.p, S->r32.p, S->p32.p, S->q32.p, S->z32.p,
+                                                         S->dinv32.p, red_area(S, 1), S->scal.p, S->flags.p);
+    cg_p_k<float><<<vg, kBlk, 0, c->stream>>>(nu, S->p32.p, S->z32.p, S->scal.p, S->flags.p);
+  }));
+  int refinements = 0;
+  double hsc[S_COUNT];
+  while (true) {
+    ELFEL_CUDA(c, cudaGraphLaunch(S->g_pcg32, c->stream));
+    ELFEL_TRY(read_flags(c, S, hf));
+    if (!hf[F_RU]) continue;
+    // FP64 residual replacement
+    fold_k<<<vg, kBlk, 0, c->stream>>>(nu, S->x64.p, S->xa32.p);
+    ELFEL_TRY(launch_resid(c, S, S->x64.p, nullptr, S->b64.p, S->r64.p, red_area(S, 2), S_RR));
+    ELFEL_CUDA(c, cudaMemcpyAsync(hsc, S->scal.p, sizeof(hsc), cudaMemcpyDeviceToHost, c->stream));
+    ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+    ++refinements;
+    const bool conv = hsc[S_RR] <= hsc[S_TOL2] * hsc[S_BN2];
+    if (conv || hf[F_ITER] >= maxit) {
+      hf[F_CONV] = conv ? 1 : 0;
+      break;
+    }
+    demote_k<<<vg, kBlk, 0, c->stream>>>(nu, S->r64.p, S->r32.p);
+    cg_start_k<float><<<vg, kBlk, 0, c->stream>>>(nu, S->r32.p, S->z32.p, S->p32.p, S->dinv32.p, red_area(S, 0),
+                                                  S->scal.p, S->flags.p, 0);
+    ELFEL_LAUNCH_CHECK(c);
+    ELFEL_TRY(set_scal(c, S, S_RMAX, sqrt(hsc[S_RR])));
+  }
+  st->iterations = hf[F_ITER];
+  st->refinements = refinements;
+  return ELFEL_OK;
+}
+
+// MINRES on A x = b (precision T), x returned in xT.  Returns iterations.
+template <typename T>
+static int run_minres(Ctx* c, SolverData* S, const T* v, const T* minv, const T* b, T* x, T* const* vb, T* const* zb,
+                      T* const* wb, T* q, double rtol, int maxit, cudaGraphExec_t* graph, int* iters, int* conv) {
+  const int64_t nu = S->nu;
+  const unsigned vg = vec_grid(c, nu);
+  int hf[F_COUNT] = {0, 0, 0, maxit, 0, 0};
+  ELFEL_CUDA(c, cudaMemcpyAsync(S->flags.p, hf, sizeof(hf), cudaMemcpyHostToDevice, c->stream));
+  ELFEL_TRY(set_scal(c, S, S_TOL2, rtol * rtol));
+  mr_start_k<T><<<vg, kBlk, 0, c->stream>>>(nu, b, vb, zb, wb, minv, x, red_area(S, 0), S->scal.p, S->flags.p);
+  scale_k<T><<<vg, kBlk, 0, c->stream>>>(nu, zb, S->scal.p);
+  ELFEL_LAUNCH_CHECK(c);
+  ELFEL_TRY(capture(c, graph, [&]() {
+    launch_mr_spmv<T>(c, S, v, zb, q, red_area(S, 0));
+    mr_vec_k<T><<<vg, kBlk, 0, c->stream>>>(nu, q, vb, zb, minv, red_area(S, 1), S->scal.p, S->flags.p);
+    mr_upd_k<T><<<vg, kBlk, 0, c->stream>>>(nu, zb, wb, x, S->scal.p, S->flags.p);
+    mr_tail_k<<<1, 1, 0, c->stream>>>(S->scal.p, S->flags.p);
+  }));
+  while (true) {
+    ELFEL_CUDA(c, cudaGraphLaunch(*graph, c->stream));
+    ELFEL_TRY(read_flags(c, S, hf));
+    if (hf[F_DONE]) break;
+  }
+  *iters = hf[F_ITER];
+  *conv = hf[F_CONV];
+  return ELFEL_OK;
+}
+
+}  // namespace elfel
+
+using namespace elfel;
+
+__global__ void lift_prep_k(int64_t n, const double* T, double* y) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = T[i];
+}
+
+extern "C" int elfel_solve(elfel_sysmat* m, const double* Fh, double* T, int64_t nu, int32_t method, double rtol,
+                           int32_t maxit, elfel_solve_stats* stats) {
+  if (!m || !m->h) return ELFEL_ERR_ARG;
+  Ctx* c = &m->h->c;
+  elfel_solve_stats st;
+  memset(&st, 0, sizeof(st));
+  if (!m->finished) return fail(c, ELFEL_ERR_STATE, "solve: finish! the matrix first");
+  if (m->nrow != m->ncol) return fail(c, ELFEL_ERR_ARG, "solve: K must be square");
+  if (nu < 0 || nu > m->nrow || !T) return fail(c, ELFEL_ERR_ARG, "solve: nu outside 0..%lld", (long long)m->nrow);
+  if (!Fh && !m->has_rhs) return fail(c, ELFEL_ERR_ARG, "solve: no right-hand side");
+  if (method < ELFEL_PCG64 || method > ELFEL_MINRES32_IR) return fail(c, ELFEL_ERR_ARG, "solve: unknown method");
+  if (!(rtol > 0.0) || maxit < 1) return fail(c, ELFEL_ERR_ARG, "solve: rtol > 0 and maxit >= 1 required");
+  cudaSetDevice(c->device);
+  const auto t0 = std::chrono::steady_clock::now();
+  ELFEL_TRY(build_solver(m, nu));
+  SolverData* S = m->solver;
+  const bool minres = method == ELFEL_MINRES64 || method == ELFEL_MINRES32_IR;
+  ELFEL_TRY(refresh_values(m, minres ? 1 : 0));
+  const int64_t n = m->nrow;
+  if (nu == 0) {
+    if (stats) *stats = st;
+    return ELFEL_OK;
+  }
+  // lifted right-hand side: b = F_f - K_ff T_f - K_fd T_d
+  ELFEL_CUDA(c, cudaMemcpyAsync(S->T64.p, T, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+  double* Fd = m->rhs.p;
+  DBuf<double> Ftmp;
+  if (Fh) {
+    ELFEL_TRY(Ftmp.alloc(c, (size_t)n));
+    ELFEL_CUDA(c, cudaMemcpyAsync(Ftmp.p, Fh, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    Fd = Ftmp.p;
+  }
+  ELFEL_TRY(launch_resid(c, S, S->T64.p, S->T64.p + nu, Fd, S->b64.p, red_area(S, 2), S_BN2));
+  Ftmp.release(c);
+  double bn2 = 0.0;
+  ELFEL_CUDA(c, cudaMemcpyAsync(&bn2, S->scal.p + S_BN2, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+  ELFEL_TRY(set_scal(c, S, S_TOL2, rtol * rtol));
+  ELFEL_TRY(set_scal(c, S, S_RMAX, sqrt(bn2)));
+  ELFEL_TRY(set_scal(c, S, S_DELTA, 0.1));
+  int rc = ELFEL_OK;
+  if (bn2 == 0.0) {
+    ELFEL_CUDA(c, cudaMemsetAsync(S->x64.p, 0, sizeof(double) * nu, c->stream));
+    st.converged = 1;
+  } else if (method == ELFEL_PCG64) {
+    rc = run_pcg64(m, rtol, maxit, &st);
+  } else if (method == ELFEL_PCG32_IR) {
+    rc = run_pcg32(m, rtol, maxit, &st);
+  } else if (method == ELFEL_MINRES64) {
+    for (int i = 0; i < 3; ++i) {
+      if (!S->v64[i].p) ELFEL_TRY(S->v64[i].alloc(c, (size_t)nu));
+      if (!S->w64[i].p) ELFEL_TRY(S->w64[i].alloc(c, (size_t)nu));
+    }
+    DBuf<double*> dptr;
+    ELFEL_TRY(dptr.alloc(c, 9));
+    double* hp[9] = {S->v64[0].p, S->v64[1].p, S->v64[2].p, S->z64.p, S->p64.p, S->y64.p,
+                     S->w64[0].p, S->w64[1].p, S->w64[2].p};
+    ELFEL_CUDA(c, cudaMemcpyAsync(dptr.p, hp, sizeof(hp), cudaMemcpyHostToDevice, c->stream));
+    if (S->g_minres64) {  // the pointer table is re-created each solve; rebuild the graph
+      cudaGraphExecDestroy(S->g_minres64);
+      S->g_minres64 = nullptr;
+    }
+    int it = 0, conv = 0;
+    rc = run_minres<double>(c, S, S->ff.v64.p, S->dinv64.p, S->b64.p, S->x64.p, dptr.p, dptr.p + 3, dptr.p + 6,
+                            S->q64.p, rtol, maxit, &S->g_minres64, &it, &conv);
+    ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+    dptr.release(c);
+    st.iterations = it;
+  } else {
+    // FP32 MINRES inside FP64 iterative refinement
+    for (int i = 0; i < 3; ++i) {
+      if (!S->v32[i].p) ELFEL_TRY(S->v32[i].alloc(c, (size_t)nu));
+      if (!S->w32[i].p) ELFEL_TRY(S->w32[i].alloc(c, (size_t)nu));
+    }
+    float* zb[3] = {S->z32.p, S->p32.p, S->zz32.p};
+    DBuf<float*> dptr;
+    ELFEL_TRY(dptr.alloc(c, 9));
+    float* hp[9] = {S->v32[0].p, S->v32[1].p, S->v32[2].p, zb[0], zb[1], zb[2], S->w32[0].p, S->w32[1].p, S->w32[2].p};
+    ELFEL_CUDA(c, cudaMemcpyAsync(dptr.p, hp, sizeof(hp), cudaMemcpyHostToDevice, c->stream));
+    if (S->g_minres32) {
+      cudaGraphExecDestroy(S->g_minres32);
+      S->g_minres32 = nullptr;
+    }
+    const unsigned vg = vec_grid(c, nu);
+    ELFEL_CUDA(c, cudaMemsetAsync(S->x64.p, 0, sizeof(double) * nu, c->stream));
+    ELFEL_CUDA(c, cudaMemcpyAsync(S->r64.p, S->b64.p, sizeof(double) * nu, cudaMemcpyDeviceToDevice, c->stream));
+    double rr = bn2;
+    int total = 0, outer = 0;
+    const double inner_tol = 1e-5;
+    while (true) {
+      demote_k<<<vg, kBlk, 0, c->stream>>>(nu, S->r64.p, S->b32.p);
+      int it = 0, conv = 0;
+      rc = run_minres<float>(c, S, S->ff.v32.p, S->dinv32.p, S->b32.p, S->x32.p, dptr.p, dptr.p + 3, dptr.p + 6,
+                             S->q32.p, inner_tol, maxit - total, &S->g_minres32, &it, &conv);
+      if (rc != ELFEL_OK) break;
+      total += it;
+      ++outer;
+      add_scaled_k<<<vg, kBlk, 0, c->stream>>>(nu, S->x64.p, S->x32.p);
+      ELFEL_TRY(launch_resid(c, S, S->x64.p, nullptr, S->b64.p, S->r64.p, red_area(S, 2), S_RR));
+      ELFEL_CUDA(c, cudaMemcpyAsync(&rr, S->scal.p + S_RR, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+      if (rr <= rtol * rtol * bn2 || total >= maxit || outer >= 100) break;
+    }
+    dptr.release(c);
+    st.iterations = total;
+    st.refinements = outer;
+  }
+  if (rc != ELFEL_OK) return rc;
+  // final FP64 true residual
+  ELFEL_TRY(launch_resid(c, S, S->x64.p, nullptr, S->b64.p, S->r64.p, red_area(S, 2), S_RR));
+  double rr = 0.0;
+  ELFEL_CUDA(c, cudaMemcpyAsync(&rr, S->scal.p + S_RR, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  ELFEL_CUDA(c, cudaMemcpyAsync(T, S->x64.p, sizeof(double) * nu, cudaMemcpyDeviceToHost, c->stream));
+  ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+  st.relres = bn2 > 0.0 ? sqrt(rr / bn2) : 0.0;
+  st.converged = st.relres <= rtol ? 1 : 0;
+  st.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (stats) *stats = st;
+  if (!st.converged)
+    return fail(c, ELFEL_ERR_NOT_CONVERGED, "solve: relative residual %.3e > %.3e after %d iterations", st.relres,
+                rtol, st.iterations);
+  return ELFEL_OK;
+}

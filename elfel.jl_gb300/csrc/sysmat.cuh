@@ -1,0 +1,148 @@
+// Device-resident sparse system: CSC pattern, slot map, values, rhs, solver data.
+#pragma once
+#include "common.cuh"
+#include "integrate.cuh"
+
+namespace elfel {
+
+// One local-matrix kind appended per element, in the order of the reference's
+// assemble! calls.  rows come from table R (nel x nr), columns from C (nel x nc).
+//   transposed = 0: assemble!(am, lma)            -> slots column-major (i fastest)
+//   transposed = 1: assemble!(am, transpose(lma)) -> parent entries row-major,
+//                   row/col swapped (src/Assemblers.jl:109-114)
+// Storage: values live in a per-element record of `store_per_elem` doubles.
+//   store_off: offset of this block's (parent's) values in the record
+//   sym = 1:   the block is symmetric and only j >= i is stored (i,j)->(min,max)
+struct SlotBlock {
+  const int32_t* R = nullptr;  // nullptr: every row number is 0 (a vector as a 1 x n matrix)
+  const int32_t* C = nullptr;
+  int nr = 0, nc = 0;
+  int transposed = 0;
+  int sym = 0;
+  int slot_off = 0;   // offset of this block among the element's slots
+  int store_off = 0;  // offset of the values this block reads
+};
+
+constexpr int kMaxBlocks = 4;
+
+struct SlotGen {
+  int64_t nel = 0;
+  int slots_per_elem = 0;   // S
+  int store_per_elem = 0;   // values stored per element
+  int nblocks = 0;
+  SlotBlock b[kMaxBlocks];
+  // COO mode (nblocks == 0): one slot per triplet
+  const int32_t* I = nullptr;
+  const int32_t* J = nullptr;
+  int64_t ncoo = 0;
+  int64_t total() const { return nblocks ? nel * (int64_t)slots_per_elem : ncoo; }
+};
+
+// Column-major index within a symmetric nr x nr block stored as its upper
+// triangle (i <= j), packed column by column: j*(j+1)/2 + i.
+__host__ __device__ __forceinline__ int sym_index(int i, int j) {
+  if (i > j) { int t = i; i = j; j = t; }
+  return j * (j + 1) / 2 + i;
+}
+
+__device__ __forceinline__ void slot_rc(const SlotGen& g, int64_t s, int32_t& r, int32_t& c, int64_t& store) {
+  if (g.nblocks == 0) {
+    r = g.I[s];
+    c = g.J[s];
+    store = s;
+    return;
+  }
+  const int64_t e = s / g.slots_per_elem;
+  const int l = (int)(s - e * g.slots_per_elem);
+  int bi = 0;
+#pragma unroll
+  for (int k = 1; k < kMaxBlocks; ++k)
+    if (k < g.nblocks && l >= g.b[k].slot_off) bi = k;
+  const SlotBlock& B = g.b[bi];
+  const int t = l - B.slot_off;
+  int i, j;  // parent (row, col) index within the local matrix
+  if (!B.transposed) {
+    i = t % B.nr;
+    j = t / B.nr;
+    r = B.R ? B.R[e * B.nr + i] : 0;
+    c = B.C[e * B.nc + j];
+  } else {
+    i = t / B.nc;  // parent row
+    j = t % B.nc;  // parent col
+    r = B.C[e * B.nc + j];
+    c = B.R ? B.R[e * B.nr + i] : 0;
+  }
+  const int loc = B.sym ? sym_index(i, j) : (i + j * B.nr);
+  store = e * (int64_t)g.store_per_elem + B.store_off + loc;
+}
+
+// CSC pattern with the contributor lists of each nonzero.
+struct Pattern {
+  int64_t nrow = 0, ncol = 0, nnz = 0, nslots = 0;
+  DBuf<int64_t> colptr;   // ncol+1
+  DBuf<int32_t> rowval;   // nnz, 0-based
+  DBuf<int32_t> cptr;     // nnz+1: contributors of nonzero k are contrib[cptr[k] .. cptr[k+1])
+  DBuf<int32_t> contrib;  // nslots: storage index of each contribution, ascending slot order
+  void release(Ctx* c) {
+    colptr.release(c);
+    rowval.release(c);
+    cptr.release(c);
+    contrib.release(c);
+    nrow = ncol = nnz = nslots = 0;
+  }
+};
+
+// Build the CSC pattern of the slots of `g` (nrow x ncol matrix).
+int build_pattern(Ctx* c, const SlotGen& g, int64_t nrow, int64_t ncol, Pattern* P);
+
+// vals_out[k] = sum of store[contrib[t]] over t in [cptr[k], cptr[k+1]), in order.
+int reduce_values(Ctx* c, const Pattern& P, const double* store, double* vals_out);
+
+// Convert 1-based int64 indices to 0-based int32 with a range check.
+int to_index32(Ctx* c, const int64_t* src_host, int64_t n, int64_t limit, DBuf<int32_t>* dst,
+               const char* what);
+
+// Fused-mode device data.
+struct Fused {
+  int physics = 0;
+  int npts = 0;
+  QPTab tab;
+  int nn_u = 0, ncomp_u = 0, nn_p = 0;
+  int64_t nel = 0, nnodes_u = 0, nnodes_p = 0;
+  DBuf<int32_t> conn_u, conn_p;      // nel x nn, 0-based node ids
+  DBuf<double> xy_u;                 // nnodes x 2
+  DBuf<int32_t> dofs_u, dofs_p;      // nel x nedof, 0-based DOFs
+  DBuf<int32_t> zero_rows;           // nel x nedof zeros (row table of the rhs "matrix")
+  DBuf<double> coef;                 // per-element coefficients
+  DBuf<double> kstore;               // element matrix records, nel x store_per_elem
+  DBuf<double> fstore;               // element vector records, nel x nedof
+  SlotGen kgen, fgen;
+  Pattern fpat;                      // F pattern: 1 x ndofs matrix
+  DBuf<double> pmass_store;          // Stokes: pressure mass diagonal per element (nel x 3)
+  Pattern pmpat;
+  DBuf<double> pmass_diag;           // ndofs (nonzero at pressure DOFs only)
+  void release(Ctx* c) {
+    conn_u.release(c); conn_p.release(c); xy_u.release(c); dofs_u.release(c); dofs_p.release(c);
+    zero_rows.release(c); coef.release(c); kstore.release(c); fstore.release(c);
+    fpat.release(c); pmass_store.release(c); pmpat.release(c); pmass_diag.release(c);
+  }
+};
+
+struct SolverData;  // defined in solve.cu
+
+}  // namespace elfel
+
+struct elfel_sysmat {
+  elfel_ctx* h = nullptr;
+  int started = 0, finished = 0;
+  int64_t nrow = 0, ncol = 0;
+  void* coo_stage = nullptr;  // COO mode: device buffers of the appended triplets
+  elfel::Pattern P;
+  elfel::DBuf<double> vals;  // nnz CSC values
+  elfel::DBuf<double> rhs;   // nrow (fused mode)
+  int has_rhs = 0;
+  int fused = 0;
+  elfel::Fused F;
+  elfel::SolverData* solver = nullptr;
+  uint64_t values_version = 0;  // bumped whenever vals change
+};

@@ -1,0 +1,202 @@
+"""Device assembly against the oracle (GPU).
+
+Pattern (colptr/rowval) and DOF numbering: bit-exact.  Values: FP64, within
+1e-12 of the largest entry (the device reorganises the quadrature sums of
+straight-sided elements, so the last bits differ).  COO mode sums in the same
+order as the oracle and is checked bit for bit.
+"""
+import numpy as np
+import pytest
+
+from problems import (elasticity_D, elasticity_setup, heat_oracle, heat_space, stokes_oracle_K, stokes_setup,
+                      traction_oracle)
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-12  # FP64 parity tolerance, relative to max |entry|
+
+
+def same_pattern(K, K0):
+    K.sort_indices()
+    return (K.indptr == K0.indptr).all() and (K.indices == K0.indices).all() and K.shape == K0.shape
+
+
+def close(a, b, rtol=RTOL):
+    scale = max(np.abs(b).max(), 1e-300)
+    return np.abs(a - b).max() <= rtol * scale
+
+
+def test_coo_7x7_golden(E, O, gpu, golden):
+    """test/test_assemblers.jl:6-34 through SysmatAssemblerSparse on the device."""
+    g = golden("assemblers.json")
+    a = E.start(E.SysmatAssemblerSparse(0.0), 7, 7)
+    for blk in g["blocks"]:
+        m = np.array(blk["m"])
+        for j in range(m.shape[1]):
+            for i in range(m.shape[0]):
+                E.assemble(a, blk["gi"][i], blk["gj"][j], m[i, j])
+    A = E.finish(a)
+    B = np.array(g["B"])
+    assert np.linalg.norm(A.toarray() - B) / np.linalg.norm(B) < g["rtol"]
+    I, J, V = a.triplets()
+    A0 = O.sparse(I - 1, J - 1, V, 7, 7)
+    assert same_pattern(A, A0) and (A.data == A0.data).all()
+
+
+def test_coo_local_and_transpose(E, O, gpu, golden):
+    """test/test_assemblers.jl:47-129: local assemblers, plain and transposed."""
+    g = golden("assemblers.json")
+    B = np.array(g["B"])
+    for transposed in (False, True):
+        a = E.start(E.SysmatAssemblerSparse(0.0), 7, 7)
+        for blk in g["blocks"]:
+            m = np.array(blk["m"])
+            gi, gj = blk["gi"], blk["gj"]
+            if transposed:
+                la = E.LocalMatrixAssembler(len(gj), len(gi), 0.0)
+                E.init(la, gj, gi)
+                la.M[:, :] = m.T
+                E.assemble(a, E.transpose(la))
+            else:
+                la = E.LocalMatrixAssembler(len(gi), len(gj), 0.0)
+                E.init(la, gi, gj)
+                la.M[:, :] = m
+                E.assemble(a, la)
+        A = E.finish(a).toarray()
+        assert np.linalg.norm(A - B) / np.linalg.norm(B) < g["rtol"]
+
+
+@pytest.mark.parametrize("seed,n,m,k", [(0, 50, 40, 3000), (1, 1, 1, 10), (2, 300, 7, 20000), (3, 5, 2000, 4000)])
+def test_coo_random_bitexact(E, O, gpu, seed, n, m, k):
+    """Random triplets with many duplicates, zeros, a long column: bit-exact vs the oracle."""
+    rng = np.random.default_rng(seed)
+    I = rng.integers(1, n + 1, k)
+    J = rng.integers(1, m + 1, k)
+    if m > 3:
+        J[: k // 3] = 2  # one long column (> one warp's shared-memory tile)
+    V = rng.standard_normal(k)
+    V[::5] = 0.0
+    a = E.start(E.SysmatAssemblerSparse(0.0), n, m)
+    a._chunks.append((I, J, V))
+    A = E.finish(a)
+    A0 = O.sparse(I - 1, J - 1, V, n, m)
+    assert same_pattern(A, A0)
+    assert (A.data == A0.data).all()
+
+
+def test_coo_empty_and_errors(E, gpu):
+    a = E.start(E.SysmatAssemblerSparse(0.0), 4, 3)
+    A = E.finish(a)
+    assert A.shape == (4, 3) and A.nnz == 0
+    a = E.start(E.SysmatAssemblerSparse(0.0), 4, 3)
+    E.assemble(a, 5, 1, 1.0)  # row outside 1..4
+    with pytest.raises(E.ElfelError):
+        E.finish(a)
+
+
+def test_sysvec(E, gpu):
+    """test/test_assemblers.jl:142-163 (SysvecAssembler)."""
+    rng = np.random.default_rng(5)
+    N = 30
+    v = np.zeros(N)
+    a = E.start(E.SysvecAssembler(), N)
+    for rows in ([1, 7, 2], [29, 15, 1, 7, 3, 6, 2]):
+        vals = rng.random(len(rows))
+        for i, p in zip(rows, vals):
+            E.assemble(a, i, p)
+            v[i - 1] += p
+    w = E.finish(a)
+    assert np.linalg.norm(v - w) / np.linalg.norm(w) <= 1e-9
+    lva = E.LocalVectorAssembler(3, 0.0)
+    E.init(lva, [3, 3, 1])
+    lva.V[:] = [1.0, 2.0, 4.0]
+    a = E.start(E.SysvecAssembler(), 4)
+    E.assemble(a, lva)
+    assert E.finish(a).tolist() == [4.0, 0.0, 3.0, 0.0]
+
+
+HEAT_CASES = [
+    # etype, nx, ny, orientation, jitter, curved, npts
+    ("T3", 4, 4, "a", 0.0, False, 1),
+    ("T3", 17, 9, "alternate", 0.02, False, 3),
+    ("T6", 6, 5, "a", 0.0, False, 3),
+    ("T6", 13, 11, "alternate", 0.02, False, 3),
+    ("T6", 9, 7, "a", 0.01, True, 3),
+    ("T6", 8, 8, "a", 0.01, True, 6),
+    ("T3", 100, 100, "alternate", 0.0, False, 3),
+]
+
+
+@pytest.mark.parametrize("case", HEAT_CASES)
+def test_fused_heat_parity(E, O, gpu, case):
+    etype, nx, ny, orient, jit, curved, npts = case
+    blk = E.T3block if etype == "T3" else E.T6block
+    mesh = blk(1.0, 1.0, nx, ny, orientation=orient)
+    if jit:
+        mesh = E.jitter(mesh, jit / max(nx, ny), seed=11, curved=curved)
+    fe = E.FEH1_T3() if etype == "T3" else E.FEH1_T6()
+    fesp = heat_space(E, mesh, fe)
+    rng = np.random.default_rng(4)
+    kappa = np.exp(rng.uniform(np.log(0.5), np.log(2.0), mesh.nel))
+    n = E.ndofs(fesp)
+    am = E.start(E.SysmatAssemblerGPU(), n, n)
+    E.assemble_heat(am, E.FEIterator(fesp), E.QPIterator(fesp, {"kind": "default", "npts": npts}), kappa, -6.0)
+    K, F = E.finish(am), am.rhs()
+    K0, F0 = heat_oracle(E, O, mesh, fesp, npts, kappa, -6.0)
+    assert same_pattern(K, K0)
+    assert close(K.data, K0.data) and close(F, F0)
+    # re-assembly with new coefficients reuses the pattern
+    am.heat(kappa * 2.0, -3.0)
+    K2 = E.finish(am)
+    assert same_pattern(K2, K0) and close(K2.data, 2.0 * K0.data)
+
+
+def test_fused_heat_nnz_formula(E, gpu):
+    """Pattern size of the uniform T6 block: 46 N^2 + 16 N + 1 nonzeros."""
+    for N in (3, 10, 31):
+        mesh = E.T6block(1.0, 1.0, N, N)
+        fesp = heat_space(E, mesh, E.FEH1_T6())
+        n = E.ndofs(fesp)
+        am = E.start(E.SysmatAssemblerGPU(), n, n)
+        E.assemble_heat(am, E.FEIterator(fesp), E.QPIterator(fesp, {"npts": 3}), 1.0, -6.0)
+        assert E.finish(am).nnz == 46 * N * N + 16 * N + 1
+
+
+@pytest.mark.parametrize("etype,curved", [("T3", False), ("T6", False), ("T6", True)])
+def test_fused_elasticity_parity(E, O, gpu, etype, curved):
+    mesh, fesp, bforce, right = elasticity_setup(E, 10, 6, etype=etype)
+    if curved:
+        mesh = E.jitter(mesh, 0.01, seed=2, curved=True)
+        fesp = E.FESpace(float, mesh, fesp.fe, 2)
+        left = E.vselect(mesh.xy, [0.0, 0.0, 0.0, 1.0], inflate=1e-4)
+        E.setebc(fesp, 0, left, 1, 0.0)
+        E.setebc(fesp, 0, left, 2, 0.0)
+        E.numberdofs(fesp)
+    n = E.ndofs(fesp)
+    elit = E.FEIterator(fesp)
+    am = E.start(E.SysmatAssemblerGPU(), n, n)
+    E.assemble_elasticity(am, elit, E.QPIterator(fesp, {"npts": 3}), 1.0, 0.3, True, bforce, right, (1.0, 0.0))
+    K, F = E.finish(am), am.rhs()
+    D = elasticity_D(1.0, 0.3, True)
+    ke, fe = O.elasticity_element_matrices(3, mesh.conn - 1, mesh.xy, D, bforce)
+    ed = elit.eldofs_table() - 1
+    K0 = O.sparse(*O.local_coo(ed, ed, ke), n, n)
+    F0 = O.vec_assemble(n, ed, fe)
+    if not curved:
+        F0 = F0 + traction_oracle(mesh, ed, right, (1.0, 0.0), n)
+    assert same_pattern(K, K0)
+    assert close(K.data, K0.data)
+    if not curved:
+        assert close(F, F0)
+
+
+def test_fused_stokes_parity(E, O, gpu):
+    vmesh, pmesh, ufesp, pfesp = stokes_setup(E, 6)
+    K0, n = stokes_oracle_K(E, O, vmesh, ufesp, pfesp)
+    am = E.start(E.SysmatAssemblerGPU(), n, n)
+    E.assemble_stokes(am, E.FEIterator(ufesp), E.FEIterator(pfesp), E.QPIterator(ufesp, {"npts": 3}), 1.0)
+    K = E.finish(am)
+    assert same_pattern(K, K0)
+    assert close(K.data, K0.data)
+    # explicit zeros of the cross-component couplings are in the pattern
+    assert (K.data == 0.0).sum() > 0 and (K0.data == 0.0).sum() > 0
