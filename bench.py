@@ -1,0 +1,412 @@
+"""Benchmark of the GB300 element-assembly + sparse-solve path.
+
+Default workload: the quadratic heat problem at scale -- unit square,
+1000 x 1000 cells, 2 FEH1_T6 triangles per cell (2,000,000 elements,
+4,004,001 nodes), interior vertices jittered by a seeded uniform +-0.2h
+(midside nodes kept at edge midpoints), conductivity per element
+log-uniform in [0.5, 2], Q = -6, Dirichlet T = 1 + x^2 + 2y^2 on the
+boundary, 3-point rule.  Synthetic, seeded.
+
+One step = one fused assembly of K and F (element integration + slot-map
+reduction into the device CSC built once).  The JSON line reports
+  value   elements assembled per second, inputs resident in HBM;
+  e2e     the same metric through the C ABI from pinned host buffers:
+          upload of mesh, DOF table and coefficients, pattern build,
+          assembly, download of the CSC and F, every step;
+  pcg     the solve of the same system to relative residual 1e-10 with
+          FP64 Jacobi-PCG and with FP32 CG + FP64 residual replacement;
+  roofline / cpu_baseline / clocks as described in the design doc.
+
+``--impl reference`` times the CPU restatement of the reference path (the
+oracle: element loop, COO triplets, SparseArrays.sparse semantics) on the
+host cores instead.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "elems assembled/s; PCG time (FP32+refine vs FP64) at 1e-10; serve p50/p99"
+UNIT = "elements/s"
+
+
+def build_problem(E, N, seed=20261203, jit=0.2):
+    mesh = E.T6block(1.0, 1.0, N, N)
+    mesh = E.jitter(mesh, jit / N, seed=seed)
+    fesp = E.FESpace(float, mesh, E.FEH1_T6())
+    bn = E.boundary_nodes(mesh)
+    x, y = mesh.xy[bn - 1, 0], mesh.xy[bn - 1, 1]
+    E.setebc(fesp, 0, bn, 1, 1.0 + x ** 2 + 2.0 * y ** 2)
+    E.numberdofs(fesp)
+    rng = np.random.default_rng(seed + 1)
+    kappa = np.exp(rng.uniform(np.log(0.5), np.log(2.0), mesh.nel))
+    return mesh, fesp, kappa
+
+
+def read_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.p = None
+        self.window = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={self.Q}", "--format=csv,noheader",
+                                       "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def mark(self, t0, t1):
+        """The timed region, as datetime.now() values; samples outside it are dropped."""
+        self.window = (t0, t1)
+
+    def stop(self):
+        import datetime
+
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [s.strip() for s in line.split(",")]
+                if len(parts) < 10:
+                    continue
+                try:
+                    ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f")
+                    if self.window and not (self.window[0] <= ts <= self.window[1]):
+                        continue
+                    sm.append(float(parts[2].split()[0]))
+                    smax.append(float(parts[3].split()[0]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[6:10]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_assembly_rate(E, O, N, threads, budget_s):
+    """Oracle (CPU restatement of the reference path) assembly throughput on a bounded sample."""
+    mesh, fesp, kappa = build_problem(E, N)
+    ed = E.FEIterator(fesp).eldofs_table() - 1
+    n = E.ndofs(fesp)
+    O.set_threads(threads)
+    conn0 = mesh.conn - 1
+    times = []
+    t_end = time.perf_counter() + budget_s
+    while True:
+        t0 = time.perf_counter()
+        ke, fe = O.heat_element_matrices(6, 3, conn0, mesh.xy, kappa, -6.0)
+        I, J, V = O.local_coo(ed, ed, ke)
+        K = O.sparse(I, J, V, n, n)
+        F = O.vec_assemble(n, ed, fe)
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() > t_end and len(times) >= 2:
+            break
+    del K, F
+    t = statistics.median(times)
+    return mesh.nel / t, t, len(times), mesh.nel
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def reference_arm(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    import __graft_entry__ as entry
+
+    E = entry.package()
+    O = entry.oracle()
+    threads = os.cpu_count() or 1
+    # bounded sample of the same workload: 200 x 200 cells (80,000 T6 elements)
+    N = 200
+    mesh, fesp, kappa = build_problem(E, N)
+    ed = E.FEIterator(fesp).eldofs_table() - 1
+    n = E.ndofs(fesp)
+    O.set_threads(threads)
+    step_times = []
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        ke, fe = O.heat_element_matrices(6, 3, mesh.conn - 1, mesh.xy, kappa, -6.0)
+        I, J, V = O.local_coo(ed, ed, ke)
+        K = O.sparse(I, J, V, n, n)
+        F = O.vec_assemble(n, ed, fe)
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            step_times.append(dt)
+    t = sum(step_times) / len(step_times)
+    v = mesh.nel / t
+    out = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": ws, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+           "config": {"workload": "heat T6 1000x1000 (2M elements), reference CPU path on a 200x200 sample",
+                      "sample_elements": int(mesh.nel), "parallelism": "host threads"},
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                            "sample": f"T6 heat 200x200 ({mesh.nel} elements): element loop (OpenMP) + COO + "
+                                      f"sparse() (1 thread) + vector assembly, mean of {len(step_times)} steps"},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=1000, help="cells per side")
+    ap.add_argument("--no-pcg", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=12.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+    assert args.warmup >= 3 or os.environ.get("ELFEL_BENCH_ALLOW_FEW_WARMUP"), "at least 3 warm-up steps"
+
+    import torch
+
+    ws, rank, local = dist_env()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    import __graft_entry__ as entry
+
+    E = entry.package()
+    if rank == 0:
+        E.build()  # incremental: a no-op when the library is current
+    if dist:
+        dist.barrier()
+    E._native.load()
+    ctx = E.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    N = args.n
+    t_setup0 = time.perf_counter()
+    mesh, fesp, kappa = build_problem(E, N)
+    host_setup_s = time.perf_counter() - t_setup0
+    nel = mesh.nel
+    n, nu = E.ndofs(fesp), E.nunknowns(fesp)
+    elit = E.FEIterator(fesp)
+    qpit = E.QPIterator(fesp, {"kind": "default", "npts": 3})
+
+    # --- device-resident assembly (value) ---------------------------------
+    am = E.start(E.SysmatAssemblerGPU(ctx), n, n)
+    ctx.profile(True)
+    t0 = time.perf_counter()
+    am.setup(E._native.ELFEL_HEAT, elit, qpit)
+    ctx.synchronize()
+    pattern_s = time.perf_counter() - t0
+    setup_phases = ctx.phases()
+    am.heat(kappa, -6.0)  # uploads the coefficients once
+    ctx.synchronize()
+    ctx.profile(False)
+    flush =torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    import datetime
+
+    clocks = Clocks(local)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            flush.zero_()
+            am.heat(None, -6.0)
+        torch.cuda.synchronize()
+        time.sleep(0.3)  # let the sampler start
+        if dist:
+            dist.barrier()
+        ctx.profile(True)
+        evs = []
+        dt0 = datetime.datetime.now()
+        wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()  # L2 (129 MB) flushed between timed steps
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            am.heat(None, -6.0)
+            b.record(stream)
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+        clocks.mark(dt0, datetime.datetime.now())
+        clk = clocks.stop()
+    phases = ctx.phases()
+    ctx.profile(False)
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    t_step = sum(step_ms) / len(step_ms) / 1e3
+    if dist:
+        tt = torch.tensor([t_step], device=f"cuda:{local}")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_step = float(tt.item())
+    value = ws * nel / t_step
+
+    # --- roofline of the dominant kernel (live CUDA events) ---------------
+    hbm, peak_kind = read_peaks()
+    nslots = nel * 36
+    nnz_est = 46 * N * N + 16 * N + 1
+    alg = {  # compulsory bytes of each kernel per launch, as designed
+        "integrate_heat": nel * 6 * 4 + mesh.nnodes * 16 + nel * 8 + nel * 21 * 8 + nel * 6 * 8,
+        "reduce_K": (nnz_est + 1) * 4 + nslots * 4 + nel * 21 * 8 + nnz_est * 8,
+        "reduce_F": (n + 1) * 8 + (n + 1) * 4 + nel * 6 * 4 + nel * 6 * 8 + n * 8,
+    }
+    per = {k: (ms / cnt if cnt else 0.0) for k, (ms, cnt) in phases.items()}
+    dom = max(per, key=per.get)
+    kernel_rows = {k: {"ms_per_launch": per[k], "alg_bytes": alg.get(k),
+                       "gbs": (alg[k] / (per[k] * 1e-3) / 1e9) if k in alg and per[k] else None,
+                       "share": per[k] / sum(per.values())} for k in per}
+    # whole-assembly algorithmic bytes (conn + coords + coefficient + K values + F)
+    asm_bytes = nel * 6 * 4 + mesh.nnodes * 16 + nel * 8 + nnz_est * 8 + n * 8
+    ach = alg[dom] / (per[dom] * 1e-3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            tr = json.load(f)
+        ent = tr.get(dom)
+        if ent:
+            traffic = ent["bytes_per_element"] * nel
+    roofline = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                "traffic": traffic, "kernel": dom, "peak_kind": peak_kind,
+                "assembly": {"alg_bytes": asm_bytes, "achieved": asm_bytes / t_step / 1e9,
+                             "frac": asm_bytes / t_step / 1e9 / hbm},
+                "kernels": kernel_rows}
+
+    # --- e2e through the C ABI from pinned host buffers -------------------
+    conn_h = torch.from_numpy(np.ascontiguousarray(mesh.conn)).pin_memory()
+    xy_h = torch.from_numpy(np.ascontiguousarray(mesh.xy)).pin_memory()
+    dofs_h = torch.from_numpy(elit.eldofs_table()).pin_memory()
+    kap_h = torch.from_numpy(kappa).pin_memory()
+    nnz_dev = int(46 * N * N + 16 * N + 1)
+    colptr_h = torch.empty(n + 1, dtype=torch.int64).pin_memory()
+    rowval_h = torch.empty(nnz_dev, dtype=torch.int64).pin_memory()
+    nzval_h = torch.empty(nnz_dev, dtype=torch.float64).pin_memory()
+    F_h = torch.empty(n, dtype=torch.float64).pin_memory()
+    import ctypes
+
+    N_ = E._native
+    pc = N_.f64(qpit.quadr.param_coords)
+    w = N_.f64(qpit.quadr.weights)
+
+    def as_p(t, typ):
+        return ctypes.cast(ctypes.c_void_p(t.data_ptr()), typ)
+
+    sp = N_.Space(6, 1, nel, mesh.nnodes, as_p(conn_h, N_._i64p), as_p(xy_h, N_._dp), as_p(dofs_h, N_._i64p))
+    desc = N_.FusedDesc(N_.ELFEL_HEAT, 3, N_.ptr(pc), N_.ptr(w), n, sp, N_.Space())
+    lib = ctx.lib
+    hm = ctypes.c_void_p()
+    ctx.check(lib.elfel_sysmat_create(ctx.h, ctypes.byref(hm)))
+
+    def e2e_step():
+        ctx.check(lib.elfel_fused_setup(hm, ctypes.byref(desc)))
+        ctx.check(lib.elfel_fused_heat(hm, as_p(kap_h, N_._dp), -6.0))
+        ctx.check(lib.elfel_sysmat_csc(hm, as_p(colptr_h, N_._i64p), as_p(rowval_h, N_._i64p), as_p(nzval_h, N_._dp)))
+        ctx.check(lib.elfel_sysmat_rhs(hm, as_p(F_h, N_._dp)))
+
+    e2e_steps = max(2, min(args.steps, 5))
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    t_e2e = (time.perf_counter() - t0) / e2e_steps
+    lib.elfel_sysmat_destroy(hm)
+    h2d = conn_h.numel() * 8 + xy_h.numel() * 8 + dofs_h.numel() * 8 + kap_h.numel() * 8 + pc.nbytes + w.nbytes
+    d2h = colptr_h.numel() * 8 + rowval_h.numel() * 8 + nzval_h.numel() * 8 + F_h.numel() * 8
+    e2e = {"value": ws * nel / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+           "ms_per_step": t_e2e * 1e3,
+           "what": "C-ABI fused_setup (H2D mesh+eldofs, device pattern build) + fused_heat (H2D kappa) + CSC/F D2H"}
+    assert int(colptr_h[-1]) == nnz_dev + 1  # pattern size of the uniform T6 block
+
+    # --- PCG: FP64 vs FP32 + FP64 refinement, to 1e-10 ---------------------
+    pcg = None
+    if not args.no_pcg:
+        T0 = np.zeros(n)
+        E.gathersysvec(T0, fesp)
+        res = {}
+        for method in ("pcg64", "pcg32_ir"):
+            T = T0.copy()
+            torch.cuda.synchronize()
+            st = am.solve(T, nu, None, method=method, rtol=1e-10)
+            res[method] = (st, T)
+        st64, T64 = res["pcg64"]
+        st32, T32 = res["pcg32_ir"]
+        rel = float(np.abs(T32[:nu] - T64[:nu]).max() / np.abs(T64[:nu]).max())
+        pcg = {"rtol": 1e-10, "fp64": st64, "fp32_ir": st32, "speedup": st64["seconds"] / st32["seconds"],
+               "fp32_vs_fp64_rel_err_max": rel}
+
+    # --- CPU baseline (oracle restatement on the host cores) --------------
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        O = entry.oracle()
+        threads = os.cpu_count() or 1
+        rate, tper, reps, sel = cpu_assembly_rate(E, O, 200, threads, args.cpu_budget)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"T6 heat 200x200 ({sel} elements): element loop (OpenMP) + COO + sparse() (1 thread) + "
+                         f"vector assembly; median of {reps} runs, {tper:.3f} s each"}
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64", "data": "synthetic (seeded T6 mesh, jitter 0.2h, kappa log-uniform [0.5,2])",
+           "config": {"workload": f"heat T6 {N}x{N} ({nel} elements, {mesh.nnodes} nodes), 3-point rule, "
+                                  f"fused K+F assembly, pattern reused",
+                      "elements": nel, "ndofs": n, "nnz": nnz_dev, "l2": "256 MB buffer written between timed steps",
+                      "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU"},
+           "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 3 * args.steps, "clocks": clk,
+           "pcg": pcg, "pattern_build_s": pattern_s, "setup_phases_ms": {k: v[0] for k, v in setup_phases.items()},
+           "wall_s_timed": wall, "host_mesh_setup_s": host_setup_s}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    del am
+    ctx.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

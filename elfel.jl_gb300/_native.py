@@ -6,6 +6,7 @@ created, the calls raise.
 """
 import ctypes
 import os
+import weakref
 
 import numpy as np
 
@@ -85,6 +86,8 @@ SIGNATURES = {
     "elfel_ctx_set_stream": (ctypes.c_int, [_vp, _vp]),
     "elfel_ctx_stream": (_vp, [_vp]),
     "elfel_ctx_synchronize": (ctypes.c_int, [_vp]),
+    "elfel_ctx_profile": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "elfel_ctx_profile_read": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, _dp, _i64p]),
     "elfel_sysmat_create": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
     "elfel_sysmat_destroy": (ctypes.c_int, [_vp]),
     "elfel_sysmat_start": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int64]),
@@ -150,6 +153,10 @@ class Context:
             raise ElfelError(rc, f"cannot create a context on CUDA device {device}")
         self.h = h
         self.device = device
+        self._children = weakref.WeakSet()  # handles to close before the context
+
+    def adopt(self, child):
+        self._children.add(child)
 
     def check(self, rc):
         if rc == ELFEL_OK:
@@ -173,8 +180,29 @@ class Context:
     def synchronize(self):
         self.check(self.lib.elfel_ctx_synchronize(self.h))
 
+    def profile(self, enable=True):
+        """Start (clearing earlier records) or stop recording per-phase CUDA events."""
+        self.check(self.lib.elfel_ctx_profile(self.h, int(bool(enable))))
+
+    def phases(self):
+        """{phase name: (total device ms, launches)} recorded since profile(True)."""
+        out = {}
+        i = 0
+        buf = ctypes.create_string_buffer(64)
+        while True:
+            ms, k = ctypes.c_double(), ctypes.c_int64()
+            rc = self.lib.elfel_ctx_profile_read(self.h, i, buf, 64, ctypes.byref(ms), ctypes.byref(k))
+            if rc == ELFEL_ERR_ARG:
+                break
+            self.check(rc)
+            out[buf.value.decode()] = (ms.value, k.value)
+            i += 1
+        return out
+
     def close(self):
         if getattr(self, "h", None):
+            for ch in list(self._children):
+                ch.close()
             self.lib.elfel_ctx_destroy(self.h)
             self.h = None
 

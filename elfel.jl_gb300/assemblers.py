@@ -28,11 +28,13 @@ class _Handle:
         h = ctypes.c_void_p()
         self.ctx.check(self.lib.elfel_sysmat_create(self.ctx.h, ctypes.byref(h)))
         self.h = h
+        self.ctx.adopt(self)
 
     def close(self):
-        if getattr(self, "h", None):
+        # a system never outlives its context: Context.close() closes it first
+        if getattr(self, "h", None) and getattr(self.ctx, "h", None):
             self.lib.elfel_sysmat_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:

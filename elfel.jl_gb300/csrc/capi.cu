@@ -220,11 +220,17 @@ extern "C" int elfel_sysmat_finish(elfel_sysmat* m, int64_t* nnz) {
     g.I = I.p;
     g.J = J.p;
     g.ncoo = n;
-    ELFEL_TRY(build_pattern(c, g, m->nrow, m->ncol, &m->P));
+    {
+      Phase ph(c, "pattern_coo");
+      ELFEL_TRY(build_pattern(c, g, m->nrow, m->ncol, &m->P));
+    }
     I.release(c);
     J.release(c);
     ELFEL_TRY(m->vals.alloc(c, (size_t)(m->P.nnz > 0 ? m->P.nnz : 1)));
-    ELFEL_TRY(reduce_values(c, m->P, s->V.p, m->vals.p));
+    {
+      Phase ph(c, "reduce_coo");
+      ELFEL_TRY(reduce_values(c, m->P, s->V.p, m->vals.p));
+    }
     ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
     m->values_version++;
   }
@@ -388,7 +394,10 @@ extern "C" int elfel_fused_setup(elfel_sysmat* m, const elfel_fused_desc* d) {
     g.store_per_elem = 78 + 36;
   }
   m->nrow = m->ncol = d->ndofs;
-  ELFEL_TRY(build_pattern(c, g, d->ndofs, d->ndofs, &m->P));
+  {
+    Phase ph(c, "pattern_K");
+    ELFEL_TRY(build_pattern(c, g, d->ndofs, d->ndofs, &m->P));
+  }
   // right-hand side: a 1 x ndofs "matrix" of the element vectors
   SlotGen& fg = F.fgen;
   fg = SlotGen();
@@ -441,8 +450,14 @@ extern "C" int elfel_fused_set_geometry(elfel_sysmat* m, const double* xy) {
 
 static int finish_values(elfel_sysmat* m) {
   Ctx* c = &m->h->c;
-  ELFEL_TRY(reduce_values(c, m->P, m->F.kstore.p, m->vals.p));
-  ELFEL_TRY(reduce_dense(c, m->F.fpat, m->F.fstore.p, m->rhs.p));
+  {
+    Phase ph(c, "reduce_K");
+    ELFEL_TRY(reduce_values(c, m->P, m->F.kstore.p, m->vals.p));
+  }
+  {
+    Phase ph(c, "reduce_F");
+    ELFEL_TRY(reduce_dense(c, m->F.fpat, m->F.fstore.p, m->rhs.p));
+  }
   m->has_rhs = 1;
   m->finished = 1;
   m->values_version++;
@@ -457,7 +472,10 @@ extern "C" int elfel_fused_heat(elfel_sysmat* m, const double* kappa, double Q) 
   Fused& F = m->F;
   if (kappa && F.nel)
     ELFEL_CUDA(c, cudaMemcpyAsync(F.coef.p, kappa, sizeof(double) * F.nel, cudaMemcpyHostToDevice, c->stream));
-  ELFEL_TRY(launch_heat(c, F.nn_u, F.nel, F.conn_u.p, F.xy_u.p, F.coef.p, Q, F.tab, F.kstore.p, F.fstore.p));
+  {
+    Phase ph(c, "integrate_heat");
+    ELFEL_TRY(launch_heat(c, F.nn_u, F.nel, F.conn_u.p, F.xy_u.p, F.coef.p, Q, F.tab, F.kstore.p, F.fstore.p));
+  }
   return finish_values(m);
 }
 
@@ -489,7 +507,10 @@ extern "C" int elfel_fused_elasticity(elfel_sysmat* m, double E, double nu, int3
     ELFEL_CUDA(c, cudaMemcpyAsync(F.coef.p, bforce, sizeof(double) * 2 * F.nel, cudaMemcpyHostToDevice, c->stream));
     bf = F.coef.p;
   }
-  ELFEL_TRY(launch_elasticity(c, F.nn_u, F.nel, F.conn_u.p, F.xy_u.p, D, bf, F.tab, F.kstore.p, F.fstore.p));
+  {
+    Phase ph(c, "integrate_elasticity");
+    ELFEL_TRY(launch_elasticity(c, F.nn_u, F.nel, F.conn_u.p, F.xy_u.p, D, bf, F.tab, F.kstore.p, F.fstore.p));
+  }
   ELFEL_TRY(finish_values(m));
   if (ntrac > 0) {
     const int nen = F.nn_u == 6 ? 3 : 2;
@@ -541,8 +562,14 @@ extern "C" int elfel_fused_stokes(elfel_sysmat* m, double mu) {
     return fail(c, ELFEL_ERR_STATE, "stokes: fused_setup(ELFEL_STOKES) first");
   cudaSetDevice(c->device);
   Fused& F = m->F;
-  ELFEL_TRY(launch_stokes(c, F.nel, F.conn_u.p, F.xy_u.p, mu, F.tab, F.kstore.p, F.pmass_store.p));
-  ELFEL_TRY(reduce_values(c, m->P, F.kstore.p, m->vals.p));
+  {
+    Phase ph(c, "integrate_stokes");
+    ELFEL_TRY(launch_stokes(c, F.nel, F.conn_u.p, F.xy_u.p, mu, F.tab, F.kstore.p, F.pmass_store.p));
+  }
+  {
+    Phase ph(c, "reduce_K");
+    ELFEL_TRY(reduce_values(c, m->P, F.kstore.p, m->vals.p));
+  }
   ELFEL_CUDA(c, cudaMemsetAsync(m->rhs.p, 0, sizeof(double) * m->nrow, c->stream));
   ELFEL_TRY(reduce_dense(c, F.pmpat, F.pmass_store.p, F.pmass_diag.p));
   m->has_rhs = 1;

@@ -16,6 +16,11 @@ constexpr int kWarp = 32;
 constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs; grids are sized in multiples of this
 
 // ------------------------------------------------------------------ context
+struct PhaseRec {
+  std::string name;
+  cudaEvent_t start = nullptr, stop = nullptr;
+};
+
 struct Ctx {
   int device = 0;
   cudaStream_t stream = nullptr;      // stream all work is issued on
@@ -28,6 +33,31 @@ struct Ctx {
   // scratch for deterministic reductions (partials + counters), grown on demand
   void* red_scratch = nullptr;
   size_t red_scratch_bytes = 0;
+  // phase timing: CUDA events recorded on `stream` around each kernel launch
+  int profiling = 0;
+  std::vector<PhaseRec> phases;
+};
+
+// Records a start event on construction and a stop event on destruction when
+// the context is profiling; otherwise does nothing.
+struct Phase {
+  Ctx* c;
+  int idx = -1;
+  Phase(Ctx* ctx, const char* name) : c(ctx) {
+    if (!c->profiling) return;
+    PhaseRec r;
+    r.name = name;
+    if (cudaEventCreate(&r.start) != cudaSuccess || cudaEventCreate(&r.stop) != cudaSuccess) {
+      cudaGetLastError();
+      return;
+    }
+    cudaEventRecord(r.start, c->stream);
+    c->phases.push_back(r);
+    idx = (int)c->phases.size() - 1;
+  }
+  ~Phase() {
+    if (idx >= 0) cudaEventRecord(c->phases[idx].stop, c->stream);
+  }
 };
 
 // Record an error message on the context and return the code.

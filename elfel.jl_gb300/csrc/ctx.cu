@@ -175,6 +175,8 @@ int scan_counts_i32(Ctx* c, const int32_t* counts, int64_t n, int64_t* offsets) 
 // ------------------------------------------------------------------ C ABI
 using namespace elfel;
 
+static void clear_phases(Ctx* c);
+
 extern "C" int elfel_abi_version(void) { return ELFEL_ABI_VERSION; }
 
 extern "C" int elfel_ctx_create(int device, int64_t mem_budget_bytes, elfel_ctx** out) {
@@ -205,6 +207,7 @@ extern "C" int elfel_ctx_destroy(elfel_ctx* h) {
   cudaSetDevice(h->c.device);
   if (h->c.red_scratch) dfree(&h->c, h->c.red_scratch, h->c.red_scratch_bytes);
   cudaStreamSynchronize(h->c.stream);
+  clear_phases(&h->c);
   if (h->c.own_stream) cudaStreamDestroy(h->c.own_stream);
   delete h;
   return ELFEL_OK;
@@ -230,6 +233,57 @@ extern "C" int elfel_ctx_set_stream(elfel_ctx* h, void* s) {
 }
 
 extern "C" void* elfel_ctx_stream(const elfel_ctx* h) { return h ? (void*)h->c.stream : nullptr; }
+
+static void clear_phases(Ctx* c) {
+  for (PhaseRec& r : c->phases) {
+    if (r.start) cudaEventDestroy(r.start);
+    if (r.stop) cudaEventDestroy(r.stop);
+  }
+  c->phases.clear();
+}
+
+extern "C" int elfel_ctx_profile(elfel_ctx* h, int enable) {
+  if (!h) return ELFEL_ERR_ARG;
+  Ctx* c = &h->c;
+  cudaSetDevice(c->device);
+  if (enable) {
+    ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+    clear_phases(c);
+  }
+  c->profiling = enable ? 1 : 0;
+  return ELFEL_OK;
+}
+
+extern "C" int elfel_ctx_profile_read(elfel_ctx* h, int index, char* name, int name_cap, double* total_ms,
+                                      int64_t* count) {
+  if (!h) return ELFEL_ERR_ARG;
+  Ctx* c = &h->c;
+  cudaSetDevice(c->device);
+  ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+  // distinct names in first-seen order
+  std::vector<std::string> names;
+  for (const PhaseRec& r : c->phases) {
+    bool seen = false;
+    for (const std::string& n : names) seen = seen || n == r.name;
+    if (!seen) names.push_back(r.name);
+  }
+  if (index < 0 || index >= (int)names.size()) return ELFEL_ERR_ARG;
+  double ms = 0.0;
+  int64_t k = 0;
+  for (const PhaseRec& r : c->phases) {
+    if (r.name != names[index]) continue;
+    float t = 0.0f;
+    ELFEL_CUDA(c, cudaEventElapsedTime(&t, r.start, r.stop));
+    ms += t;
+    ++k;
+  }
+  if (name && name_cap > 0) {
+    snprintf(name, (size_t)name_cap, "%s", names[index].c_str());
+  }
+  if (total_ms) *total_ms = ms;
+  if (count) *count = k;
+  return ELFEL_OK;
+}
 
 extern "C" int elfel_ctx_synchronize(elfel_ctx* h) {
   if (!h) return ELFEL_ERR_ARG;

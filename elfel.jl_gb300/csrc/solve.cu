@@ -40,7 +40,7 @@ enum {
   S_COUNT
 };
 // device int flags
-enum { F_DONE = 0, F_RU, F_ITER, F_MAXIT, F_ROT, F_CONV, F_COUNT };
+enum { F_DONE = 0, F_RU, F_ITER, F_MAXIT, F_ROT, F_CONV, F_BRK, F_COUNT };
 
 struct Red4 {
   double* partials;  // nblocks x 4
@@ -126,13 +126,25 @@ __device__ __forceinline__ bool grid_sums(double (&v)[NV], Red4 red, double (&to
   }
   __syncthreads();
   if (!last) return false;
+  // The last block adds the partials with all its threads: thread t sums
+  // blocks t, t + kBlk, ... in order, then a fixed-shape tree; the order
+  // depends only on gridDim, so the result is deterministic.
+  __threadfence();
+#pragma unroll
+  for (int a = 0; a < NV; ++a) {
+    double s = 0.0;
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += kBlk) s += __ldcg(red.partials + b * 4 + a);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) sh[a][wid] = s;
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
-    __threadfence();
-    volatile double* pp = red.partials;
 #pragma unroll
     for (int a = 0; a < NV; ++a) {
       double s = 0.0;
-      for (unsigned b = 0; b < gridDim.x; ++b) s += pp[b * 4 + a];
+#pragma unroll
+      for (int w = 0; w < kBlk / 32; ++w) s += sh[a][w];
       tot[a] = s;
     }
     *red.ticket = 0u;
@@ -235,7 +247,10 @@ __global__ void __launch_bounds__(kBlk) cg_update_k(int64_t n, T* __restrict__ x
                                                    T* __restrict__ z, const T* __restrict__ dinv, Red4 red,
                                                    double* scal, int* flags) {
   if (flags[F_DONE] || flags[F_RU]) return;
-  const T alpha = (T)(scal[S_RZ] / scal[S_PQ]);
+  // breakdown (p.Ap not positive or not finite): no update, report below
+  const double pq = scal[S_PQ];
+  const bool brk = !(pq > 0.0) || !isfinite(pq);
+  const T alpha = brk ? (T)0 : (T)(scal[S_RZ] / pq);
   T prz = 0, prr = 0;
   for (int64_t i = blockIdx.x * (int64_t)kBlk + threadIdx.x; i < n; i += (int64_t)gridDim.x * kBlk) {
     const T pi = p[i];
@@ -256,16 +271,25 @@ __global__ void __launch_bounds__(kBlk) cg_update_k(int64_t n, T* __restrict__ x
     scal[S_RR] = rr;
     const int it = ++flags[F_ITER];
     const bool conv = rr <= scal[S_TOL2] * scal[S_BN2];
+    const bool bad = brk || !isfinite(rz) || !isfinite(rr);
     if (!ACC) {
-      if (conv || it >= flags[F_MAXIT]) {
+      if (conv || bad || it >= flags[F_MAXIT]) {
         flags[F_DONE] = 1;
-        flags[F_CONV] = conv ? 1 : 0;
+        flags[F_CONV] = (conv && !bad) ? 1 : 0;
       }
+    } else if (bad) {
+      // FP32 recurrence broke down (e.g. its residual reached exactly zero):
+      // replace the residual and restart the direction from it
+      flags[F_BRK] = 1;
+      flags[F_RU] = 1;
     } else {
       // FP32 recurrence: ask for an FP64 residual replacement when the
       // residual dropped by delta since the last one, or looks converged.
       const double rn = sqrt(rr);
       if (rn > scal[S_RMAX]) scal[S_RMAX] = rn;
+      // a recurrence that looks converged has spent its search directions:
+      // the replacement restarts from p = z (F_BRK = 2)
+      if (conv) flags[F_BRK] = 2;
       if (conv || it >= flags[F_MAXIT] || rn < scal[S_DELTA] * scal[S_RMAX]) flags[F_RU] = 1;
     }
   }
@@ -796,6 +820,10 @@ static int run_pcg32(elfel_sysmat* m, double rtol, int maxit, elfel_solve_stats*
     ELFEL_CUDA(c, cudaGraphLaunch(S->g_pcg32, c->stream));
     ELFEL_TRY(read_flags(c, S, hf));
     if (!hf[F_RU]) continue;
+    // recurrence residual before the replacement
+    ELFEL_CUDA(c, cudaMemcpyAsync(hsc, S->scal.p, sizeof(hsc), cudaMemcpyDeviceToHost, c->stream));
+    ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+    const double rr_rec = hsc[S_RR];
     // FP64 residual replacement
     fold_k<<<vg, kBlk, 0, c->stream>>>(nu, S->x64.p, S->xa32.p);
     ELFEL_TRY(launch_resid(c, S, S->x64.p, nullptr, S->b64.p, S->r64.p, red_area(S, 2), S_RR));
@@ -807,9 +835,16 @@ static int run_pcg32(elfel_sysmat* m, double rtol, int maxit, elfel_solve_stats*
       hf[F_CONV] = conv ? 1 : 0;
       break;
     }
+    // keep the search direction unless the FP32 recurrence broke down or its
+    // residual drifted far below the true one (then restart from p = z)
+    const int restart = hf[F_BRK] || !(rr_rec > 0.0) || !(rr_rec >= 1e-6 * hsc[S_RR]);
+    if (hf[F_BRK]) {
+      int z = 0;
+      ELFEL_CUDA(c, cudaMemcpyAsync(S->flags.p + F_BRK, &z, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    }
     demote_k<<<vg, kBlk, 0, c->stream>>>(nu, S->r64.p, S->r32.p);
     cg_start_k<float><<<vg, kBlk, 0, c->stream>>>(nu, S->r32.p, S->z32.p, S->p32.p, S->dinv32.p, red_area(S, 0),
-                                                  S->scal.p, S->flags.p, 0);
+                                                  S->scal.p, S->flags.p, restart);
     ELFEL_LAUNCH_CHECK(c);
     ELFEL_TRY(set_scal(c, S, S_RMAX, sqrt(hsc[S_RR])));
   }

@@ -67,6 +67,15 @@ ELFEL_API int elfel_ctx_memory(const elfel_ctx* ctx, int64_t* in_use, int64_t* p
 ELFEL_API int elfel_ctx_set_stream(elfel_ctx* ctx, void* cuda_stream);
 ELFEL_API void* elfel_ctx_stream(const elfel_ctx* ctx);
 ELFEL_API int elfel_ctx_synchronize(elfel_ctx* ctx);
+/* Phase timing (no reference counterpart; replaces the @time calls of
+ * examples/heat/poisson/t3.jl:72,78-79): enable = 1 clears and starts
+ * recording CUDA events around every kernel phase on the context's stream,
+ * enable = 0 stops.  profile_read returns, for the index-th distinct phase
+ * name, the summed device milliseconds and the number of launches;
+ * ELFEL_ERR_ARG past the last phase. */
+ELFEL_API int elfel_ctx_profile(elfel_ctx* ctx, int enable);
+ELFEL_API int elfel_ctx_profile_read(elfel_ctx* ctx, int index, char* name, int name_cap, double* total_ms,
+                                     int64_t* count);
 
 /* ------------------------------------- SysmatAssemblerSparse (COO mode) */
 /* SysmatAssemblerSparse(0.0): src/Assemblers.jl:58-60 */
