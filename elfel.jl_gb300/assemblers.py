@@ -265,15 +265,7 @@ class SysmatAssemblerGPU:
 
     def solve(self, T, nu, F=None, method="pcg32_ir", rtol=1e-10, maxit=200000):
         """solve!(T, K, F, nu) of test/test_heat.jl:73-76, on the device.  T is updated in place."""
-        st = N.SolveStats()
-        Fa = N.f64(F) if F is not None else None
-        if T.dtype != np.float64 or not T.flags.c_contiguous:
-            raise TypeError("T must be a contiguous float64 array")
-        rc = self._hd.lib.elfel_solve(self._hd.h, N.ptr(Fa), N.ptr(T), int(nu), _SOLVERS[method], float(rtol),
-                                      int(maxit), ctypes.byref(st))
-        stats = st.as_dict()
-        self._hd.check(rc)
-        return stats
+        return _solve_handle(self._hd, T, nu, F, method, rtol, maxit)
 
 
 def assemble_heat(am, elit, qpit, kappa, Q):
@@ -295,8 +287,35 @@ def assemble_stokes(am, uelit, pelit, qpit, mu):
     return am.stokes(mu)
 
 
-def solve(T, K, F, nu, method="pcg32_ir", rtol=1e-10, maxit=200000):
-    """solve!(T, K, F, nu): T[1:nu] = K[1:nu,1:nu] \\ (F - K*T)[1:nu] on the device."""
-    if not isinstance(K, SysmatAssemblerGPU):
-        raise TypeError("solve needs the device-resident system (SysmatAssemblerGPU)")
-    return K.solve(T, nu, F, method, rtol, maxit)
+def _solve_handle(hd, T, nu, F, method, rtol, maxit):
+    st = N.SolveStats()
+    Fa = N.f64(F) if F is not None else None
+    if T.dtype != np.float64 or not T.flags.c_contiguous:
+        raise TypeError("T must be a contiguous float64 array")
+    rc = hd.lib.elfel_solve(hd.h, N.ptr(Fa), N.ptr(T), int(nu), _SOLVERS[method], float(rtol), int(maxit),
+                            ctypes.byref(st))
+    stats = st.as_dict()
+    hd.check(rc)
+    return stats
+
+
+def solve(T, K, F, nu, method="pcg32_ir", rtol=1e-10, maxit=200000, ctx=None):
+    """solve!(T, K, F, nu): T[1:nu] = K[1:nu,1:nu] \\ (F - K*T)[1:nu] on the device.
+
+    K is the device-resident fused system (SysmatAssemblerGPU; F may be None),
+    a finished SysmatAssemblerSparse, or any host sparse matrix (uploaded).
+    T is updated in place; returns the solver statistics.
+    """
+    if isinstance(K, SysmatAssemblerGPU):
+        return K.solve(T, nu, F, method, rtol, maxit)
+    if F is None:
+        raise ValueError("F is required unless K is a fused device system")
+    if isinstance(K, SysmatAssemblerSparse):
+        if K._hd is None:
+            raise ValueError("finish the assembler before solving")
+        return _solve_handle(K._hd, T, nu, F, method, rtol, maxit)
+    A = sp.coo_matrix(K)
+    a = start(SysmatAssemblerSparse(0.0, ctx=ctx), A.shape[0], A.shape[1])
+    a._chunks.append((A.row.astype(np.int64) + 1, A.col.astype(np.int64) + 1, A.data.astype(np.float64)))
+    finish(a)
+    return _solve_handle(a._hd, T, nu, F, method, rtol, maxit)

@@ -29,6 +29,7 @@ struct Ctx {
   int64_t in_use = 0;       // bytes currently held
   int64_t peak = 0;
   int sm_count = kSMs;
+  int trace = 0;  // ELFEL_TRACE=1: solver progress on stderr
   std::string last_error;
   // scratch for deterministic reductions (partials + counters), grown on demand
   void* red_scratch = nullptr;

@@ -1,5 +1,6 @@
 // Context, device memory accounting, errors and the device scan.
 #include <stdarg.h>
+#include <stdlib.h>
 
 #include "common.cuh"
 
@@ -198,6 +199,8 @@ extern "C" int elfel_ctx_create(int device, int64_t mem_budget_bytes, elfel_ctx*
     return ELFEL_ERR_CUDA;
   }
   h->c.own_stream = h->c.stream;
+  const char* tr = getenv("ELFEL_TRACE");
+  h->c.trace = (tr && tr[0] == '1') ? 1 : 0;
   *out = h;
   return ELFEL_OK;
 }

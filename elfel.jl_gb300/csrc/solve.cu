@@ -17,10 +17,20 @@
 //                      diagonal preconditioner: |K_ii| on rows with a diagonal,
 //                      the pressure mass-matrix diagonal on Stokes pressure rows;
 //   ELFEL_MINRES32_IR  the same MINRES in FP32 inside FP64 iterative refinement.
-// All reductions are deterministic (per-block partials summed in block order).
-// Iterations are launched as CUDA graphs of kGraphIters iterations; kernels of
-// a finished (or paused) iteration exit at once, so the graph needs no host
-// decision per iteration.
+//
+// Matrix format of the iterations: SELL-C-sigma (Kreutzer et al. 2014) with
+// C = 32 rows per slice (one warp, one row per lane) and rows sorted by length
+// within windows of sigma = 256 rows, so a slice pads little.  Slices store
+// their entries column-major: entry j of the slice's rows is one coalesced
+// 32-wide load.  Column indices are 16-bit deltas from the row's own
+// (permuted) index when every delta fits, else 32-bit.  The Krylov vectors
+// live in the permuted order; the right-hand side goes in and the solution
+// comes out through the permutation.  Matrix streams use evict-first loads so
+// the gathered vector stays in L2.
+//
+// All reductions are deterministic (per-block partials added in a fixed
+// order).  Iterations run as CUDA graphs of kGraphIters iterations; kernels
+// of a finished (or paused) iteration exit at once.
 #include <math.h>
 
 #include <chrono>
@@ -31,6 +41,9 @@ namespace elfel {
 
 constexpr int kBlk = 256;
 constexpr int kGraphIters = 16;
+constexpr int kMaxRedBlocks = 2048;  // partial-sum slots per reduction area
+constexpr int kGridCap = 152 * 8;    // 8 resident 256-thread blocks per SM
+constexpr int kSigma = 256;          // row-sorting window
 
 // device scalar slots
 enum {
@@ -43,46 +56,77 @@ enum {
 enum { F_DONE = 0, F_RU, F_ITER, F_MAXIT, F_ROT, F_CONV, F_BRK, F_COUNT };
 
 struct Red4 {
-  double* partials;  // nblocks x 4
+  double* partials;  // kMaxRedBlocks x 4
   unsigned* ticket;
 };
 
+// CSR in the original order (rows 0..nu-1): free part (col < nu) and data part.
 struct Csr {
   int64_t nrows = 0, nnz = 0;
-  DBuf<int32_t> rowptr, col, map;
+  DBuf<int32_t> rowptr, col, map;  // map: index into the CSC values
+  DBuf<double> v64;
+  void release(Ctx* c) {
+    rowptr.release(c); col.release(c); map.release(c); v64.release(c);
+    nrows = nnz = 0;
+  }
+};
+
+// SELL-C-sigma matrix of the free-free block (permuted rows and columns).
+struct Sell {
+  int64_t nrows = 0, nslices = 0, nnz_pad = 0;
+  int d16 = 0;
+  DBuf<int64_t> sptr;   // nslices + 1 entry offsets
+  DBuf<int32_t> sw;     // slice widths
+  DBuf<int16_t> dcol;   // d16: column - row (permuted)
+  DBuf<int32_t> col;    // !d16: column (permuted)
+  DBuf<int32_t> map;    // CSC index of each entry, -1 for padding
+  DBuf<int32_t> perm;   // permuted row -> original row
   DBuf<double> v64;
   DBuf<float> v32;
   void release(Ctx* c) {
-    rowptr.release(c); col.release(c); map.release(c); v64.release(c); v32.release(c);
-    nrows = nnz = 0;
+    sptr.release(c); sw.release(c); dcol.release(c); col.release(c); map.release(c); perm.release(c);
+    v64.release(c); v32.release(c);
+    nrows = nslices = nnz_pad = 0;
   }
+};
+
+// POD view passed to kernels.
+struct SellView {
+  int64_t nrows, nslices;
+  const int64_t* sptr;
+  const int32_t* sw;
+  const int16_t* d16;
+  const int32_t* c32;
 };
 
 struct SolverData {
   int64_t nu = -1;
   const void* pattern_id = nullptr;
   int64_t pattern_nnz = -1;
-  uint64_t values_version = ~0ull;
-  int group = 4;  // lanes per row in the SpMV
+  int group = 4;  // lanes per row of the CSR kernels (lifting, final residual)
   Csr ff, fd;
-  DBuf<double> dinv64;
-  DBuf<float> dinv32;
-  DBuf<double> b64, x64, r64, T64, y64;
-  DBuf<double> v64[3], w64[3], z64, p64, q64;
-  DBuf<float> r32, p32, q32, z32, xa32;
-  DBuf<float> v32[3], w32[3], zz32, b32, x32;
+  Sell A;
+  // original order
+  DBuf<double> T64, bo64, xo64, ro64, dinvo;
+  // permuted order
+  DBuf<double> dinv64, b64, x64, r64, z64, p64, q64, y64;
+  DBuf<float> dinv32, r32, p32, q32, z32, xa32, zz32, b32, x32;
+  DBuf<double> v64[3], w64[3];
+  DBuf<float> v32[3], w32[3];
   DBuf<double> scal;
   DBuf<int> flags;
   DBuf<double> red;  // 3 reduction areas
   DBuf<unsigned> tickets;
   cudaGraphExec_t g_pcg64 = nullptr, g_pcg32 = nullptr, g_minres64 = nullptr, g_minres32 = nullptr;
+  SellView view() const {
+    return SellView{A.nrows, A.nslices, A.sptr.p, A.sw.p, A.d16 ? A.dcol.p : nullptr, A.d16 ? nullptr : A.col.p};
+  }
   void release(Ctx* c) {
-    ff.release(c); fd.release(c); dinv64.release(c); dinv32.release(c);
-    b64.release(c); x64.release(c); r64.release(c); T64.release(c); y64.release(c);
+    ff.release(c); fd.release(c); A.release(c);
+    for (DBuf<double>* b : {&T64, &bo64, &xo64, &ro64, &dinvo, &dinv64, &b64, &x64, &r64, &z64, &p64, &q64, &y64})
+      b->release(c);
+    for (DBuf<float>* b : {&dinv32, &r32, &p32, &q32, &z32, &xa32, &zz32, &b32, &x32}) b->release(c);
     for (int i = 0; i < 3; ++i) { v64[i].release(c); w64[i].release(c); v32[i].release(c); w32[i].release(c); }
-    z64.release(c); p64.release(c); q64.release(c);
-    r32.release(c); p32.release(c); q32.release(c); z32.release(c); xa32.release(c); zz32.release(c);
-    b32.release(c); x32.release(c);
     scal.release(c); flags.release(c); red.release(c); tickets.release(c);
     for (cudaGraphExec_t* g : {&g_pcg64, &g_pcg32, &g_minres64, &g_minres32})
       if (*g) { cudaGraphExecDestroy(*g); *g = nullptr; }
@@ -152,42 +196,56 @@ __device__ __forceinline__ bool grid_sums(double (&v)[NV], Red4 red, double (&to
   return threadIdx.x == 0;
 }
 
-// ------------------------------------------------------------------ SpMV
-// y = A x on rows [0, n); G lanes per row; returns per-thread partial of y.w
-// (w = x when wdot == nullptr).  Row loop is warp-uniform so the group
-// shuffles always see the whole warp.
-template <typename T, int G>
-__device__ __forceinline__ double spmv_rows(int64_t n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
-                                            const T* __restrict__ v, const T* __restrict__ x, T* __restrict__ y,
-                                            const T* __restrict__ wdot) {
-  constexpr int RPW = 32 / G;  // rows per warp step
+// ------------------------------------------------------------------ SELL SpMV
+template <bool D16>
+__device__ __forceinline__ int sell_col(const SellView& A, int64_t k, int64_t row) {
+  if (D16) return (int)row + (int)__ldcs(A.d16 + k);
+  return __ldcs(A.c32 + k);
+}
+
+// y = A x over all slices (one warp per slice, lane = row).  Returns the
+// thread's partial of y.w (w = x when wdot is null).
+template <typename T, bool D16>
+__device__ __forceinline__ double sell_rows(const SellView& A, const T* __restrict__ v, const T* __restrict__ x,
+                                            T* __restrict__ y, const T* __restrict__ wdot) {
   const int lane = threadIdx.x & 31;
-  const int g = lane / G, lg = lane % G;
   const int64_t warp = ((int64_t)blockIdx.x * kBlk + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * kBlk) >> 5;
   T part = 0;
-  for (int64_t r0 = warp * RPW; r0 < n; r0 += nwarps * RPW) {
-    const int64_t r = r0 + g;
-    T s = 0;
-    if (r < n) {
-      const int32_t b = rp[r], e = rp[r + 1];
-      for (int32_t k = b + lg; k < e; k += G) s += v[k] * __ldg(x + ci[k]);
+  for (int64_t s = warp; s < A.nslices; s += nwarps) {
+    const int64_t base = A.sptr[s] + lane;
+    const int64_t row = s * 32 + lane;
+    const int w = row < A.nrows ? A.sw[s] : 0;  // lanes past the last row stay idle
+    T a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    int j = 0;
+    for (; j + 3 < w; j += 4) {
+      const int64_t k = base + (int64_t)j * 32;
+      const int c0 = sell_col<D16>(A, k, row), c1 = sell_col<D16>(A, k + 32, row);
+      const int c2 = sell_col<D16>(A, k + 64, row), c3 = sell_col<D16>(A, k + 96, row);
+      const T v0 = __ldcs(v + k), v1 = __ldcs(v + k + 32), v2 = __ldcs(v + k + 64), v3 = __ldcs(v + k + 96);
+      a0 += v0 * __ldg(x + c0);
+      a1 += v1 * __ldg(x + c1);
+      a2 += v2 * __ldg(x + c2);
+      a3 += v3 * __ldg(x + c3);
     }
-#pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
-    if (r < n && lg == 0) {
-      y[r] = s;
-      part += s * (wdot ? wdot[r] : x[r]);
+    for (; j < w; ++j) {
+      const int64_t k = base + (int64_t)j * 32;
+      a0 += __ldcs(v + k) * __ldg(x + sell_col<D16>(A, k, row));
+    }
+    const T acc = (a0 + a1) + (a2 + a3);
+    if (row < A.nrows) {
+      y[row] = acc;
+      part += acc * (wdot ? wdot[row] : x[row]);
     }
   }
   return (double)part;
 }
 
-template <typename T, int G>
-__global__ void __launch_bounds__(kBlk) spmv_dot_k(int64_t n, const int32_t* __restrict__ rp,
-                                                  const int32_t* __restrict__ ci, const T* __restrict__ v,
-                                                  const T* __restrict__ x, T* __restrict__ y, Red4 red,
-                                                  double* scal, int slot, const int* flags) {
+// CG: q = A p, scal[slot] = p.q.  Skips a finished or paused iteration.
+template <typename T, bool D16>
+__global__ void __launch_bounds__(kBlk) sell_cg_spmv_k(SellView A, const T* __restrict__ v, const T* __restrict__ x,
+                                                      T* __restrict__ y, Red4 red, double* scal, int slot,
+                                                      int* flags) {
   if (flags[F_DONE] || flags[F_RU]) {
     // F_RU = 1: requested by the previous update; p has been advanced once by
     // cg_p_k since.  Mark it 2 so the rest of the graph skips until the host
@@ -195,13 +253,42 @@ __global__ void __launch_bounds__(kBlk) spmv_dot_k(int64_t n, const int32_t* __r
     if (flags[F_RU] == 1 && blockIdx.x == 0 && threadIdx.x == 0) ((volatile int*)flags)[F_RU] = 2;
     return;
   }
-  double p[1] = {spmv_rows<T, G>(n, rp, ci, v, x, y, nullptr)};
+  double p[1] = {sell_rows<T, D16>(A, v, x, y, nullptr)};
   double t[1];
   if (grid_sums<1>(p, red, t)) scal[slot] = t[0];
 }
 
-// r = b - A_ff x - A_fd t (FP64), rr partial; used for the lifted rhs and
-// for the true residual.  t may be null (no data columns).
+// r = b - A x in FP64 (permuted order), scal[slot] = r.r
+template <bool D16>
+__global__ void __launch_bounds__(kBlk) sell_resid_k(SellView A, const double* __restrict__ v,
+                                                    const double* __restrict__ x, const double* __restrict__ b,
+                                                    double* __restrict__ r, Red4 red, double* scal, int slot) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * kBlk + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * kBlk) >> 5;
+  double part = 0.0;
+  for (int64_t s = warp; s < A.nslices; s += nwarps) {
+    const int64_t base = A.sptr[s] + lane;
+    const int64_t row = s * 32 + lane;
+    const int w = row < A.nrows ? A.sw[s] : 0;
+    double acc = 0.0;
+    for (int j = 0; j < w; ++j) {
+      const int64_t k = base + (int64_t)j * 32;
+      acc += __ldcs(v + k) * __ldg(x + sell_col<D16>(A, k, row));
+    }
+    if (row < A.nrows) {
+      const double rv = b[row] - acc;
+      r[row] = rv;
+      part += rv * rv;
+    }
+  }
+  double p[1] = {part};
+  double t[1];
+  if (grid_sums<1>(p, red, t)) scal[slot] = t[0];
+}
+
+// CSR (original order): r = b - A_ff x - A_fd t, rr partial; for the lifted
+// right-hand side and the final residual.  t may be null (no data columns).
 template <int G>
 __global__ void __launch_bounds__(kBlk) resid64_k(int64_t n, const int32_t* __restrict__ rp,
                                                  const int32_t* __restrict__ ci, const double* __restrict__ v,
@@ -241,6 +328,14 @@ __global__ void __launch_bounds__(kBlk) resid64_k(int64_t n, const int32_t* __re
 }
 
 // ------------------------------------------------------------------ PCG
+// Grid-stride loops process 4 items per thread per step (independent loads in
+// flight).
+#define FOR4(i, n)                                                                                \
+  for (int64_t i##0 = blockIdx.x * (int64_t)kBlk + threadIdx.x, i##s = (int64_t)gridDim.x * kBlk; \
+       i##0 < (n); i##0 += 4 * i##s)                                                              \
+    _Pragma("unroll") for (int i##u = 0; i##u < 4; ++i##u)                                        \
+      if (const int64_t i = i##0 + i##u * i##s; i < (n))
+
 template <typename T, bool ACC>
 __global__ void __launch_bounds__(kBlk) cg_update_k(int64_t n, T* __restrict__ x, T* __restrict__ r,
                                                    const T* __restrict__ p, const T* __restrict__ q,
@@ -252,7 +347,7 @@ __global__ void __launch_bounds__(kBlk) cg_update_k(int64_t n, T* __restrict__ x
   const bool brk = !(pq > 0.0) || !isfinite(pq);
   const T alpha = brk ? (T)0 : (T)(scal[S_RZ] / pq);
   T prz = 0, prr = 0;
-  for (int64_t i = blockIdx.x * (int64_t)kBlk + threadIdx.x; i < n; i += (int64_t)gridDim.x * kBlk) {
+  FOR4(i, n) {
     const T pi = p[i];
     x[i] += alpha * pi;
     const T ri = r[i] - alpha * q[i];
@@ -302,17 +397,16 @@ __global__ void __launch_bounds__(kBlk) cg_p_k(int64_t n, T* __restrict__ p, con
   // recurrence's next direction when the residual gets replaced
   if (flags[F_DONE] || flags[F_RU] == 2) return;
   const T beta = (T)scal[S_BETA];
-  for (int64_t i = blockIdx.x * (int64_t)kBlk + threadIdx.x; i < n; i += (int64_t)gridDim.x * kBlk)
-    p[i] = z[i] + beta * p[i];
+  FOR4(i, n) p[i] = z[i] + beta * p[i];
 }
 
-// z = dinv r, p = z, rz = r.z, and the initial scalars.
+// z = dinv r, p = z (set_p), rz = r.z, and the initial scalars.
 template <typename T>
 __global__ void __launch_bounds__(kBlk) cg_start_k(int64_t n, const T* __restrict__ r, T* __restrict__ z,
                                                   T* __restrict__ p, const T* __restrict__ dinv, Red4 red,
                                                   double* scal, int* flags, int set_p) {
   T prz = 0;
-  for (int64_t i = blockIdx.x * (int64_t)kBlk + threadIdx.x; i < n; i += (int64_t)gridDim.x * kBlk) {
+  FOR4(i, n) {
     const T zi = dinv[i] * r[i];
     z[i] = zi;
     if (set_p) p[i] = zi;
@@ -328,20 +422,28 @@ __global__ void __launch_bounds__(kBlk) cg_start_k(int64_t n, const T* __restric
 
 // x64 += xacc, xacc = 0
 __global__ void fold_k(int64_t n, double* __restrict__ x, float* __restrict__ xa) {
-  for (int64_t i = blockIdx.x * (int64_t)kBlk + threadIdx.x; i < n; i += (int64_t)gridDim.x * kBlk) {
+  FOR4(i, n) {
     x[i] += (double)xa[i];
     xa[i] = 0.0f;
   }
 }
 
 __global__ void demote_k(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
-  for (int64_t i = blockIdx.x * (int64_t)kBlk + threadIdx.x; i < n; i += (int64_t)gridDim.x * kBlk)
-    b[i] = (float)a[i];
+  FOR4(i, n) b[i] = (float)a[i];
 }
 
 __global__ void add_scaled_k(int64_t n, double* __restrict__ x, const float* __restrict__ d) {
-  for (int64_t i = blockIdx.x * (int64_t)kBlk + threadIdx.x; i < n; i += (int64_t)gridDim.x * kBlk)
-    x[i] += (double)d[i];
+  FOR4(i, n) x[i] += (double)d[i];
+}
+
+// out[i] = in[perm[i]]  /  out[perm[i]] = in[i]
+__global__ void permute_in_k(int64_t n, const int32_t* __restrict__ perm, const double* __restrict__ in,
+                             double* __restrict__ out) {
+  FOR4(i, n) out[i] = in[perm[i]];
+}
+__global__ void permute_out_k(int64_t n, const int32_t* __restrict__ perm, const double* __restrict__ in,
+                              double* __restrict__ out) {
+  FOR4(i, n) out[perm[i]] = in[i];
 }
 
 // ------------------------------------------------------------------ MINRES
@@ -352,16 +454,14 @@ __global__ void add_scaled_k(int64_t n, double* __restrict__ x, const float* __r
 //                  z_{j+1} = minv v_{j+1}; gamn^2 = z_{j+1}.v_{j+1};
 //                  last block: Givens rotation scalars
 //   step 3 (upd):  w_{j+1} = (z_j - a3 w_{j-1} - a2 w_j)/a1;  x += c_{j+1} eta w_{j+1}
-// where z_j denotes the normalised z (z/gam), stored in zbuf[rot].
-template <typename T, int G>
-__global__ void __launch_bounds__(kBlk) mr_spmv_k(int64_t n, const int32_t* __restrict__ rp,
-                                                 const int32_t* __restrict__ ci, const T* __restrict__ v,
-                                                 T* const* zb, T* __restrict__ q, Red4 red, double* scal,
-                                                 const int* flags) {
+// where z_j is the normalised z (z/gam), kept in zb[rot].
+template <typename T, bool D16>
+__global__ void __launch_bounds__(kBlk) mr_spmv_k(SellView A, const T* __restrict__ v, T* const* zb,
+                                                 T* __restrict__ q, Red4 red, double* scal, const int* flags) {
   if (flags[F_DONE]) return;
   const int rot = flags[F_ROT];
   const T* z = zb[rot % 3];
-  double p[1] = {spmv_rows<T, G>(n, rp, ci, v, z, q, nullptr)};
+  double p[1] = {sell_rows<T, D16>(A, v, z, q, nullptr)};
   double t[1];
   if (grid_sums<1>(p, red, t)) scal[S_DEL] = t[0];
 }
@@ -378,7 +478,7 @@ __global__ void __launch_bounds__(kBlk) mr_vec_k(int64_t n, const T* __restrict_
   const double gam = scal[S_GAM], gamp = scal[S_GAMP];
   const T a = (T)(scal[S_DEL] / gam), bcoef = (T)(gamp > 0.0 ? gam / gamp : 0.0);
   T pz = 0;
-  for (int64_t i = blockIdx.x * (int64_t)kBlk + threadIdx.x; i < n; i += (int64_t)gridDim.x * kBlk) {
+  FOR4(i, n) {
     const T vv = q[i] - a * vj[i] - bcoef * vjm[i];
     vn[i] = vv;
     const T zz = minv[i] * vv;
@@ -406,7 +506,6 @@ __global__ void __launch_bounds__(kBlk) mr_vec_k(int64_t n, const T* __restrict_
     scal[S_S] = sn;
     scal[S_GAMP] = g;
     scal[S_GAMN] = gamn;
-    (void)sp;
   }
 }
 
@@ -426,7 +525,7 @@ __global__ void __launch_bounds__(kBlk) mr_upd_k(int64_t n, T* const* zb, T* con
   const T ce = (T)(scal[S_CN] * scal[S_ETA]);
   const double gamn = scal[S_GAMN];
   const T ig = (T)(gamn > 0.0 ? 1.0 / gamn : 0.0);
-  for (int64_t i = blockIdx.x * (int64_t)kBlk + threadIdx.x; i < n; i += (int64_t)gridDim.x * kBlk) {
+  FOR4(i, n) {
     const T w = (z[i] - a3 * wjm[i] - a2 * wj[i]) * ia1;
     wn[i] = w;
     x[i] += ce * w;
@@ -448,13 +547,13 @@ __global__ void mr_tail_k(double* scal, int* flags) {
   }
 }
 
-// MINRES start: v1 = r (in vb[0]), z1 = minv r, gam = sqrt(z.v), z normalised.
+// MINRES start: v1 = r (in vb[0]), z1 = minv r, gam = sqrt(z.v).
 template <typename T>
 __global__ void __launch_bounds__(kBlk) mr_start_k(int64_t n, const T* __restrict__ r, T* const* vb, T* const* zb,
                                                   T* const* wb, const T* __restrict__ minv, T* __restrict__ x,
                                                   Red4 red, double* scal, int* flags) {
   T pz = 0;
-  for (int64_t i = blockIdx.x * (int64_t)kBlk + threadIdx.x; i < n; i += (int64_t)gridDim.x * kBlk) {
+  FOR4(i, n) {
     const T ri = r[i];
     vb[0][i] = ri;
     vb[1][i] = 0;
@@ -486,11 +585,12 @@ __global__ void __launch_bounds__(kBlk) mr_start_k(int64_t n, const T* __restric
   }
 }
 
+// z1 /= gam (after mr_start_k)
 template <typename T>
 __global__ void scale_k(int64_t n, T* const* zb, const double* scal) {
   const double g = scal[S_GAM];
   const T ig = (T)(g > 0.0 ? 1.0 / g : 0.0);
-  for (int64_t i = blockIdx.x * (int64_t)kBlk + threadIdx.x; i < n; i += (int64_t)gridDim.x * kBlk) zb[0][i] *= ig;
+  FOR4(i, n) zb[0][i] *= ig;
 }
 
 // ------------------------------------------------------------------ setup
@@ -527,33 +627,148 @@ __global__ void to32_k(int64_t n, const int64_t* a, int32_t* b) {
     b[i] = (int32_t)a[i];
 }
 
-__global__ void gather_vals_k(int64_t n, const int32_t* map, const double* src, double* d64, float* d32) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double v = src[map[i]];
-    d64[i] = v;
-    if (d32) d32[i] = (float)v;
+// Sort the rows of each window of kSigma rows by length, longest first
+// (ties by row number): one 256-thread block per window, bitonic network.
+__global__ void __launch_bounds__(kSigma) sigma_sort_k(int64_t nu, const int32_t* __restrict__ rowptr,
+                                                      int32_t* __restrict__ perm) {
+  __shared__ unsigned long long key[kSigma];
+  const int64_t r = (int64_t)blockIdx.x * kSigma + threadIdx.x;
+  if (r < nu) {
+    const unsigned len = (unsigned)(rowptr[r + 1] - rowptr[r]);
+    key[threadIdx.x] = ((unsigned long long)(0x7fffffffu - len) << 32) | (unsigned long long)(unsigned)r;
+  } else {
+    key[threadIdx.x] = ~0ull;
+  }
+  __syncthreads();
+  for (int size = 2; size <= kSigma; size <<= 1) {
+    const int h = size >> 1;
+    if (threadIdx.x < kSigma / 2) {
+      const int t = threadIdx.x;
+      const int i = (t / h) * size + (t % h);
+      const int j = (t / h) * size + size - 1 - (t % h);
+      const unsigned long long a = key[i], b = key[j];
+      if (a > b) { key[i] = b; key[j] = a; }
+    }
+    __syncthreads();
+    for (int stride = h >> 1; stride > 0; stride >>= 1) {
+      if (threadIdx.x < kSigma / 2) {
+        const int t = threadIdx.x;
+        const int i = (t / stride) * 2 * stride + (t % stride);
+        const int j = i + stride;
+        const unsigned long long a = key[i], b = key[j];
+        if (a > b) { key[i] = b; key[j] = a; }
+      }
+      __syncthreads();
+    }
+  }
+  if (r < nu) perm[r] = (int32_t)(key[threadIdx.x] & 0xffffffffull);
+}
+
+__global__ void iperm_k(int64_t nu, const int32_t* perm, int32_t* iperm) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nu; i += (int64_t)gridDim.x * blockDim.x)
+    iperm[perm[i]] = (int32_t)i;
+}
+
+// slice width = length of its first (longest) row; w32[s] = 32 * width (for the scan)
+__global__ void slice_width_k(int64_t nu, int64_t nsl, const int32_t* rowptr, const int32_t* perm, int32_t* sw,
+                              int32_t* w32) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < nsl; s += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t r = perm[s * 32];
+    const int32_t w = rowptr[r + 1] - rowptr[r];
+    sw[s] = w;
+    w32[s] = 32 * w;
   }
 }
 
-// Preconditioner diagonal: 1/K_ii where K_ii != 0, else 1/aux_i where aux_i > 0
-// (pressure mass diagonal), else 1.  abs_diag selects |K_ii| (MINRES needs SPD M).
+// Fill one permuted row per thread; padding: map = -1, column = own row.
+__global__ void sell_fill_k(int64_t nu, int64_t nsl, const int32_t* __restrict__ rowptr,
+                            const int32_t* __restrict__ colff, const int32_t* __restrict__ mapff,
+                            const int32_t* __restrict__ perm, const int32_t* __restrict__ iperm,
+                            const int64_t* __restrict__ sptr, const int32_t* __restrict__ sw, int32_t* __restrict__ col,
+                            int32_t* __restrict__ map, int* __restrict__ wide) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nsl * 32;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = i >> 5;
+    const int lane = (int)(i & 31);
+    const int64_t base = sptr[s] + lane;
+    const int w = sw[s];
+    int len = 0;
+    int32_t rp = 0;
+    if (i < nu) {
+      const int32_t r = perm[i];
+      rp = rowptr[r];
+      len = rowptr[r + 1] - rp;
+    }
+    for (int j = 0; j < w; ++j) {
+      const int64_t k = base + (int64_t)j * 32;
+      if (j < len) {
+        const int32_t cn = iperm[colff[rp + j]];
+        col[k] = cn;
+        map[k] = mapff[rp + j];
+        const int64_t d = (int64_t)cn - i;
+        if (d < -32768 || d > 32767) atomicExch(wide, 1);
+      } else {
+        col[k] = i < nu ? (int32_t)i : 0;
+        map[k] = -1;
+      }
+    }
+  }
+}
+
+__global__ void sell_delta_k(int64_t npad, int64_t nu, const int64_t* sptr, int64_t nsl, const int32_t* col,
+                             int16_t* dcol) {
+  // entry k of slice s, lane l belongs to row s*32 + l; slices are contiguous
+  for (int64_t s = blockIdx.x * (int64_t)(blockDim.x / 32) + (threadIdx.x >> 5); s < nsl;
+       s += (int64_t)gridDim.x * (blockDim.x / 32)) {
+    const int lane = threadIdx.x & 31;
+    const int64_t row = s * 32 + lane;
+    for (int64_t k = sptr[s] + lane; k < sptr[s + 1]; k += 32)
+      dcol[k] = (int16_t)(row < nu ? (int64_t)col[k] - row : 0);
+  }
+}
+
+__global__ void sell_vals_k(int64_t npad, const int32_t* __restrict__ map, const double* __restrict__ vals,
+                            double* __restrict__ v64, float* __restrict__ v32) {
+  FOR4(k, npad) {
+    const int32_t m = map[k];
+    const double v = m >= 0 ? vals[m] : 0.0;
+    v64[k] = v;
+    v32[k] = (float)v;
+  }
+}
+
+__global__ void gather_vals_k(int64_t n, const int32_t* map, const double* src, double* d64) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    d64[i] = src[map[i]];
+}
+
+// Preconditioner diagonal in the original order: 1/K_ii where K_ii != 0, else
+// 1/aux_i where aux_i > 0 (pressure mass diagonal), else 1.  abs_diag selects
+// |K_ii| (MINRES needs an SPD preconditioner).
 __global__ void diag_k(int64_t nu, const int32_t* rp, const int32_t* ci, const double* v, const double* aux,
-                       int abs_diag, double* d64, float* d32) {
+                       int abs_diag, double* d) {
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nu; r += (int64_t)gridDim.x * blockDim.x) {
-    double d = 0.0;
+    double dv = 0.0;
     int32_t lo = rp[r], hi = rp[r + 1] - 1;
     while (lo <= hi) {
       int32_t mid = (lo + hi) >> 1;
-      if (ci[mid] == r) { d = v[mid]; break; }
+      if (ci[mid] == r) { dv = v[mid]; break; }
       if (ci[mid] < r) lo = mid + 1; else hi = mid - 1;
     }
-    if (abs_diag) d = fabs(d);
+    if (abs_diag) dv = fabs(dv);
     double inv;
-    if (d != 0.0) inv = 1.0 / d;
+    if (dv != 0.0) inv = 1.0 / dv;
     else if (aux && aux[r] > 0.0) inv = 1.0 / aux[r];
     else inv = 1.0;
-    d64[r] = inv;
-    d32[r] = (float)inv;
+    d[r] = inv;
+  }
+}
+
+__global__ void permute_diag_k(int64_t n, const int32_t* perm, const double* in, double* d64, float* d32) {
+  FOR4(i, n) {
+    const double v = in[perm[i]];
+    d64[i] = v;
+    d32[i] = (float)v;
   }
 }
 
@@ -566,17 +781,71 @@ static int pick_group(int64_t nnz, int64_t n) {
   return 32;
 }
 
-// Reduction-carrying kernels use at most kSMs*4 blocks (the partials area size).
-static unsigned vec_grid(Ctx* c, int64_t n) {
-  (void)c;
-  return grid_for(n, kBlk, (int64_t)kSMs * 4);
-}
+static unsigned vec_grid(int64_t n) { return grid_for(n, kBlk * 4, kGridCap); }
+static unsigned sell_grid(const SolverData* S) { return grid_for(S->A.nslices, kBlk / 32, kGridCap); }
 
 static Red4 red_area(SolverData* S, int k) {
   Red4 r;
-  r.partials = S->red.p + (size_t)k * kSMs * 4 * 4;
+  r.partials = S->red.p + (size_t)k * kMaxRedBlocks * 4;
   r.ticket = S->tickets.p + k;
   return r;
+}
+
+static int build_sell(Ctx* c, SolverData* S) {
+  const int64_t nu = S->nu;
+  Sell& A = S->A;
+  A.nrows = nu;
+  A.nslices = (nu + 31) / 32;
+  const int64_t nsl = A.nslices;
+  const int64_t nwin = (nu + kSigma - 1) / kSigma;
+  DBuf<int32_t> iperm, w32, col;
+  DBuf<int> wide;
+  ELFEL_TRY(A.perm.alloc(c, (size_t)nsl * 32));
+  ELFEL_TRY(iperm.alloc(c, (size_t)(nu > 0 ? nu : 1)));
+  // rows past nu in the last slice map to row 0 (never written)
+  ELFEL_CUDA(c, cudaMemsetAsync(A.perm.p, 0, sizeof(int32_t) * nsl * 32, c->stream));
+  sigma_sort_k<<<(unsigned)nwin, kSigma, 0, c->stream>>>(nu, S->ff.rowptr.p, A.perm.p);
+  iperm_k<<<grid_for(nu, 256, (int64_t)c->sm_count * 16), 256, 0, c->stream>>>(nu, A.perm.p, iperm.p);
+  ELFEL_LAUNCH_CHECK(c);
+  ELFEL_TRY(A.sw.alloc(c, (size_t)nsl));
+  ELFEL_TRY(w32.alloc(c, (size_t)nsl));
+  ELFEL_TRY(A.sptr.alloc(c, (size_t)nsl + 1));
+  slice_width_k<<<grid_for(nsl, 256), 256, 0, c->stream>>>(nu, nsl, S->ff.rowptr.p, A.perm.p, A.sw.p, w32.p);
+  ELFEL_LAUNCH_CHECK(c);
+  ELFEL_TRY(scan_counts_i32(c, w32.p, nsl, A.sptr.p));
+  w32.release(c);
+  ELFEL_CUDA(c, cudaMemcpyAsync(&A.nnz_pad, A.sptr.p + nsl, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+  ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (A.nnz_pad >= (int64_t)0x7fffffff) return fail(c, ELFEL_ERR_ARG, "solver matrix too large for 32-bit offsets");
+  const size_t np = (size_t)(A.nnz_pad > 0 ? A.nnz_pad : 1);
+  ELFEL_TRY(col.alloc(c, np));
+  ELFEL_TRY(A.map.alloc(c, np));
+  ELFEL_TRY(wide.alloc(c, 1));
+  ELFEL_CUDA(c, cudaMemsetAsync(wide.p, 0, sizeof(int), c->stream));
+  sell_fill_k<<<grid_for(nsl * 32, 256, (int64_t)c->sm_count * 16), 256, 0, c->stream>>>(
+      nu, nsl, S->ff.rowptr.p, S->ff.col.p, S->ff.map.p, A.perm.p, iperm.p, A.sptr.p, A.sw.p, col.p, A.map.p, wide.p);
+  ELFEL_LAUNCH_CHECK(c);
+  int hw = 0;
+  ELFEL_CUDA(c, cudaMemcpyAsync(&hw, wide.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+  wide.release(c);
+  iperm.release(c);
+  if (!hw) {
+    A.d16 = 1;
+    ELFEL_TRY(A.dcol.alloc(c, np));
+    sell_delta_k<<<grid_for(nsl, 8, (int64_t)c->sm_count * 16), 256, 0, c->stream>>>(A.nnz_pad, nu, A.sptr.p, nsl,
+                                                                                    col.p, A.dcol.p);
+    ELFEL_LAUNCH_CHECK(c);
+    col.release(c);
+  } else {
+    A.d16 = 0;
+    A.col = col;
+    col.p = nullptr;
+    col.n = 0;
+  }
+  ELFEL_TRY(A.v64.alloc(c, np));
+  ELFEL_TRY(A.v32.alloc(c, np));
+  return ELFEL_OK;
 }
 
 static int build_solver(elfel_sysmat* m, int64_t nu) {
@@ -585,6 +854,7 @@ static int build_solver(elfel_sysmat* m, int64_t nu) {
   SolverData* S = m->solver;
   if (S->nu == nu && S->pattern_id == (const void*)m->P.rowval.p && S->pattern_nnz == m->P.nnz) return ELFEL_OK;
   S->release(c);
+  Phase ph(c, "solver_setup");
   const int64_t n = m->nrow;
   // Full CSR of K through the pattern builder: slots = CSC nonzeros, with
   // row and column roles swapped so that the CSC of K^T (= CSR of K) comes out.
@@ -630,7 +900,6 @@ static int build_solver(elfel_sysmat* m, int64_t nu) {
   ELFEL_TRY(S->fd.col.alloc(c, (size_t)(tfd > 0 ? tfd : 1)));
   ELFEL_TRY(S->fd.map.alloc(c, (size_t)(tfd > 0 ? tfd : 1)));
   ELFEL_TRY(S->ff.v64.alloc(c, (size_t)(tff > 0 ? tff : 1)));
-  ELFEL_TRY(S->ff.v32.alloc(c, (size_t)(tff > 0 ? tff : 1)));
   ELFEL_TRY(S->fd.v64.alloc(c, (size_t)(tfd > 0 ? tfd : 1)));
   to32_k<<<grid_for(nu + 1, 256), 256, 0, c->stream>>>(nu + 1, pff.p, S->ff.rowptr.p);
   to32_k<<<grid_for(nu + 1, 256), 256, 0, c->stream>>>(nu + 1, pfd.p, S->fd.rowptr.p);
@@ -640,88 +909,62 @@ static int build_solver(elfel_sysmat* m, int64_t nu) {
   ELFEL_LAUNCH_CHECK(c);
   R.release(c);
   nff.release(c); nfd.release(c); pff.release(c); pfd.release(c);
+  S->nu = nu;
+  if (nu > 0) ELFEL_TRY(build_sell(c, S));
   const size_t vn = (size_t)(nu > 0 ? nu : 1);
-  ELFEL_TRY(S->dinv64.alloc(c, vn));
-  ELFEL_TRY(S->dinv32.alloc(c, vn));
-  for (DBuf<double>* b : {&S->b64, &S->x64, &S->r64, &S->z64, &S->p64, &S->q64, &S->y64}) ELFEL_TRY(b->alloc(c, vn));
-  for (DBuf<float>* b : {&S->r32, &S->p32, &S->q32, &S->z32, &S->xa32, &S->zz32, &S->b32, &S->x32})
+  for (DBuf<double>* b : {&S->bo64, &S->xo64, &S->ro64, &S->dinvo, &S->dinv64, &S->b64, &S->x64, &S->r64, &S->z64,
+                          &S->p64, &S->q64, &S->y64})
+    ELFEL_TRY(b->alloc(c, vn));
+  for (DBuf<float>* b : {&S->dinv32, &S->r32, &S->p32, &S->q32, &S->z32, &S->xa32, &S->zz32, &S->b32, &S->x32})
     ELFEL_TRY(b->alloc(c, vn));
   ELFEL_TRY(S->T64.alloc(c, (size_t)(n > 0 ? n : 1)));
   ELFEL_TRY(S->scal.alloc(c, S_COUNT));
   ELFEL_TRY(S->flags.alloc(c, F_COUNT));
-  ELFEL_TRY(S->red.alloc(c, (size_t)3 * kSMs * 4 * 4));
+  ELFEL_TRY(S->red.alloc(c, (size_t)3 * kMaxRedBlocks * 4));
   ELFEL_TRY(S->tickets.alloc(c, 4));
   ELFEL_CUDA(c, cudaMemsetAsync(S->tickets.p, 0, sizeof(unsigned) * 4, c->stream));
   ELFEL_CUDA(c, cudaMemsetAsync(S->scal.p, 0, sizeof(double) * S_COUNT, c->stream));
   ELFEL_CUDA(c, cudaMemsetAsync(S->flags.p, 0, sizeof(int) * F_COUNT, c->stream));
   S->group = pick_group(tff, nu);
-  S->nu = nu;
   S->pattern_id = m->P.rowval.p;
   S->pattern_nnz = m->P.nnz;
-  S->values_version = ~0ull;
   ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
   return ELFEL_OK;
 }
 
+// Values of the solver matrices from the CSC values (FP64, and the FP32 copy).
 static int refresh_values(elfel_sysmat* m, int abs_diag) {
   Ctx* c = &m->h->c;
   SolverData* S = m->solver;
   const int64_t nu = S->nu;
+  Phase ph(c, "solver_values");
   if (S->ff.nnz)
     gather_vals_k<<<grid_for(S->ff.nnz, 256, (int64_t)c->sm_count * 16), 256, 0, c->stream>>>(
-        S->ff.nnz, S->ff.map.p, m->vals.p, S->ff.v64.p, S->ff.v32.p);
+        S->ff.nnz, S->ff.map.p, m->vals.p, S->ff.v64.p);
   if (S->fd.nnz)
     gather_vals_k<<<grid_for(S->fd.nnz, 256, (int64_t)c->sm_count * 16), 256, 0, c->stream>>>(
-        S->fd.nnz, S->fd.map.p, m->vals.p, S->fd.v64.p, nullptr);
+        S->fd.nnz, S->fd.map.p, m->vals.p, S->fd.v64.p);
+  if (S->A.nnz_pad)
+    sell_vals_k<<<vec_grid(S->A.nnz_pad), kBlk, 0, c->stream>>>(S->A.nnz_pad, S->A.map.p, m->vals.p, S->A.v64.p,
+                                                                 S->A.v32.p);
   const double* aux = (m->fused && m->F.physics == ELFEL_STOKES) ? m->F.pmass_diag.p : nullptr;
-  if (nu > 0)
-    diag_k<<<grid_for(nu, 256, (int64_t)c->sm_count * 16), 256, 0, c->stream>>>(
-        nu, S->ff.rowptr.p, S->ff.col.p, S->ff.v64.p, aux, abs_diag, S->dinv64.p, S->dinv32.p);
+  if (nu > 0) {
+    diag_k<<<grid_for(nu, 256, (int64_t)c->sm_count * 16), 256, 0, c->stream>>>(nu, S->ff.rowptr.p, S->ff.col.p,
+                                                                                S->ff.v64.p, aux, abs_diag,
+                                                                                S->dinvo.p);
+    permute_diag_k<<<vec_grid(nu), kBlk, 0, c->stream>>>(nu, S->A.perm.p, S->dinvo.p, S->dinv64.p, S->dinv32.p);
+  }
   ELFEL_LAUNCH_CHECK(c);
-  S->values_version = m->values_version;
   return ELFEL_OK;
 }
 
-// Launch helpers dispatching on the group size.
-template <typename T>
-static void launch_spmv_dot(Ctx* c, SolverData* S, const T* v, const T* x, T* y, Red4 red, int slot) {
-  const unsigned grid = vec_grid(c, S->nu * S->group);
-  const int64_t n = S->nu;
-  const int32_t *rp = S->ff.rowptr.p, *ci = S->ff.col.p;
-  double* sc = S->scal.p;
-  const int* fl = S->flags.p;
-  switch (S->group) {
-    case 2: spmv_dot_k<T, 2><<<grid, kBlk, 0, c->stream>>>(n, rp, ci, v, x, y, red, sc, slot, fl); break;
-    case 4: spmv_dot_k<T, 4><<<grid, kBlk, 0, c->stream>>>(n, rp, ci, v, x, y, red, sc, slot, fl); break;
-    case 8: spmv_dot_k<T, 8><<<grid, kBlk, 0, c->stream>>>(n, rp, ci, v, x, y, red, sc, slot, fl); break;
-    case 16: spmv_dot_k<T, 16><<<grid, kBlk, 0, c->stream>>>(n, rp, ci, v, x, y, red, sc, slot, fl); break;
-    default: spmv_dot_k<T, 32><<<grid, kBlk, 0, c->stream>>>(n, rp, ci, v, x, y, red, sc, slot, fl); break;
-  }
-}
-
-template <typename T>
-static void launch_mr_spmv(Ctx* c, SolverData* S, const T* v, T* const* zb, T* q, Red4 red) {
-  const unsigned grid = vec_grid(c, S->nu * S->group);
-  const int64_t n = S->nu;
-  const int32_t *rp = S->ff.rowptr.p, *ci = S->ff.col.p;
-  double* sc = S->scal.p;
-  const int* fl = S->flags.p;
-  switch (S->group) {
-    case 2: mr_spmv_k<T, 2><<<grid, kBlk, 0, c->stream>>>(n, rp, ci, v, zb, q, red, sc, fl); break;
-    case 4: mr_spmv_k<T, 4><<<grid, kBlk, 0, c->stream>>>(n, rp, ci, v, zb, q, red, sc, fl); break;
-    case 8: mr_spmv_k<T, 8><<<grid, kBlk, 0, c->stream>>>(n, rp, ci, v, zb, q, red, sc, fl); break;
-    case 16: mr_spmv_k<T, 16><<<grid, kBlk, 0, c->stream>>>(n, rp, ci, v, zb, q, red, sc, fl); break;
-    default: mr_spmv_k<T, 32><<<grid, kBlk, 0, c->stream>>>(n, rp, ci, v, zb, q, red, sc, fl); break;
-  }
-}
-
-// r = b - A x (with the data-column part when t != null); scal[slot] = r.r
+// CSR residual in the original order: r = b - A_ff x (- A_fd t); scal[slot] = r.r
 static int launch_resid(Ctx* c, SolverData* S, const double* x, const double* t, const double* b, double* r,
                         Red4 red, int slot) {
-  const unsigned grid = vec_grid(c, S->nu * S->group);
+  const unsigned grid = grid_for(S->nu * S->group, kBlk, kGridCap);
   const int64_t n = S->nu;
   const Csr &A = S->ff, &D = S->fd;
-#define RES_ARGS                                                                                                  \
+#define RES_ARGS \
   n, A.rowptr.p, A.col.p, A.v64.p, x, D.rowptr.p, D.col.p, D.v64.p, t, S->nu, b, r, red, S->scal.p, slot
   switch (S->group) {
     case 2: resid64_k<2><<<grid, kBlk, 0, c->stream>>>(RES_ARGS); break;
@@ -733,6 +976,35 @@ static int launch_resid(Ctx* c, SolverData* S, const double* x, const double* t,
 #undef RES_ARGS
   ELFEL_LAUNCH_CHECK(c);
   return ELFEL_OK;
+}
+
+// SELL residual in the permuted order (FP64).
+static int launch_sell_resid(Ctx* c, SolverData* S, const double* x, const double* b, double* r, Red4 red, int slot) {
+  const SellView V = S->view();
+  if (S->A.d16)
+    sell_resid_k<true><<<sell_grid(S), kBlk, 0, c->stream>>>(V, S->A.v64.p, x, b, r, red, S->scal.p, slot);
+  else
+    sell_resid_k<false><<<sell_grid(S), kBlk, 0, c->stream>>>(V, S->A.v64.p, x, b, r, red, S->scal.p, slot);
+  ELFEL_LAUNCH_CHECK(c);
+  return ELFEL_OK;
+}
+
+template <typename T>
+static void launch_cg_spmv(Ctx* c, SolverData* S, const T* v, const T* x, T* y, Red4 red, int slot) {
+  const SellView V = S->view();
+  if (S->A.d16)
+    sell_cg_spmv_k<T, true><<<sell_grid(S), kBlk, 0, c->stream>>>(V, v, x, y, red, S->scal.p, slot, S->flags.p);
+  else
+    sell_cg_spmv_k<T, false><<<sell_grid(S), kBlk, 0, c->stream>>>(V, v, x, y, red, S->scal.p, slot, S->flags.p);
+}
+
+template <typename T>
+static void launch_mr_spmv(Ctx* c, SolverData* S, const T* v, T* const* zb, T* q, Red4 red) {
+  const SellView V = S->view();
+  if (S->A.d16)
+    mr_spmv_k<T, true><<<sell_grid(S), kBlk, 0, c->stream>>>(V, v, zb, q, red, S->scal.p, S->flags.p);
+  else
+    mr_spmv_k<T, false><<<sell_grid(S), kBlk, 0, c->stream>>>(V, v, zb, q, red, S->scal.p, S->flags.p);
 }
 
 static int read_flags(Ctx* c, SolverData* S, int* h) {
@@ -763,21 +1035,20 @@ static int capture(Ctx* c, cudaGraphExec_t* out, F&& body) {
 }
 
 // ------------------------------------------------------------------ drivers
-static int run_pcg64(elfel_sysmat* m, double rtol, int maxit, elfel_solve_stats* st) {
+static int run_pcg64(elfel_sysmat* m, int maxit, elfel_solve_stats* st) {
   Ctx* c = &m->h->c;
   SolverData* S = m->solver;
   const int64_t nu = S->nu;
-  const unsigned vg = vec_grid(c, nu);
-  // x = 0, r = b
+  const unsigned vg = vec_grid(nu);
   ELFEL_CUDA(c, cudaMemsetAsync(S->x64.p, 0, sizeof(double) * nu, c->stream));
   ELFEL_CUDA(c, cudaMemcpyAsync(S->r64.p, S->b64.p, sizeof(double) * nu, cudaMemcpyDeviceToDevice, c->stream));
-  int hf[F_COUNT] = {0, 0, 0, maxit, 0, 0};
+  int hf[F_COUNT] = {0, 0, 0, maxit, 0, 0, 0};
   ELFEL_CUDA(c, cudaMemcpyAsync(S->flags.p, hf, sizeof(hf), cudaMemcpyHostToDevice, c->stream));
   cg_start_k<double><<<vg, kBlk, 0, c->stream>>>(nu, S->r64.p, S->z64.p, S->p64.p, S->dinv64.p, red_area(S, 0),
                                                  S->scal.p, S->flags.p, 1);
   ELFEL_LAUNCH_CHECK(c);
   ELFEL_TRY(capture(c, &S->g_pcg64, [&]() {
-    launch_spmv_dot<double>(c, S, S->ff.v64.p, S->p64.p, S->q64.p, red_area(S, 0), S_PQ);
+    launch_cg_spmv<double>(c, S, S->A.v64.p, S->p64.p, S->q64.p, red_area(S, 0), S_PQ);
     cg_update_k<double, false><<<vg, kBlk, 0, c->stream>>>(nu, S->x64.p, S->r64.p, S->p64.p, S->q64.p, S->z64.p,
                                                             S->dinv64.p, red_area(S, 1), S->scal.p, S->flags.p);
     cg_p_k<double><<<vg, kBlk, 0, c->stream>>>(nu, S->p64.p, S->z64.p, S->scal.p, S->flags.p);
@@ -789,36 +1060,42 @@ static int run_pcg64(elfel_sysmat* m, double rtol, int maxit, elfel_solve_stats*
   }
   st->iterations = hf[F_ITER];
   st->refinements = 0;
-  // true residual
-  ELFEL_TRY(launch_resid(c, S, S->x64.p, nullptr, S->b64.p, S->r64.p, red_area(S, 2), S_RR));
   return ELFEL_OK;
 }
 
-static int run_pcg32(elfel_sysmat* m, double rtol, int maxit, elfel_solve_stats* st) {
+static int run_pcg32(elfel_sysmat* m, int maxit, elfel_solve_stats* st) {
   Ctx* c = &m->h->c;
   SolverData* S = m->solver;
   const int64_t nu = S->nu;
-  const unsigned vg = vec_grid(c, nu);
+  const unsigned vg = vec_grid(nu);
   ELFEL_CUDA(c, cudaMemsetAsync(S->x64.p, 0, sizeof(double) * nu, c->stream));
   ELFEL_CUDA(c, cudaMemsetAsync(S->xa32.p, 0, sizeof(float) * nu, c->stream));
   ELFEL_CUDA(c, cudaMemcpyAsync(S->r64.p, S->b64.p, sizeof(double) * nu, cudaMemcpyDeviceToDevice, c->stream));
   demote_k<<<vg, kBlk, 0, c->stream>>>(nu, S->r64.p, S->r32.p);
-  int hf[F_COUNT] = {0, 0, 0, maxit, 0, 0};
+  int hf[F_COUNT] = {0, 0, 0, maxit, 0, 0, 0};
   ELFEL_CUDA(c, cudaMemcpyAsync(S->flags.p, hf, sizeof(hf), cudaMemcpyHostToDevice, c->stream));
   cg_start_k<float><<<vg, kBlk, 0, c->stream>>>(nu, S->r32.p, S->z32.p, S->p32.p, S->dinv32.p, red_area(S, 0),
                                                 S->scal.p, S->flags.p, 1);
   ELFEL_LAUNCH_CHECK(c);
   ELFEL_TRY(capture(c, &S->g_pcg32, [&]() {
-    launch_spmv_dot<float>(c, S, S->ff.v32.p, S->p32.p, S->q32.p, red_area(S, 0), S_PQ);
+    launch_cg_spmv<float>(c, S, S->A.v32.p, S->p32.p, S->q32.p, red_area(S, 0), S_PQ);
     cg_update_k<float, true><<<vg, kBlk, 0, c->stream>>>(nu, S->xa32.p, S->r32.p, S->p32.p, S->q32.p, S->z32.p,
                                                          S->dinv32.p, red_area(S, 1), S->scal.p, S->flags.p);
     cg_p_k<float><<<vg, kBlk, 0, c->stream>>>(nu, S->p32.p, S->z32.p, S->scal.p, S->flags.p);
   }));
   int refinements = 0;
+  int launches = 0;
   double hsc[S_COUNT];
   while (true) {
     ELFEL_CUDA(c, cudaGraphLaunch(S->g_pcg32, c->stream));
     ELFEL_TRY(read_flags(c, S, hf));
+    ++launches;
+    if (c->trace && (launches % 256) == 0) {
+      ELFEL_CUDA(c, cudaMemcpyAsync(hsc, S->scal.p, sizeof(hsc), cudaMemcpyDeviceToHost, c->stream));
+      ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+      fprintf(stderr, "[elfel pcg32] it %d recurrence %.3e rmax %.3e flags ru %d brk %d\n", hf[F_ITER],
+              sqrt(hsc[S_RR]), hsc[S_RMAX], hf[F_RU], hf[F_BRK]);
+    }
     if (!hf[F_RU]) continue;
     // recurrence residual before the replacement
     ELFEL_CUDA(c, cudaMemcpyAsync(hsc, S->scal.p, sizeof(hsc), cudaMemcpyDeviceToHost, c->stream));
@@ -826,18 +1103,22 @@ static int run_pcg32(elfel_sysmat* m, double rtol, int maxit, elfel_solve_stats*
     const double rr_rec = hsc[S_RR];
     // FP64 residual replacement
     fold_k<<<vg, kBlk, 0, c->stream>>>(nu, S->x64.p, S->xa32.p);
-    ELFEL_TRY(launch_resid(c, S, S->x64.p, nullptr, S->b64.p, S->r64.p, red_area(S, 2), S_RR));
+    ELFEL_TRY(launch_sell_resid(c, S, S->x64.p, S->b64.p, S->r64.p, red_area(S, 2), S_RR));
     ELFEL_CUDA(c, cudaMemcpyAsync(hsc, S->scal.p, sizeof(hsc), cudaMemcpyDeviceToHost, c->stream));
     ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
     ++refinements;
     const bool conv = hsc[S_RR] <= hsc[S_TOL2] * hsc[S_BN2];
+    // keep the search direction unless the FP32 recurrence broke down or its
+    // residual drifted far below the true one (then restart from p = z)
+    const int restart = hf[F_BRK] || !(rr_rec > 0.0) || !(rr_rec >= 1e-6 * hsc[S_RR]);
+    if (c->trace)
+      fprintf(stderr, "[elfel pcg32] it %d replace %d: recurrence %.3e true %.3e (rel %.3e) brk %d restart %d\n",
+              hf[F_ITER], refinements, sqrt(rr_rec), sqrt(hsc[S_RR]), sqrt(hsc[S_RR] / hsc[S_BN2]), hf[F_BRK],
+              restart);
     if (conv || hf[F_ITER] >= maxit) {
       hf[F_CONV] = conv ? 1 : 0;
       break;
     }
-    // keep the search direction unless the FP32 recurrence broke down or its
-    // residual drifted far below the true one (then restart from p = z)
-    const int restart = hf[F_BRK] || !(rr_rec > 0.0) || !(rr_rec >= 1e-6 * hsc[S_RR]);
     if (hf[F_BRK]) {
       int z = 0;
       ELFEL_CUDA(c, cudaMemcpyAsync(S->flags.p + F_BRK, &z, sizeof(int), cudaMemcpyHostToDevice, c->stream));
@@ -853,13 +1134,13 @@ static int run_pcg32(elfel_sysmat* m, double rtol, int maxit, elfel_solve_stats*
   return ELFEL_OK;
 }
 
-// MINRES on A x = b (precision T), x returned in xT.  Returns iterations.
+// MINRES on A x = b (precision T, permuted order).
 template <typename T>
 static int run_minres(Ctx* c, SolverData* S, const T* v, const T* minv, const T* b, T* x, T* const* vb, T* const* zb,
                       T* const* wb, T* q, double rtol, int maxit, cudaGraphExec_t* graph, int* iters, int* conv) {
   const int64_t nu = S->nu;
-  const unsigned vg = vec_grid(c, nu);
-  int hf[F_COUNT] = {0, 0, 0, maxit, 0, 0};
+  const unsigned vg = vec_grid(nu);
+  int hf[F_COUNT] = {0, 0, 0, maxit, 0, 0, 0};
   ELFEL_CUDA(c, cudaMemcpyAsync(S->flags.p, hf, sizeof(hf), cudaMemcpyHostToDevice, c->stream));
   ELFEL_TRY(set_scal(c, S, S_TOL2, rtol * rtol));
   mr_start_k<T><<<vg, kBlk, 0, c->stream>>>(nu, b, vb, zb, wb, minv, x, red_area(S, 0), S->scal.p, S->flags.p);
@@ -885,11 +1166,6 @@ static int run_minres(Ctx* c, SolverData* S, const T* v, const T* minv, const T*
 
 using namespace elfel;
 
-__global__ void lift_prep_k(int64_t n, const double* T, double* y) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    y[i] = T[i];
-}
-
 extern "C" int elfel_solve(elfel_sysmat* m, const double* Fh, double* T, int64_t nu, int32_t method, double rtol,
                            int32_t maxit, elfel_solve_stats* stats) {
   if (!m || !m->h) return ELFEL_ERR_ARG;
@@ -913,7 +1189,7 @@ extern "C" int elfel_solve(elfel_sysmat* m, const double* Fh, double* T, int64_t
     if (stats) *stats = st;
     return ELFEL_OK;
   }
-  // lifted right-hand side: b = F_f - K_ff T_f - K_fd T_d
+  // lifted right-hand side in the original order: b = F_f - K_ff T_f - K_fd T_d
   ELFEL_CUDA(c, cudaMemcpyAsync(S->T64.p, T, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
   double* Fd = m->rhs.p;
   DBuf<double> Ftmp;
@@ -922,8 +1198,10 @@ extern "C" int elfel_solve(elfel_sysmat* m, const double* Fh, double* T, int64_t
     ELFEL_CUDA(c, cudaMemcpyAsync(Ftmp.p, Fh, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
     Fd = Ftmp.p;
   }
-  ELFEL_TRY(launch_resid(c, S, S->T64.p, S->T64.p + nu, Fd, S->b64.p, red_area(S, 2), S_BN2));
+  ELFEL_TRY(launch_resid(c, S, S->T64.p, S->T64.p + nu, Fd, S->bo64.p, red_area(S, 2), S_BN2));
   Ftmp.release(c);
+  permute_in_k<<<vec_grid(nu), kBlk, 0, c->stream>>>(nu, S->A.perm.p, S->bo64.p, S->b64.p);
+  ELFEL_LAUNCH_CHECK(c);
   double bn2 = 0.0;
   ELFEL_CUDA(c, cudaMemcpyAsync(&bn2, S->scal.p + S_BN2, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -935,10 +1213,13 @@ extern "C" int elfel_solve(elfel_sysmat* m, const double* Fh, double* T, int64_t
     ELFEL_CUDA(c, cudaMemsetAsync(S->x64.p, 0, sizeof(double) * nu, c->stream));
     st.converged = 1;
   } else if (method == ELFEL_PCG64) {
-    rc = run_pcg64(m, rtol, maxit, &st);
+    Phase ph(c, "pcg64");
+    rc = run_pcg64(m, maxit, &st);
   } else if (method == ELFEL_PCG32_IR) {
-    rc = run_pcg32(m, rtol, maxit, &st);
+    Phase ph(c, "pcg32_ir");
+    rc = run_pcg32(m, maxit, &st);
   } else if (method == ELFEL_MINRES64) {
+    Phase ph(c, "minres64");
     for (int i = 0; i < 3; ++i) {
       if (!S->v64[i].p) ELFEL_TRY(S->v64[i].alloc(c, (size_t)nu));
       if (!S->w64[i].p) ELFEL_TRY(S->w64[i].alloc(c, (size_t)nu));
@@ -953,27 +1234,28 @@ extern "C" int elfel_solve(elfel_sysmat* m, const double* Fh, double* T, int64_t
       S->g_minres64 = nullptr;
     }
     int it = 0, conv = 0;
-    rc = run_minres<double>(c, S, S->ff.v64.p, S->dinv64.p, S->b64.p, S->x64.p, dptr.p, dptr.p + 3, dptr.p + 6,
+    rc = run_minres<double>(c, S, S->A.v64.p, S->dinv64.p, S->b64.p, S->x64.p, dptr.p, dptr.p + 3, dptr.p + 6,
                             S->q64.p, rtol, maxit, &S->g_minres64, &it, &conv);
     ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
     dptr.release(c);
     st.iterations = it;
   } else {
     // FP32 MINRES inside FP64 iterative refinement
+    Phase ph(c, "minres32_ir");
     for (int i = 0; i < 3; ++i) {
       if (!S->v32[i].p) ELFEL_TRY(S->v32[i].alloc(c, (size_t)nu));
       if (!S->w32[i].p) ELFEL_TRY(S->w32[i].alloc(c, (size_t)nu));
     }
-    float* zb[3] = {S->z32.p, S->p32.p, S->zz32.p};
     DBuf<float*> dptr;
     ELFEL_TRY(dptr.alloc(c, 9));
-    float* hp[9] = {S->v32[0].p, S->v32[1].p, S->v32[2].p, zb[0], zb[1], zb[2], S->w32[0].p, S->w32[1].p, S->w32[2].p};
+    float* hp[9] = {S->v32[0].p, S->v32[1].p, S->v32[2].p, S->z32.p, S->p32.p, S->zz32.p,
+                    S->w32[0].p, S->w32[1].p, S->w32[2].p};
     ELFEL_CUDA(c, cudaMemcpyAsync(dptr.p, hp, sizeof(hp), cudaMemcpyHostToDevice, c->stream));
     if (S->g_minres32) {
       cudaGraphExecDestroy(S->g_minres32);
       S->g_minres32 = nullptr;
     }
-    const unsigned vg = vec_grid(c, nu);
+    const unsigned vg = vec_grid(nu);
     ELFEL_CUDA(c, cudaMemsetAsync(S->x64.p, 0, sizeof(double) * nu, c->stream));
     ELFEL_CUDA(c, cudaMemcpyAsync(S->r64.p, S->b64.p, sizeof(double) * nu, cudaMemcpyDeviceToDevice, c->stream));
     double rr = bn2;
@@ -982,15 +1264,17 @@ extern "C" int elfel_solve(elfel_sysmat* m, const double* Fh, double* T, int64_t
     while (true) {
       demote_k<<<vg, kBlk, 0, c->stream>>>(nu, S->r64.p, S->b32.p);
       int it = 0, conv = 0;
-      rc = run_minres<float>(c, S, S->ff.v32.p, S->dinv32.p, S->b32.p, S->x32.p, dptr.p, dptr.p + 3, dptr.p + 6,
+      rc = run_minres<float>(c, S, S->A.v32.p, S->dinv32.p, S->b32.p, S->x32.p, dptr.p, dptr.p + 3, dptr.p + 6,
                              S->q32.p, inner_tol, maxit - total, &S->g_minres32, &it, &conv);
       if (rc != ELFEL_OK) break;
       total += it;
       ++outer;
       add_scaled_k<<<vg, kBlk, 0, c->stream>>>(nu, S->x64.p, S->x32.p);
-      ELFEL_TRY(launch_resid(c, S, S->x64.p, nullptr, S->b64.p, S->r64.p, red_area(S, 2), S_RR));
+      ELFEL_TRY(launch_sell_resid(c, S, S->x64.p, S->b64.p, S->r64.p, red_area(S, 2), S_RR));
       ELFEL_CUDA(c, cudaMemcpyAsync(&rr, S->scal.p + S_RR, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
       ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+      if (c->trace)
+        fprintf(stderr, "[elfel minres32] outer %d inner %d rel %.3e\n", outer, it, sqrt(rr / bn2));
       if (rr <= rtol * rtol * bn2 || total >= maxit || outer >= 100) break;
     }
     dptr.release(c);
@@ -998,18 +1282,20 @@ extern "C" int elfel_solve(elfel_sysmat* m, const double* Fh, double* T, int64_t
     st.refinements = outer;
   }
   if (rc != ELFEL_OK) return rc;
-  // final FP64 true residual
-  ELFEL_TRY(launch_resid(c, S, S->x64.p, nullptr, S->b64.p, S->r64.p, red_area(S, 2), S_RR));
+  // solution back to the original order; final FP64 residual there
+  permute_out_k<<<vec_grid(nu), kBlk, 0, c->stream>>>(nu, S->A.perm.p, S->x64.p, S->xo64.p);
+  ELFEL_LAUNCH_CHECK(c);
+  ELFEL_TRY(launch_resid(c, S, S->xo64.p, nullptr, S->bo64.p, S->ro64.p, red_area(S, 2), S_RR));
   double rr = 0.0;
   ELFEL_CUDA(c, cudaMemcpyAsync(&rr, S->scal.p + S_RR, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-  ELFEL_CUDA(c, cudaMemcpyAsync(T, S->x64.p, sizeof(double) * nu, cudaMemcpyDeviceToHost, c->stream));
+  ELFEL_CUDA(c, cudaMemcpyAsync(T, S->xo64.p, sizeof(double) * nu, cudaMemcpyDeviceToHost, c->stream));
   ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
   st.relres = bn2 > 0.0 ? sqrt(rr / bn2) : 0.0;
   st.converged = st.relres <= rtol ? 1 : 0;
   st.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   if (stats) *stats = st;
   if (!st.converged)
-    return fail(c, ELFEL_ERR_NOT_CONVERGED, "solve: relative residual %.3e > %.3e after %d iterations", st.relres,
-                rtol, st.iterations);
+    return fail(c, ELFEL_ERR_NOT_CONVERGED, "solve: relative residual %.3e > %.3e after %d iterations (%d replacements)",
+                st.relres, rtol, st.iterations, st.refinements);
   return ELFEL_OK;
 }

@@ -90,6 +90,29 @@ def test_solve_with_host_rhs_and_nonzero_free_start(E, O, gpu):
     assert np.abs(T - T0).max() / np.abs(T0).max() < ERR_TOL
 
 
+@pytest.mark.parametrize("method", ["pcg64", "pcg32_ir"])
+def test_generic_matrix_wide_columns(E, O, gpu, method):
+    """A host CSC with randomly renumbered DOFs (column deltas beyond 16 bits -> 32-bit
+    column path), some data DOFs, solved through solve!(T, K, F, nu)."""
+    import scipy.sparse as sp
+
+    rng = np.random.default_rng(12)
+    m = 200
+    L1 = sp.diags([-np.ones(m - 1), 2.0 * np.ones(m), -np.ones(m - 1)], [-1, 0, 1])
+    A = (sp.kron(sp.eye(m), L1) + sp.kron(L1, sp.eye(m))).tocsr()  # 40,000 unknowns
+    p = rng.permutation(A.shape[0])
+    A = A[p][:, p].tocsc()
+    n = A.shape[0]
+    nu = n - 500
+    F = rng.standard_normal(n)
+    T = np.zeros(n)
+    T[nu:] = rng.standard_normal(n - nu)
+    T0 = O.solve_lifted(A, F, T.copy(), nu)
+    st = E.solve(T, A, F, nu, method=method, rtol=1e-11)
+    assert st["converged"]
+    assert np.abs(T - T0).max() / np.abs(T0).max() < ERR_TOL
+
+
 def test_not_converged_reports(E, gpu):
     mesh, fesp, am, _ = heat_system(E, "T6", 30)
     n, nu = E.ndofs(fesp), E.nunknowns(fesp)
