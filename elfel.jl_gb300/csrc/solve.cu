@@ -42,12 +42,18 @@ namespace elfel {
 constexpr int kBlk = 256;
 constexpr int kGraphIters = 16;
 constexpr int kMaxRedBlocks = 2048;  // partial-sum slots per reduction area
-constexpr int kGridCap = 152 * 8;    // 8 resident 256-thread blocks per SM
+constexpr int kVecOcc = 8;           // resident 256-thread blocks per SM, vector kernels
+constexpr int kSellOcc = 6;          // resident blocks per SM, SELL kernels (<= 40 registers)
+constexpr int kGridCap = 152 * kVecOcc;
+constexpr int kSellGridCap = 152 * kSellOcc;  // one full wave: no ragged second wave
 constexpr int kSigma = 256;          // row-sorting window
 
 // device scalar slots
 enum {
   S_PQ = 0, S_RZ, S_RR, S_BETA, S_BN2, S_TOL2, S_RMAX, S_DELTA,
+  S_ALPHA,  // rz / pq, computed once by the SpMV's last block
+  S_SCALE,  // FP32 refinement: the FP32 residual is (FP64 residual) / S_SCALE
+  S_BN2S,   // ||b||^2 / S_SCALE^2: the FP32 recurrence's convergence threshold
   // MINRES
   S_GAM, S_GAMP, S_GAMN, S_DEL, S_C, S_CP, S_S, S_SP, S_ETA, S_ETA0, S_A1, S_A2, S_A3, S_CN,
   S_COUNT
@@ -143,17 +149,19 @@ void solver_release(Ctx* c, elfel_sysmat* m) {
 
 // ------------------------------------------------------------------ reductions
 // Sum NV per-thread values over the grid; the last block gets the totals.
-template <int NV>
-__device__ __forceinline__ bool grid_sums(double (&v)[NV], Red4 red, double (&tot)[NV]) {
+// The warp stage adds in the working precision T (FP32 kernels keep the FP64
+// pipe free); warp, block and grid totals are then added in FP64.
+template <int NV, typename T>
+__device__ __forceinline__ bool grid_sums(T (&v)[NV], Red4 red, double (&tot)[NV]) {
   __shared__ double sh[NV][kBlk / 32];
   __shared__ bool last;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int a = 0; a < NV; ++a) {
-    double x = v[a];
+    T x = v[a];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-    if (lane == 0) sh[a][wid] = x;
+    if (lane == 0) sh[a][wid] = (double)x;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -206,7 +214,7 @@ __device__ __forceinline__ int sell_col(const SellView& A, int64_t k, int64_t ro
 // y = A x over all slices (one warp per slice, lane = row).  Returns the
 // thread's partial of y.w (w = x when wdot is null).
 template <typename T, bool D16>
-__device__ __forceinline__ double sell_rows(const SellView& A, const T* __restrict__ v, const T* __restrict__ x,
+__device__ __forceinline__ T sell_rows(const SellView& A, const T* __restrict__ v, const T* __restrict__ x,
                                             T* __restrict__ y, const T* __restrict__ wdot) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * kBlk + threadIdx.x) >> 5;
@@ -238,12 +246,12 @@ __device__ __forceinline__ double sell_rows(const SellView& A, const T* __restri
       part += acc * (wdot ? wdot[row] : x[row]);
     }
   }
-  return (double)part;
+  return part;
 }
 
 // CG: q = A p, scal[slot] = p.q.  Skips a finished or paused iteration.
 template <typename T, bool D16>
-__global__ void __launch_bounds__(kBlk) sell_cg_spmv_k(SellView A, const T* __restrict__ v, const T* __restrict__ x,
+__global__ void __launch_bounds__(kBlk, kSellOcc) sell_cg_spmv_k(SellView A, const T* __restrict__ v, const T* __restrict__ x,
                                                       T* __restrict__ y, Red4 red, double* scal, int slot,
                                                       int* flags) {
   if (flags[F_DONE] || flags[F_RU]) {
@@ -253,14 +261,18 @@ __global__ void __launch_bounds__(kBlk) sell_cg_spmv_k(SellView A, const T* __re
     if (flags[F_RU] == 1 && blockIdx.x == 0 && threadIdx.x == 0) ((volatile int*)flags)[F_RU] = 2;
     return;
   }
-  double p[1] = {sell_rows<T, D16>(A, v, x, y, nullptr)};
+  T p[1] = {sell_rows<T, D16>(A, v, x, y, nullptr)};
   double t[1];
-  if (grid_sums<1>(p, red, t)) scal[slot] = t[0];
+  if (grid_sums<1>(p, red, t)) {
+    const double pq = t[0];
+    scal[slot] = pq;
+    scal[S_ALPHA] = (pq > 0.0 && isfinite(pq)) ? scal[S_RZ] / pq : 0.0;
+  }
 }
 
 // r = b - A x in FP64 (permuted order), scal[slot] = r.r
 template <bool D16>
-__global__ void __launch_bounds__(kBlk) sell_resid_k(SellView A, const double* __restrict__ v,
+__global__ void __launch_bounds__(kBlk, kSellOcc) sell_resid_k(SellView A, const double* __restrict__ v,
                                                     const double* __restrict__ x, const double* __restrict__ b,
                                                     double* __restrict__ r, Red4 red, double* scal, int slot) {
   const int lane = threadIdx.x & 31;
@@ -337,7 +349,7 @@ __global__ void __launch_bounds__(kBlk) resid64_k(int64_t n, const int32_t* __re
       if (const int64_t i = i##0 + i##u * i##s; i < (n))
 
 template <typename T, bool ACC>
-__global__ void __launch_bounds__(kBlk) cg_update_k(int64_t n, T* __restrict__ x, T* __restrict__ r,
+__global__ void __launch_bounds__(kBlk, kVecOcc) cg_update_k(int64_t n, T* __restrict__ x, T* __restrict__ r,
                                                    const T* __restrict__ p, const T* __restrict__ q,
                                                    T* __restrict__ z, const T* __restrict__ dinv, Red4 red,
                                                    double* scal, int* flags) {
@@ -345,7 +357,7 @@ __global__ void __launch_bounds__(kBlk) cg_update_k(int64_t n, T* __restrict__ x
   // breakdown (p.Ap not positive or not finite): no update, report below
   const double pq = scal[S_PQ];
   const bool brk = !(pq > 0.0) || !isfinite(pq);
-  const T alpha = brk ? (T)0 : (T)(scal[S_RZ] / pq);
+  const T alpha = brk ? (T)0 : (T)scal[S_ALPHA];
   T prz = 0, prr = 0;
   FOR4(i, n) {
     const T pi = p[i];
@@ -357,7 +369,7 @@ __global__ void __launch_bounds__(kBlk) cg_update_k(int64_t n, T* __restrict__ x
     prz += ri * zi;
     prr += ri * ri;
   }
-  double v[2] = {(double)prz, (double)prr};
+  T v[2] = {prz, prr};
   double t[2];
   if (grid_sums<2>(v, red, t)) {
     const double rz = t[0], rr = t[1];
@@ -365,7 +377,7 @@ __global__ void __launch_bounds__(kBlk) cg_update_k(int64_t n, T* __restrict__ x
     scal[S_RZ] = rz;
     scal[S_RR] = rr;
     const int it = ++flags[F_ITER];
-    const bool conv = rr <= scal[S_TOL2] * scal[S_BN2];
+    const bool conv = rr <= scal[S_TOL2] * (ACC ? scal[S_BN2S] : scal[S_BN2]);
     const bool bad = brk || !isfinite(rz) || !isfinite(rr);
     if (!ACC) {
       if (conv || bad || it >= flags[F_MAXIT]) {
@@ -391,7 +403,7 @@ __global__ void __launch_bounds__(kBlk) cg_update_k(int64_t n, T* __restrict__ x
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kBlk) cg_p_k(int64_t n, T* __restrict__ p, const T* __restrict__ z,
+__global__ void __launch_bounds__(kBlk, kVecOcc) cg_p_k(int64_t n, T* __restrict__ p, const T* __restrict__ z,
                                               const double* scal, const int* flags) {
   // runs once more after a replacement request (F_RU = 1), so that p is the
   // recurrence's next direction when the residual gets replaced
@@ -402,7 +414,7 @@ __global__ void __launch_bounds__(kBlk) cg_p_k(int64_t n, T* __restrict__ p, con
 
 // z = dinv r, p = z (set_p), rz = r.z, and the initial scalars.
 template <typename T>
-__global__ void __launch_bounds__(kBlk) cg_start_k(int64_t n, const T* __restrict__ r, T* __restrict__ z,
+__global__ void __launch_bounds__(kBlk, kVecOcc) cg_start_k(int64_t n, const T* __restrict__ r, T* __restrict__ z,
                                                   T* __restrict__ p, const T* __restrict__ dinv, Red4 red,
                                                   double* scal, int* flags, int set_p) {
   T prz = 0;
@@ -412,7 +424,7 @@ __global__ void __launch_bounds__(kBlk) cg_start_k(int64_t n, const T* __restric
     if (set_p) p[i] = zi;
     prz += r[i] * zi;
   }
-  double v[1] = {(double)prz};
+  T v[1] = {prz};
   double t[1];
   if (grid_sums<1>(v, red, t)) {
     scal[S_RZ] = t[0];
@@ -420,20 +432,22 @@ __global__ void __launch_bounds__(kBlk) cg_start_k(int64_t n, const T* __restric
   }
 }
 
-// x64 += xacc, xacc = 0
-__global__ void fold_k(int64_t n, double* __restrict__ x, float* __restrict__ xa) {
+// x64 += s * xacc, xacc = 0  (the FP32 iterate solves for the correction / s)
+__global__ void fold_k(int64_t n, double* __restrict__ x, float* __restrict__ xa, double s) {
   FOR4(i, n) {
-    x[i] += (double)xa[i];
+    x[i] += s * (double)xa[i];
     xa[i] = 0.0f;
   }
 }
 
-__global__ void demote_k(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
-  FOR4(i, n) b[i] = (float)a[i];
+// b = a * inv_s in FP32: residuals are demoted at unit norm, so FP32 dot
+// products neither underflow nor overflow whatever the scale of the problem
+__global__ void demote_k(int64_t n, const double* __restrict__ a, float* __restrict__ b, double inv_s) {
+  FOR4(i, n) b[i] = (float)(a[i] * inv_s);
 }
 
-__global__ void add_scaled_k(int64_t n, double* __restrict__ x, const float* __restrict__ d) {
-  FOR4(i, n) x[i] += (double)d[i];
+__global__ void add_scaled_k(int64_t n, double* __restrict__ x, const float* __restrict__ d, double s) {
+  FOR4(i, n) x[i] += s * (double)d[i];
 }
 
 // out[i] = in[perm[i]]  /  out[perm[i]] = in[i]
@@ -456,18 +470,18 @@ __global__ void permute_out_k(int64_t n, const int32_t* __restrict__ perm, const
 //   step 3 (upd):  w_{j+1} = (z_j - a3 w_{j-1} - a2 w_j)/a1;  x += c_{j+1} eta w_{j+1}
 // where z_j is the normalised z (z/gam), kept in zb[rot].
 template <typename T, bool D16>
-__global__ void __launch_bounds__(kBlk) mr_spmv_k(SellView A, const T* __restrict__ v, T* const* zb,
+__global__ void __launch_bounds__(kBlk, kSellOcc) mr_spmv_k(SellView A, const T* __restrict__ v, T* const* zb,
                                                  T* __restrict__ q, Red4 red, double* scal, const int* flags) {
   if (flags[F_DONE]) return;
   const int rot = flags[F_ROT];
   const T* z = zb[rot % 3];
-  double p[1] = {sell_rows<T, D16>(A, v, z, q, nullptr)};
+  T p[1] = {sell_rows<T, D16>(A, v, z, q, nullptr)};
   double t[1];
   if (grid_sums<1>(p, red, t)) scal[S_DEL] = t[0];
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kBlk) mr_vec_k(int64_t n, const T* __restrict__ q, T* const* vb, T* const* zb,
+__global__ void __launch_bounds__(kBlk, kVecOcc) mr_vec_k(int64_t n, const T* __restrict__ q, T* const* vb, T* const* zb,
                                                 const T* __restrict__ minv, Red4 red, double* scal, int* flags) {
   if (flags[F_DONE]) return;
   const int rot = flags[F_ROT];
@@ -485,7 +499,7 @@ __global__ void __launch_bounds__(kBlk) mr_vec_k(int64_t n, const T* __restrict_
     zn[i] = zz;
     pz += zz * vv;
   }
-  double v[1] = {(double)pz};
+  T v[1] = {pz};
   double t[1];
   if (grid_sums<1>(v, red, t)) {
     const double gamn = sqrt(fmax(t[0], 0.0));
@@ -510,7 +524,7 @@ __global__ void __launch_bounds__(kBlk) mr_vec_k(int64_t n, const T* __restrict_
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kBlk) mr_upd_k(int64_t n, T* const* zb, T* const* wb, T* __restrict__ x,
+__global__ void __launch_bounds__(kBlk, kVecOcc) mr_upd_k(int64_t n, T* const* zb, T* const* wb, T* __restrict__ x,
                                                 double* scal, int* flags) {
   if (flags[F_DONE]) return;
   const int rot = flags[F_ROT];
@@ -549,7 +563,7 @@ __global__ void mr_tail_k(double* scal, int* flags) {
 
 // MINRES start: v1 = r (in vb[0]), z1 = minv r, gam = sqrt(z.v).
 template <typename T>
-__global__ void __launch_bounds__(kBlk) mr_start_k(int64_t n, const T* __restrict__ r, T* const* vb, T* const* zb,
+__global__ void __launch_bounds__(kBlk, kVecOcc) mr_start_k(int64_t n, const T* __restrict__ r, T* const* vb, T* const* zb,
                                                   T* const* wb, const T* __restrict__ minv, T* __restrict__ x,
                                                   Red4 red, double* scal, int* flags) {
   T pz = 0;
@@ -566,7 +580,7 @@ __global__ void __launch_bounds__(kBlk) mr_start_k(int64_t n, const T* __restric
     pz += zi * ri;
     x[i] = 0;
   }
-  double v[1] = {(double)pz};
+  T v[1] = {pz};
   double t[1];
   if (grid_sums<1>(v, red, t)) {
     const double g = sqrt(fmax(t[0], 0.0));
@@ -782,7 +796,7 @@ static int pick_group(int64_t nnz, int64_t n) {
 }
 
 static unsigned vec_grid(int64_t n) { return grid_for(n, kBlk * 4, kGridCap); }
-static unsigned sell_grid(const SolverData* S) { return grid_for(S->A.nslices, kBlk / 32, kGridCap); }
+static unsigned sell_grid(const SolverData* S) { return grid_for(S->A.nslices, kBlk / 32, kSellGridCap); }
 
 static Red4 red_area(SolverData* S, int k) {
   Red4 r;
@@ -1071,7 +1085,15 @@ static int run_pcg32(elfel_sysmat* m, int maxit, elfel_solve_stats* st) {
   ELFEL_CUDA(c, cudaMemsetAsync(S->x64.p, 0, sizeof(double) * nu, c->stream));
   ELFEL_CUDA(c, cudaMemsetAsync(S->xa32.p, 0, sizeof(float) * nu, c->stream));
   ELFEL_CUDA(c, cudaMemcpyAsync(S->r64.p, S->b64.p, sizeof(double) * nu, cudaMemcpyDeviceToDevice, c->stream));
-  demote_k<<<vg, kBlk, 0, c->stream>>>(nu, S->r64.p, S->r32.p);
+  // the FP32 recurrence works on r / s with s = ||r|| (unit-norm residual)
+  double hsc0[S_COUNT];
+  ELFEL_CUDA(c, cudaMemcpyAsync(hsc0, S->scal.p, sizeof(hsc0), cudaMemcpyDeviceToHost, c->stream));
+  ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+  double s = sqrt(hsc0[S_BN2]);
+  demote_k<<<vg, kBlk, 0, c->stream>>>(nu, S->r64.p, S->r32.p, 1.0 / s);
+  ELFEL_TRY(set_scal(c, S, S_SCALE, s));
+  ELFEL_TRY(set_scal(c, S, S_BN2S, 1.0));
+  ELFEL_TRY(set_scal(c, S, S_RMAX, 1.0));
   int hf[F_COUNT] = {0, 0, 0, maxit, 0, 0, 0};
   ELFEL_CUDA(c, cudaMemcpyAsync(S->flags.p, hf, sizeof(hf), cudaMemcpyHostToDevice, c->stream));
   cg_start_k<float><<<vg, kBlk, 0, c->stream>>>(nu, S->r32.p, S->z32.p, S->p32.p, S->dinv32.p, red_area(S, 0),
@@ -1100,9 +1122,9 @@ static int run_pcg32(elfel_sysmat* m, int maxit, elfel_solve_stats* st) {
     // recurrence residual before the replacement
     ELFEL_CUDA(c, cudaMemcpyAsync(hsc, S->scal.p, sizeof(hsc), cudaMemcpyDeviceToHost, c->stream));
     ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
-    const double rr_rec = hsc[S_RR];
+    const double rr_rec = hsc[S_RR] * s * s;  // recurrence residual, unscaled
     // FP64 residual replacement
-    fold_k<<<vg, kBlk, 0, c->stream>>>(nu, S->x64.p, S->xa32.p);
+    fold_k<<<vg, kBlk, 0, c->stream>>>(nu, S->x64.p, S->xa32.p, s);
     ELFEL_TRY(launch_sell_resid(c, S, S->x64.p, S->b64.p, S->r64.p, red_area(S, 2), S_RR));
     ELFEL_CUDA(c, cudaMemcpyAsync(hsc, S->scal.p, sizeof(hsc), cudaMemcpyDeviceToHost, c->stream));
     ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -1110,11 +1132,15 @@ static int run_pcg32(elfel_sysmat* m, int maxit, elfel_solve_stats* st) {
     const bool conv = hsc[S_RR] <= hsc[S_TOL2] * hsc[S_BN2];
     // keep the search direction unless the FP32 recurrence broke down or its
     // residual drifted far below the true one (then restart from p = z)
-    const int restart = hf[F_BRK] || !(rr_rec > 0.0) || !(rr_rec >= 1e-6 * hsc[S_RR]);
+    const int restart = hf[F_BRK] || !(rr_rec > 0.0) || !(rr_rec >= 1e-6 * hsc[S_RR]) || !(hsc[S_RR] > 0.0);
     if (c->trace)
       fprintf(stderr, "[elfel pcg32] it %d replace %d: recurrence %.3e true %.3e (rel %.3e) brk %d restart %d\n",
               hf[F_ITER], refinements, sqrt(rr_rec), sqrt(hsc[S_RR]), sqrt(hsc[S_RR] / hsc[S_BN2]), hf[F_BRK],
               restart);
+    if (!(hsc[S_RR] > 0.0)) {  // exact solution
+      hf[F_CONV] = 1;
+      break;
+    }
     if (conv || hf[F_ITER] >= maxit) {
       hf[F_CONV] = conv ? 1 : 0;
       break;
@@ -1123,11 +1149,14 @@ static int run_pcg32(elfel_sysmat* m, int maxit, elfel_solve_stats* st) {
       int z = 0;
       ELFEL_CUDA(c, cudaMemcpyAsync(S->flags.p + F_BRK, &z, sizeof(int), cudaMemcpyHostToDevice, c->stream));
     }
-    demote_k<<<vg, kBlk, 0, c->stream>>>(nu, S->r64.p, S->r32.p);
+    s = sqrt(hsc[S_RR]);
+    demote_k<<<vg, kBlk, 0, c->stream>>>(nu, S->r64.p, S->r32.p, 1.0 / s);
     cg_start_k<float><<<vg, kBlk, 0, c->stream>>>(nu, S->r32.p, S->z32.p, S->p32.p, S->dinv32.p, red_area(S, 0),
                                                   S->scal.p, S->flags.p, restart);
     ELFEL_LAUNCH_CHECK(c);
-    ELFEL_TRY(set_scal(c, S, S_RMAX, sqrt(hsc[S_RR])));
+    ELFEL_TRY(set_scal(c, S, S_SCALE, s));
+    ELFEL_TRY(set_scal(c, S, S_BN2S, hsc[S_BN2] / hsc[S_RR]));
+    ELFEL_TRY(set_scal(c, S, S_RMAX, 1.0));
   }
   st->iterations = hf[F_ITER];
   st->refinements = refinements;
@@ -1262,14 +1291,16 @@ extern "C" int elfel_solve(elfel_sysmat* m, const double* Fh, double* T, int64_t
     int total = 0, outer = 0;
     const double inner_tol = 1e-5;
     while (true) {
-      demote_k<<<vg, kBlk, 0, c->stream>>>(nu, S->r64.p, S->b32.p);
+      const double s = sqrt(rr);  // inner solve on the unit-norm residual
+      if (!(s > 0.0)) break;
+      demote_k<<<vg, kBlk, 0, c->stream>>>(nu, S->r64.p, S->b32.p, 1.0 / s);
       int it = 0, conv = 0;
       rc = run_minres<float>(c, S, S->A.v32.p, S->dinv32.p, S->b32.p, S->x32.p, dptr.p, dptr.p + 3, dptr.p + 6,
                              S->q32.p, inner_tol, maxit - total, &S->g_minres32, &it, &conv);
       if (rc != ELFEL_OK) break;
       total += it;
       ++outer;
-      add_scaled_k<<<vg, kBlk, 0, c->stream>>>(nu, S->x64.p, S->x32.p);
+      add_scaled_k<<<vg, kBlk, 0, c->stream>>>(nu, S->x64.p, S->x32.p, s);
       ELFEL_TRY(launch_sell_resid(c, S, S->x64.p, S->b64.p, S->r64.p, red_area(S, 2), S_RR));
       ELFEL_CUDA(c, cudaMemcpyAsync(&rr, S->scal.p + S_RR, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
       ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));

@@ -32,12 +32,14 @@ def heat_system(E, etype, N, orientation="a", jit=0.0, kappa=None, npts=3):
 def test_heat_t3_golden_on_device(E, gpu, golden):
     """test/test_heat.jl:89-111 end to end on the device: golden T vector, exact nodal values."""
     g = golden("heat_t3.json")
-    mesh = E.T3block(g["A"], g["A"], g["N"], g["N"])
-    fesp = heat_space(E, mesh, E.FEH1_T3())
-    n, nu = E.ndofs(fesp), E.nunknowns(fesp)
-    am = E.start(E.SysmatAssemblerGPU(), n, n)
-    E.assemble_heat(am, E.FEIterator(fesp), E.QPIterator(fesp, {"kind": "default"}), g["kappa"], g["Q"])
     for method in ("pcg64", "pcg32_ir"):
+        # a fresh space per run: scattersysvec! leaves the solution in the free
+        # DOF values, and solve! would then solve for a correction
+        mesh = E.T3block(g["A"], g["A"], g["N"], g["N"])
+        fesp = heat_space(E, mesh, E.FEH1_T3())
+        n, nu = E.ndofs(fesp), E.nunknowns(fesp)
+        am = E.start(E.SysmatAssemblerGPU(), n, n)
+        E.assemble_heat(am, E.FEIterator(fesp), E.QPIterator(fesp, {"kind": "default"}), g["kappa"], g["Q"])
         T = np.zeros(n)
         E.gathersysvec(T, fesp)
         st = E.solve(T, am, None, nu, method=method, rtol=1e-12)
@@ -111,6 +113,21 @@ def test_generic_matrix_wide_columns(E, O, gpu, method):
     st = E.solve(T, A, F, nu, method=method, rtol=1e-11)
     assert st["converged"]
     assert np.abs(T - T0).max() / np.abs(T0).max() < ERR_TOL
+
+
+def test_correction_solve_tiny_rhs(E, gpu):
+    """solve! from an already converged T: the lifted rhs is roundoff (~1e-15);
+    the FP32 refinement must still reach the relative tolerance (no FP32 underflow)."""
+    mesh, fesp, am, _ = heat_system(E, "T3", 8, kappa=1.0)
+    n, nu = E.ndofs(fesp), E.nunknowns(fesp)
+    T = np.zeros(n)
+    E.gathersysvec(T, fesp)
+    E.solve(T, am, None, nu, method="pcg64", rtol=1e-13)
+    for method in ("pcg64", "pcg32_ir"):
+        T2 = T.copy()
+        st = E.solve(T2, am, None, nu, method=method, rtol=1e-6)
+        assert st["converged"]
+        assert np.abs(T2[:nu]).max() < 1e-12  # the correction of a converged solution
 
 
 def test_not_converged_reports(E, gpu):
