@@ -384,9 +384,9 @@ __global__ void __launch_bounds__(kBlk, kVecOcc) cg_update_k(int64_t n, T* __res
         flags[F_DONE] = 1;
         flags[F_CONV] = (conv && !bad) ? 1 : 0;
       }
-    } else if (bad) {
-      // FP32 recurrence broke down (e.g. its residual reached exactly zero):
-      // replace the residual and restart the direction from it
+    } else if (bad || rr > 1e6 * scal[S_RMAX] * scal[S_RMAX]) {
+      // FP32 recurrence broke down (its residual reached exactly zero, or
+      // grew a thousandfold): replace the residual and restart from it
       flags[F_BRK] = 1;
       flags[F_RU] = 1;
     } else {
@@ -412,16 +412,19 @@ __global__ void __launch_bounds__(kBlk, kVecOcc) cg_p_k(int64_t n, T* __restrict
   FOR4(i, n) p[i] = z[i] + beta * p[i];
 }
 
-// z = dinv r, p = z (set_p), rz = r.z, and the initial scalars.
+// z = dinv r, rz = r.z, and the initial scalars.  set_p: p = z (restart);
+// otherwise the kept direction is carried into the new residual units:
+// p *= pscale (the FP32 refinement rescales r at every replacement).
 template <typename T>
 __global__ void __launch_bounds__(kBlk, kVecOcc) cg_start_k(int64_t n, const T* __restrict__ r, T* __restrict__ z,
                                                   T* __restrict__ p, const T* __restrict__ dinv, Red4 red,
-                                                  double* scal, int* flags, int set_p) {
+                                                  double* scal, int* flags, int set_p, T pscale) {
   T prz = 0;
   FOR4(i, n) {
     const T zi = dinv[i] * r[i];
     z[i] = zi;
     if (set_p) p[i] = zi;
+    else if (pscale != (T)1) p[i] *= pscale;
     prz += r[i] * zi;
   }
   T v[1] = {prz};
@@ -1059,7 +1062,7 @@ static int run_pcg64(elfel_sysmat* m, int maxit, elfel_solve_stats* st) {
   int hf[F_COUNT] = {0, 0, 0, maxit, 0, 0, 0};
   ELFEL_CUDA(c, cudaMemcpyAsync(S->flags.p, hf, sizeof(hf), cudaMemcpyHostToDevice, c->stream));
   cg_start_k<double><<<vg, kBlk, 0, c->stream>>>(nu, S->r64.p, S->z64.p, S->p64.p, S->dinv64.p, red_area(S, 0),
-                                                 S->scal.p, S->flags.p, 1);
+                                                 S->scal.p, S->flags.p, 1, 1.0);
   ELFEL_LAUNCH_CHECK(c);
   ELFEL_TRY(capture(c, &S->g_pcg64, [&]() {
     launch_cg_spmv<double>(c, S, S->A.v64.p, S->p64.p, S->q64.p, red_area(S, 0), S_PQ);
@@ -1097,7 +1100,7 @@ static int run_pcg32(elfel_sysmat* m, int maxit, elfel_solve_stats* st) {
   int hf[F_COUNT] = {0, 0, 0, maxit, 0, 0, 0};
   ELFEL_CUDA(c, cudaMemcpyAsync(S->flags.p, hf, sizeof(hf), cudaMemcpyHostToDevice, c->stream));
   cg_start_k<float><<<vg, kBlk, 0, c->stream>>>(nu, S->r32.p, S->z32.p, S->p32.p, S->dinv32.p, red_area(S, 0),
-                                                S->scal.p, S->flags.p, 1);
+                                                S->scal.p, S->flags.p, 1, 1.0f);
   ELFEL_LAUNCH_CHECK(c);
   ELFEL_TRY(capture(c, &S->g_pcg32, [&]() {
     launch_cg_spmv<float>(c, S, S->A.v32.p, S->p32.p, S->q32.p, red_area(S, 0), S_PQ);
@@ -1149,10 +1152,11 @@ static int run_pcg32(elfel_sysmat* m, int maxit, elfel_solve_stats* st) {
       int z = 0;
       ELFEL_CUDA(c, cudaMemcpyAsync(S->flags.p + F_BRK, &z, sizeof(int), cudaMemcpyHostToDevice, c->stream));
     }
+    const double s_old = s;
     s = sqrt(hsc[S_RR]);
     demote_k<<<vg, kBlk, 0, c->stream>>>(nu, S->r64.p, S->r32.p, 1.0 / s);
     cg_start_k<float><<<vg, kBlk, 0, c->stream>>>(nu, S->r32.p, S->z32.p, S->p32.p, S->dinv32.p, red_area(S, 0),
-                                                  S->scal.p, S->flags.p, restart);
+                                                  S->scal.p, S->flags.p, restart, (float)(s_old / s));
     ELFEL_LAUNCH_CHECK(c);
     ELFEL_TRY(set_scal(c, S, S_SCALE, s));
     ELFEL_TRY(set_scal(c, S, S_BN2S, hsc[S_BN2] / hsc[S_RR]));
