@@ -97,6 +97,7 @@ SIGNATURES = {
     "elfel_sysmat_csc": (ctypes.c_int, [_vp, _i64p, _i64p, _dp]),
     "elfel_sysmat_rhs": (ctypes.c_int, [_vp, _dp]),
     "elfel_sysvec_assemble": (ctypes.c_int, [_vp, ctypes.c_int64, _i64p, _dp, ctypes.c_int64, _dp]),
+    "elfel_sysvec_assemble_noalloc": (ctypes.c_int, [_vp, ctypes.c_int64, _vp, _vp, ctypes.c_int64, _vp]),
     "elfel_fused_setup": (ctypes.c_int, [_vp, ctypes.POINTER(FusedDesc)]),
     "elfel_fused_set_geometry": (ctypes.c_int, [_vp, _dp]),
     "elfel_fused_heat": (ctypes.c_int, [_vp, _dp, ctypes.c_double]),

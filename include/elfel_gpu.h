@@ -104,6 +104,32 @@ ELFEL_API int elfel_sysmat_rhs(elfel_sysmat* m, double* F);
 ELFEL_API int elfel_sysvec_assemble(elfel_ctx* ctx, int64_t nrow, const int64_t* rows, const double* vals,
                           int64_t n, double* out);
 
+/* Allocation-free vector assembly.  No counterpart in the reference: it is
+ * elfel_sysvec_assemble for callers that cannot allocate device memory where
+ * they assemble -- programs that give the library only memory their own
+ * runtime manages, or loops that must not call cudaMalloc because it
+ * synchronises the device and takes unbounded time.  rows (1-based) and vals
+ * (n entries) are device pointers, out (nrow doubles) is a device pointer the
+ * caller owns; out[r] = sum of vals[s] over rows[s] == r+1 in increasing s, the
+ * same bits as elfel_sysvec_assemble.
+ * Scratch: one fixed device array inside the library (about 16 MB, kept by
+ * every GPU that loads the library until the process exits), so
+ *   - sizes are limited to ELFEL_NOALLOC_MAX_ROWS rows and
+ *     ELFEL_NOALLOC_MAX_ENTRIES entries; larger calls return ELFEL_ERR_ARG;
+ *   - the first call on a device looks up the array's device address (once,
+ *     with that device current); make that first call before any stream
+ *     capture;
+ *   - every call reuses the same array, which keeps the previous call's
+ *     contents; calls whose work overlaps on the GPU (other streams, other
+ *     contexts on the same device) race on it.
+ * Work runs on the context's stream; the call synchronises that stream to
+ * report out-of-range rows.  It calls no cudaMalloc, cudaFree or other
+ * allocating routine. */
+#define ELFEL_NOALLOC_MAX_ROWS 524288
+#define ELFEL_NOALLOC_MAX_ENTRIES 2097152
+ELFEL_API int elfel_sysvec_assemble_noalloc(elfel_ctx* ctx, int64_t nrow, const int64_t* rows, const double* vals,
+                                            int64_t n, double* out);
+
 /* ------------------------------------------------ fused (device) assembly */
 enum elfel_physics {
   ELFEL_HEAT = 1,       /* test/test_heat.jl:41-58, per-element conductivity */
