@@ -43,7 +43,7 @@ constexpr int kBlk = 256;
 constexpr int kGraphIters = 16;
 constexpr int kMaxRedBlocks = 2048;  // partial-sum slots per reduction area
 constexpr int kVecOcc = 8;           // resident 256-thread blocks per SM, vector kernels
-constexpr int kSellOcc = 6;          // resident blocks per SM, SELL kernels (<= 40 registers)
+constexpr int kSellOcc = 4;          // resident blocks per SM, SELL kernels (<= 64 registers)
 constexpr int kGridCap = 152 * kVecOcc;
 constexpr int kSellGridCap = 152 * kSellOcc;  // one full wave: no ragged second wave
 constexpr int kSigma = 256;          // row-sorting window
@@ -211,11 +211,26 @@ __device__ __forceinline__ int sell_col(const SellView& A, int64_t k, int64_t ro
   return __ldcs(A.c32 + k);
 }
 
+// The x term of one stored entry.  Plain form: x_c.  Difference form (DIFF):
+// the matrix is stored with its row sums s_i in the diagonal slots, and
+//   y_i = s_i x_i + sum_{j != i} a_ij (x_j - x_i),
+// an identity for any matrix; for slowly varying x the differences are exact
+// (Sterbenz), so in FP32 the near-zero row sums of stiffness matrices do not
+// cancel catastrophically and the smallest eigenvalues are kept.  Padding
+// entries have value 0 and column = row, so they add nothing either way.
+template <typename T, bool DIFF>
+__device__ __forceinline__ T xterm(const T xc, int c, int64_t row, T xi) {
+  if (!DIFF) return xc;
+  return (int64_t)c == row ? xi : xc - xi;
+}
+
 // y = A x over all slices (one warp per slice, lane = row).  Returns the
-// thread's partial of y.w (w = x when wdot is null).
-template <typename T, bool D16>
+// thread's partial of y.w (w = x when wdot is null); with rdot, also adds
+// rdot.x into *part2.
+template <typename T, bool D16, bool DIFF = false>
 __device__ __forceinline__ T sell_rows(const SellView& A, const T* __restrict__ v, const T* __restrict__ x,
-                                            T* __restrict__ y, const T* __restrict__ wdot) {
+                                            T* __restrict__ y, const T* __restrict__ wdot,
+                                            const T* __restrict__ rdot = nullptr, T* part2 = nullptr) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * kBlk + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * kBlk) >> 5;
@@ -224,36 +239,67 @@ __device__ __forceinline__ T sell_rows(const SellView& A, const T* __restrict__ 
     const int64_t base = A.sptr[s] + lane;
     const int64_t row = s * 32 + lane;
     const int w = row < A.nrows ? A.sw[s] : 0;  // lanes past the last row stay idle
+    const T xi = (DIFF && row < A.nrows) ? x[row] : (T)0;
+    // 8 entries per lane in flight: all column and value loads of a group
+    // are issued before the dependent gathers of x
     T a0 = 0, a1 = 0, a2 = 0, a3 = 0;
     int j = 0;
-    for (; j + 3 < w; j += 4) {
+    for (; j + 7 < w; j += 8) {
+      const int64_t k = base + (int64_t)j * 32;
+      int cc[8];
+      T vv[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) cc[u] = sell_col<D16>(A, k + 32 * u, row);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) vv[u] = __ldcs(v + k + 32 * u);
+      T xx[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) xx[u] = xterm<T, DIFF>(__ldg(x + cc[u]), cc[u], row, xi);
+      a0 += vv[0] * xx[0];
+      a1 += vv[1] * xx[1];
+      a2 += vv[2] * xx[2];
+      a3 += vv[3] * xx[3];
+      a0 += vv[4] * xx[4];
+      a1 += vv[5] * xx[5];
+      a2 += vv[6] * xx[6];
+      a3 += vv[7] * xx[7];
+    }
+    if (j + 3 < w) {
       const int64_t k = base + (int64_t)j * 32;
       const int c0 = sell_col<D16>(A, k, row), c1 = sell_col<D16>(A, k + 32, row);
       const int c2 = sell_col<D16>(A, k + 64, row), c3 = sell_col<D16>(A, k + 96, row);
       const T v0 = __ldcs(v + k), v1 = __ldcs(v + k + 32), v2 = __ldcs(v + k + 64), v3 = __ldcs(v + k + 96);
-      a0 += v0 * __ldg(x + c0);
-      a1 += v1 * __ldg(x + c1);
-      a2 += v2 * __ldg(x + c2);
-      a3 += v3 * __ldg(x + c3);
+      a0 += v0 * xterm<T, DIFF>(__ldg(x + c0), c0, row, xi);
+      a1 += v1 * xterm<T, DIFF>(__ldg(x + c1), c1, row, xi);
+      a2 += v2 * xterm<T, DIFF>(__ldg(x + c2), c2, row, xi);
+      a3 += v3 * xterm<T, DIFF>(__ldg(x + c3), c3, row, xi);
+      j += 4;
     }
     for (; j < w; ++j) {
       const int64_t k = base + (int64_t)j * 32;
-      a0 += __ldcs(v + k) * __ldg(x + sell_col<D16>(A, k, row));
+      const int cj = sell_col<D16>(A, k, row);
+      a0 += __ldcs(v + k) * xterm<T, DIFF>(__ldg(x + cj), cj, row, xi);
     }
     const T acc = (a0 + a1) + (a2 + a3);
     if (row < A.nrows) {
       y[row] = acc;
-      part += acc * (wdot ? wdot[row] : x[row]);
+      const T xr = x[row];
+      part += acc * (wdot ? wdot[row] : xr);
+      if (rdot) *part2 += rdot[row] * xr;
     }
   }
   return part;
 }
 
-// CG: q = A p, scal[slot] = p.q.  Skips a finished or paused iteration.
-template <typename T, bool D16>
+// CG: q = A p, scal[slot] = p.q, alpha.  Skips a finished or paused iteration.
+// Standard CG: alpha = r.z / p.Ap.  FLEX (flexible CG, used by the FP32
+// refinement): alpha = r.p / p.Ap, the step that minimises the energy error
+// along p even when r is not orthogonal to the previous direction -- as after
+// a residual replacement; equal to the standard step in exact arithmetic.
+template <typename T, bool D16, bool DIFF, bool FLEX>
 __global__ void __launch_bounds__(kBlk, kSellOcc) sell_cg_spmv_k(SellView A, const T* __restrict__ v, const T* __restrict__ x,
-                                                      T* __restrict__ y, Red4 red, double* scal, int slot,
-                                                      int* flags) {
+                                                      T* __restrict__ y, const T* __restrict__ r, Red4 red,
+                                                      double* scal, int slot, int* flags) {
   if (flags[F_DONE] || flags[F_RU]) {
     // F_RU = 1: requested by the previous update; p has been advanced once by
     // cg_p_k since.  Mark it 2 so the rest of the graph skips until the host
@@ -261,12 +307,16 @@ __global__ void __launch_bounds__(kBlk, kSellOcc) sell_cg_spmv_k(SellView A, con
     if (flags[F_RU] == 1 && blockIdx.x == 0 && threadIdx.x == 0) ((volatile int*)flags)[F_RU] = 2;
     return;
   }
-  T p[1] = {sell_rows<T, D16>(A, v, x, y, nullptr)};
-  double t[1];
-  if (grid_sums<1>(p, red, t)) {
+  T rp = 0;
+  T p[2];
+  p[0] = sell_rows<T, D16, DIFF>(A, v, x, y, nullptr, FLEX ? r : nullptr, &rp);
+  p[1] = rp;
+  double t[2];
+  if (grid_sums<2>(p, red, t)) {
     const double pq = t[0];
     scal[slot] = pq;
-    scal[S_ALPHA] = (pq > 0.0 && isfinite(pq)) ? scal[S_RZ] / pq : 0.0;
+    const double num = FLEX ? t[1] : scal[S_RZ];
+    scal[S_ALPHA] = (pq > 0.0 && isfinite(pq)) ? num / pq : 0.0;
   }
 }
 
@@ -358,22 +408,26 @@ __global__ void __launch_bounds__(kBlk, kVecOcc) cg_update_k(int64_t n, T* __res
   const double pq = scal[S_PQ];
   const bool brk = !(pq > 0.0) || !isfinite(pq);
   const T alpha = brk ? (T)0 : (T)scal[S_ALPHA];
-  T prz = 0, prr = 0;
+  T prz = 0, prr = 0, pzo = 0;
   FOR4(i, n) {
     const T pi = p[i];
     x[i] += alpha * pi;
-    const T ri = r[i] - alpha * q[i];
+    const T ro = r[i];
+    const T ri = ro - alpha * q[i];
     r[i] = ri;
     const T zi = dinv[i] * ri;
     z[i] = zi;
     prz += ri * zi;
     prr += ri * ri;
+    if (ACC) pzo += zi * ro;
   }
-  T v[2] = {prz, prr};
-  double t[2];
-  if (grid_sums<2>(v, red, t)) {
+  T v[3] = {prz, prr, pzo};
+  double t[3];
+  if (grid_sums<3>(v, red, t)) {
     const double rz = t[0], rr = t[1];
-    scal[S_BETA] = rz / scal[S_RZ];
+    // FP32 refinement: Polak-Ribiere beta (flexible CG, Notay 2000),
+    // z_new.(r_new - r_old) / (r_old.z_old); standard CG: r_new.z_new / r_old.z_old
+    scal[S_BETA] = (ACC ? rz - t[2] : rz) / scal[S_RZ];
     scal[S_RZ] = rz;
     scal[S_RR] = rr;
     const int it = ++flags[F_ITER];
@@ -384,9 +438,9 @@ __global__ void __launch_bounds__(kBlk, kVecOcc) cg_update_k(int64_t n, T* __res
         flags[F_DONE] = 1;
         flags[F_CONV] = (conv && !bad) ? 1 : 0;
       }
-    } else if (bad || rr > 1e6 * scal[S_RMAX] * scal[S_RMAX]) {
-      // FP32 recurrence broke down (its residual reached exactly zero, or
-      // grew a thousandfold): replace the residual and restart from it
+    } else if (bad) {
+      // FP32 recurrence broke down (e.g. its residual reached exactly zero):
+      // replace the residual and restart the direction from it
       flags[F_BRK] = 1;
       flags[F_RU] = 1;
     } else {
@@ -754,6 +808,29 @@ __global__ void sell_vals_k(int64_t npad, const int32_t* __restrict__ map, const
   }
 }
 
+// FP32 values in difference form: each row's diagonal slot gets the row sum
+// s_i = sum_j a_ij (added in FP64, rounded once); the other slots keep a_ij.
+template <bool D16>
+__global__ void sell_rowsum_k(SellView A, const int32_t* __restrict__ map, const double* __restrict__ v64,
+                              float* __restrict__ v32) {
+  for (int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; row < A.nrows;
+       row += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = row >> 5;
+    const int64_t base = A.sptr[s] + (row & 31);
+    const int w = A.sw[s];
+    double sum = 0.0;
+    int64_t dpos = -1;
+    for (int j = 0; j < w; ++j) {
+      const int64_t k = base + (int64_t)j * 32;
+      if (map[k] < 0) continue;  // padding
+      sum += v64[k];
+      const int c = D16 ? (int)row + (int)A.d16[k] : A.c32[k];
+      if ((int64_t)c == row) dpos = k;
+    }
+    if (dpos >= 0) v32[dpos] = (float)sum;
+  }
+}
+
 __global__ void gather_vals_k(int64_t n, const int32_t* map, const double* src, double* d64) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     d64[i] = src[map[i]];
@@ -950,7 +1027,8 @@ static int build_solver(elfel_sysmat* m, int64_t nu) {
 }
 
 // Values of the solver matrices from the CSC values (FP64, and the FP32 copy).
-static int refresh_values(elfel_sysmat* m, int abs_diag) {
+// diff32: the FP32 copy is stored in difference form (for the FP32 CG).
+static int refresh_values(elfel_sysmat* m, int abs_diag, int diff32) {
   Ctx* c = &m->h->c;
   SolverData* S = m->solver;
   const int64_t nu = S->nu;
@@ -964,6 +1042,15 @@ static int refresh_values(elfel_sysmat* m, int abs_diag) {
   if (S->A.nnz_pad)
     sell_vals_k<<<vec_grid(S->A.nnz_pad), kBlk, 0, c->stream>>>(S->A.nnz_pad, S->A.map.p, m->vals.p, S->A.v64.p,
                                                                  S->A.v32.p);
+  if (diff32 && nu > 0) {
+    const SellView V = S->view();
+    if (S->A.d16)
+      sell_rowsum_k<true><<<grid_for(nu, 256, (int64_t)c->sm_count * 16), 256, 0, c->stream>>>(
+          V, S->A.map.p, S->A.v64.p, S->A.v32.p);
+    else
+      sell_rowsum_k<false><<<grid_for(nu, 256, (int64_t)c->sm_count * 16), 256, 0, c->stream>>>(
+          V, S->A.map.p, S->A.v64.p, S->A.v32.p);
+  }
   const double* aux = (m->fused && m->F.physics == ELFEL_STOKES) ? m->F.pmass_diag.p : nullptr;
   if (nu > 0) {
     diag_k<<<grid_for(nu, 256, (int64_t)c->sm_count * 16), 256, 0, c->stream>>>(nu, S->ff.rowptr.p, S->ff.col.p,
@@ -1006,13 +1093,17 @@ static int launch_sell_resid(Ctx* c, SolverData* S, const double* x, const doubl
   return ELFEL_OK;
 }
 
-template <typename T>
-static void launch_cg_spmv(Ctx* c, SolverData* S, const T* v, const T* x, T* y, Red4 red, int slot) {
+// DIFF: the values are in difference form (row sums in the diagonal slots);
+// FLEX: flexible-CG step length (needs the residual r).
+template <typename T, bool DIFF, bool FLEX>
+static void launch_cg_spmv(Ctx* c, SolverData* S, const T* v, const T* x, T* y, const T* r, Red4 red, int slot) {
   const SellView V = S->view();
   if (S->A.d16)
-    sell_cg_spmv_k<T, true><<<sell_grid(S), kBlk, 0, c->stream>>>(V, v, x, y, red, S->scal.p, slot, S->flags.p);
+    sell_cg_spmv_k<T, true, DIFF, FLEX><<<sell_grid(S), kBlk, 0, c->stream>>>(V, v, x, y, r, red, S->scal.p, slot,
+                                                                              S->flags.p);
   else
-    sell_cg_spmv_k<T, false><<<sell_grid(S), kBlk, 0, c->stream>>>(V, v, x, y, red, S->scal.p, slot, S->flags.p);
+    sell_cg_spmv_k<T, false, DIFF, FLEX><<<sell_grid(S), kBlk, 0, c->stream>>>(V, v, x, y, r, red, S->scal.p,
+                                                                               slot, S->flags.p);
 }
 
 template <typename T>
@@ -1065,7 +1156,7 @@ static int run_pcg64(elfel_sysmat* m, int maxit, elfel_solve_stats* st) {
                                                  S->scal.p, S->flags.p, 1, 1.0);
   ELFEL_LAUNCH_CHECK(c);
   ELFEL_TRY(capture(c, &S->g_pcg64, [&]() {
-    launch_cg_spmv<double>(c, S, S->A.v64.p, S->p64.p, S->q64.p, red_area(S, 0), S_PQ);
+    launch_cg_spmv<double, false, false>(c, S, S->A.v64.p, S->p64.p, S->q64.p, nullptr, red_area(S, 0), S_PQ);
     cg_update_k<double, false><<<vg, kBlk, 0, c->stream>>>(nu, S->x64.p, S->r64.p, S->p64.p, S->q64.p, S->z64.p,
                                                             S->dinv64.p, red_area(S, 1), S->scal.p, S->flags.p);
     cg_p_k<double><<<vg, kBlk, 0, c->stream>>>(nu, S->p64.p, S->z64.p, S->scal.p, S->flags.p);
@@ -1088,11 +1179,12 @@ static int run_pcg32(elfel_sysmat* m, int maxit, elfel_solve_stats* st) {
   ELFEL_CUDA(c, cudaMemsetAsync(S->x64.p, 0, sizeof(double) * nu, c->stream));
   ELFEL_CUDA(c, cudaMemsetAsync(S->xa32.p, 0, sizeof(float) * nu, c->stream));
   ELFEL_CUDA(c, cudaMemcpyAsync(S->r64.p, S->b64.p, sizeof(double) * nu, cudaMemcpyDeviceToDevice, c->stream));
-  // the FP32 recurrence works on r / s with s = ||r|| (unit-norm residual)
+  // the FP32 recurrence works on r / s with s = ||b||: the initial residual
+  // has unit norm whatever the scale of the problem (no FP32 under/overflow)
   double hsc0[S_COUNT];
   ELFEL_CUDA(c, cudaMemcpyAsync(hsc0, S->scal.p, sizeof(hsc0), cudaMemcpyDeviceToHost, c->stream));
   ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
-  double s = sqrt(hsc0[S_BN2]);
+  const double s = sqrt(hsc0[S_BN2]);
   demote_k<<<vg, kBlk, 0, c->stream>>>(nu, S->r64.p, S->r32.p, 1.0 / s);
   ELFEL_TRY(set_scal(c, S, S_SCALE, s));
   ELFEL_TRY(set_scal(c, S, S_BN2S, 1.0));
@@ -1103,7 +1195,7 @@ static int run_pcg32(elfel_sysmat* m, int maxit, elfel_solve_stats* st) {
                                                 S->scal.p, S->flags.p, 1, 1.0f);
   ELFEL_LAUNCH_CHECK(c);
   ELFEL_TRY(capture(c, &S->g_pcg32, [&]() {
-    launch_cg_spmv<float>(c, S, S->A.v32.p, S->p32.p, S->q32.p, red_area(S, 0), S_PQ);
+    launch_cg_spmv<float, true, true>(c, S, S->A.v32.p, S->p32.p, S->q32.p, S->r32.p, red_area(S, 0), S_PQ);
     cg_update_k<float, true><<<vg, kBlk, 0, c->stream>>>(nu, S->xa32.p, S->r32.p, S->p32.p, S->q32.p, S->z32.p,
                                                          S->dinv32.p, red_area(S, 1), S->scal.p, S->flags.p);
     cg_p_k<float><<<vg, kBlk, 0, c->stream>>>(nu, S->p32.p, S->z32.p, S->scal.p, S->flags.p);
@@ -1152,15 +1244,13 @@ static int run_pcg32(elfel_sysmat* m, int maxit, elfel_solve_stats* st) {
       int z = 0;
       ELFEL_CUDA(c, cudaMemcpyAsync(S->flags.p + F_BRK, &z, sizeof(int), cudaMemcpyHostToDevice, c->stream));
     }
-    const double s_old = s;
-    s = sqrt(hsc[S_RR]);
+    // the units stay those of the start (s = ||b||) for the whole solve, so
+    // the kept direction p needs no conversion
     demote_k<<<vg, kBlk, 0, c->stream>>>(nu, S->r64.p, S->r32.p, 1.0 / s);
     cg_start_k<float><<<vg, kBlk, 0, c->stream>>>(nu, S->r32.p, S->z32.p, S->p32.p, S->dinv32.p, red_area(S, 0),
-                                                  S->scal.p, S->flags.p, restart, (float)(s_old / s));
+                                                  S->scal.p, S->flags.p, restart, 1.0f);
     ELFEL_LAUNCH_CHECK(c);
-    ELFEL_TRY(set_scal(c, S, S_SCALE, s));
-    ELFEL_TRY(set_scal(c, S, S_BN2S, hsc[S_BN2] / hsc[S_RR]));
-    ELFEL_TRY(set_scal(c, S, S_RMAX, 1.0));
+    ELFEL_TRY(set_scal(c, S, S_RMAX, sqrt(hsc[S_RR]) / s));
   }
   st->iterations = hf[F_ITER];
   st->refinements = refinements;
@@ -1216,7 +1306,7 @@ extern "C" int elfel_solve(elfel_sysmat* m, const double* Fh, double* T, int64_t
   ELFEL_TRY(build_solver(m, nu));
   SolverData* S = m->solver;
   const bool minres = method == ELFEL_MINRES64 || method == ELFEL_MINRES32_IR;
-  ELFEL_TRY(refresh_values(m, minres ? 1 : 0));
+  ELFEL_TRY(refresh_values(m, minres ? 1 : 0, method == ELFEL_PCG32_IR ? 1 : 0));
   const int64_t n = m->nrow;
   if (nu == 0) {
     if (stats) *stats = st;
@@ -1240,7 +1330,13 @@ extern "C" int elfel_solve(elfel_sysmat* m, const double* Fh, double* T, int64_t
   ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
   ELFEL_TRY(set_scal(c, S, S_TOL2, rtol * rtol));
   ELFEL_TRY(set_scal(c, S, S_RMAX, sqrt(bn2)));
-  ELFEL_TRY(set_scal(c, S, S_DELTA, 0.1));
+  // residual-replacement threshold of the FP32 refinement (tuning knob)
+  double delta = 0.1;
+  if (const char* e = getenv("ELFEL_RU_DELTA")) {
+    const double d = atof(e);
+    if (d > 0.0 && d < 1.0) delta = d;
+  }
+  ELFEL_TRY(set_scal(c, S, S_DELTA, delta));
   int rc = ELFEL_OK;
   if (bn2 == 0.0) {
     ELFEL_CUDA(c, cudaMemsetAsync(S->x64.p, 0, sizeof(double) * nu, c->stream));
