@@ -42,10 +42,13 @@ namespace elfel {
 constexpr int kBlk = 256;
 constexpr int kGraphIters = 16;
 constexpr int kMaxRedBlocks = 2048;  // partial-sum slots per reduction area
-constexpr int kVecOcc = 8;           // resident 256-thread blocks per SM, vector kernels
-constexpr int kSellOcc = 4;          // resident blocks per SM, SELL kernels (<= 64 registers)
+constexpr int kVecOcc = 8;           // register budget of vector kernels: 8 blocks/SM (32 registers)
 constexpr int kGridCap = 152 * kVecOcc;
-constexpr int kSellGridCap = 152 * kSellOcc;  // one full wave: no ragged second wave
+constexpr int kVecGridCap = 152 * kVecOcc;  // vector kernels: one full wave (4 blocks/SM measured slower)
+constexpr int kSellOcc = 4;           // FP64 SELL kernels: <= 64 registers, 4 blocks/SM
+// FP32 SELL kernels fit their 8-deep unroll in 40 registers: 6 blocks/SM.
+template <typename T>
+constexpr int sell_occ() { return sizeof(T) == 4 ? 6 : kSellOcc; }
 constexpr int kSigma = 256;          // row-sorting window
 
 // device scalar slots
@@ -297,7 +300,7 @@ __device__ __forceinline__ T sell_rows(const SellView& A, const T* __restrict__ 
 // along p even when r is not orthogonal to the previous direction -- as after
 // a residual replacement; equal to the standard step in exact arithmetic.
 template <typename T, bool D16, bool DIFF, bool FLEX>
-__global__ void __launch_bounds__(kBlk, kSellOcc) sell_cg_spmv_k(SellView A, const T* __restrict__ v, const T* __restrict__ x,
+__global__ void __launch_bounds__(kBlk, sell_occ<T>()) sell_cg_spmv_k(SellView A, const T* __restrict__ v, const T* __restrict__ x,
                                                       T* __restrict__ y, const T* __restrict__ r, Red4 red,
                                                       double* scal, int slot, int* flags) {
   if (flags[F_DONE] || flags[F_RU]) {
@@ -527,7 +530,7 @@ __global__ void permute_out_k(int64_t n, const int32_t* __restrict__ perm, const
 //   step 3 (upd):  w_{j+1} = (z_j - a3 w_{j-1} - a2 w_j)/a1;  x += c_{j+1} eta w_{j+1}
 // where z_j is the normalised z (z/gam), kept in zb[rot].
 template <typename T, bool D16>
-__global__ void __launch_bounds__(kBlk, kSellOcc) mr_spmv_k(SellView A, const T* __restrict__ v, T* const* zb,
+__global__ void __launch_bounds__(kBlk, sell_occ<T>()) mr_spmv_k(SellView A, const T* __restrict__ v, T* const* zb,
                                                  T* __restrict__ q, Red4 red, double* scal, const int* flags) {
   if (flags[F_DONE]) return;
   const int rot = flags[F_ROT];
@@ -875,8 +878,12 @@ static int pick_group(int64_t nnz, int64_t n) {
   return 32;
 }
 
-static unsigned vec_grid(int64_t n) { return grid_for(n, kBlk * 4, kGridCap); }
-static unsigned sell_grid(const SolverData* S) { return grid_for(S->A.nslices, kBlk / 32, kSellGridCap); }
+static unsigned vec_grid(int64_t n) { return grid_for(n, kBlk * 4, kVecGridCap); }
+// one full wave of the kernel's resident blocks: no ragged second wave
+template <typename T = double>
+static unsigned sell_grid(const SolverData* S) {
+  return grid_for(S->A.nslices, kBlk / 32, (int64_t)152 * sell_occ<T>());
+}
 
 static Red4 red_area(SolverData* S, int k) {
   Red4 r;
@@ -1099,10 +1106,10 @@ template <typename T, bool DIFF, bool FLEX>
 static void launch_cg_spmv(Ctx* c, SolverData* S, const T* v, const T* x, T* y, const T* r, Red4 red, int slot) {
   const SellView V = S->view();
   if (S->A.d16)
-    sell_cg_spmv_k<T, true, DIFF, FLEX><<<sell_grid(S), kBlk, 0, c->stream>>>(V, v, x, y, r, red, S->scal.p, slot,
+    sell_cg_spmv_k<T, true, DIFF, FLEX><<<sell_grid<T>(S), kBlk, 0, c->stream>>>(V, v, x, y, r, red, S->scal.p, slot,
                                                                               S->flags.p);
   else
-    sell_cg_spmv_k<T, false, DIFF, FLEX><<<sell_grid(S), kBlk, 0, c->stream>>>(V, v, x, y, r, red, S->scal.p,
+    sell_cg_spmv_k<T, false, DIFF, FLEX><<<sell_grid<T>(S), kBlk, 0, c->stream>>>(V, v, x, y, r, red, S->scal.p,
                                                                                slot, S->flags.p);
 }
 
@@ -1110,9 +1117,9 @@ template <typename T>
 static void launch_mr_spmv(Ctx* c, SolverData* S, const T* v, T* const* zb, T* q, Red4 red) {
   const SellView V = S->view();
   if (S->A.d16)
-    mr_spmv_k<T, true><<<sell_grid(S), kBlk, 0, c->stream>>>(V, v, zb, q, red, S->scal.p, S->flags.p);
+    mr_spmv_k<T, true><<<sell_grid<T>(S), kBlk, 0, c->stream>>>(V, v, zb, q, red, S->scal.p, S->flags.p);
   else
-    mr_spmv_k<T, false><<<sell_grid(S), kBlk, 0, c->stream>>>(V, v, zb, q, red, S->scal.p, S->flags.p);
+    mr_spmv_k<T, false><<<sell_grid<T>(S), kBlk, 0, c->stream>>>(V, v, zb, q, red, S->scal.p, S->flags.p);
 }
 
 static int read_flags(Ctx* c, SolverData* S, int* h) {
