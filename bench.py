@@ -51,6 +51,75 @@ def build_problem(E, N, seed=20261203, jit=0.2):
     return mesh, fesp, kappa
 
 
+def serving_workload(n, seed=20261204):
+    """The serving stream: N log-uniform in [16, 512] (rounded), T3 or T6 with
+    probability 1/2, kappa uniform in [0.5, 2], Q uniform in [-10, -1],
+    Dirichlet T = 1 + x^2 + 2 y^2, unit square; seeded."""
+    rng = np.random.default_rng(seed)
+    N = np.rint(np.exp(rng.uniform(np.log(16.0), np.log(512.0), n))).astype(int)
+    t6 = rng.random(n) < 0.5
+    kappa = rng.uniform(0.5, 2.0, n)
+    Q = rng.uniform(-10.0, -1.0, n)
+    return [("T6" if t6[i] else "T3", int(N[i]), float(kappa[i]), float(Q[i])) for i in range(n)]
+
+
+def run_stream(E, ctx, reqs, rate, method="pcg32_ir", batched=True, max_active=64, seed=7):
+    """Serve reqs arriving as a Poisson stream of `rate` per second (rate None:
+    all at t = 0, closed loop) on a fresh server; per-request latencies."""
+    srv = E.HeatServer(method, batched=batched, max_active=max_active, rtol=1e-10, ctx=ctx)
+    n = len(reqs)
+    if rate:
+        arr = np.cumsum(np.random.default_rng(seed).exponential(1.0 / rate, n))
+    else:
+        arr = np.zeros(n)
+    t0 = srv.clock()
+    done, i, active_sum, steps = [], 0, 0, 0
+    while len(done) < n:
+        now = srv.clock() - t0
+        while i < n and arr[i] <= now:
+            et, N, kap, Q = reqs[i]
+            srv.submit(E.heat_request(et, N, kappa=kap, Q=Q, t_arrival=t0 + arr[i]))
+            i += 1
+        a, q = srv.step()
+        active_sum += a
+        steps += 1
+        done.extend(srv.poll())
+        if a == 0 and q == 0 and i < n and len(done) < n:
+            time.sleep(max(0.0, min(arr[i] - (srv.clock() - t0), 0.01)))
+    st = srv.stats()
+    srv.close()
+    lat = np.array([r["t_done"] - r["t_arrival"] for r in done])
+    bad = [r for r in done if r["status"] != 0 or not r["converged"] or r["relres"] > 1e-10]
+    span = max(r["t_done"] for r in done) - t0
+    return {"requests": n, "offered_rate_per_s": rate, "solves_per_s": n / span, "makespan_s": span,
+            "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+            "mean_ms": float(lat.mean() * 1e3), "mean_active": active_sum / max(steps, 1), "steps": steps,
+            "failed": len(bad), "iterations_total": int(sum(r["iterations"] for r in done)),
+            "elements_total": int(sum(r["nel"] for r in done)), "server": st}
+
+
+def serve_bench(E, ctx, nreq, fracs, plain_sample):
+    reqs = serving_workload(nreq)
+    run_stream(E, ctx, reqs[:16], None)  # warm-up: graphs, autotuner records
+    cap = run_stream(E, ctx, reqs, None)
+    out = {"workload": f"{nreq} heat requests: unit square, N log-uniform [16,512], T3/T6 1:1, kappa U[0.5,2], "
+                       f"Q U[-10,-1], T = 1 + x^2 + 2y^2 on the boundary, 3-point rule, FP32 CG + FP64 "
+                       f"residual replacement to 1e-10 (seeded; the first {nreq} of the stream)",
+           "closed_loop": cap, "capacity_solves_per_s": cap["solves_per_s"], "rates": []}
+    for f in fracs:
+        out["rates"].append(run_stream(E, ctx, reqs, f * cap["solves_per_s"]))
+    sub = reqs[:plain_sample]
+    plain = run_stream(E, ctx, sub, None, method="pcg64", batched=False)
+    same = run_stream(E, ctx, sub, None)
+    out["plain_fp64_one_at_a_time"] = {"sample": f"first {plain_sample} requests, closed loop",
+                                       "solves_per_s": plain["solves_per_s"], "makespan_s": plain["makespan_s"],
+                                       "failed": plain["failed"]}
+    out["batched_same_sample"] = {"solves_per_s": same["solves_per_s"], "makespan_s": same["makespan_s"],
+                                  "p50_ms": same["p50_ms"], "p99_ms": same["p99_ms"]}
+    out["speedup_vs_plain_same_sample"] = same["solves_per_s"] / plain["solves_per_s"]
+    return out
+
+
 def read_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -201,6 +270,10 @@ def main():
     ap.add_argument("--pcg-methods", default="pcg64,pcg32_ir", help="solves to run, in order")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=512, help="requests of the serving stream (4096: all)")
+    ap.add_argument("--serve-rates", default="0.3,0.6,0.9", help="arrival rates as fractions of the capacity")
+    ap.add_argument("--serve-plain-sample", type=int, default=48)
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -382,6 +455,26 @@ def main():
             st32, T32 = res["pcg32_ir"]
             pcg["speedup"] = st64["seconds"] / st32["seconds"]
             pcg["fp32_vs_fp64_rel_err_max"] = float(np.abs(T32[:nu] - T64[:nu]).max() / np.abs(T64[:nu]).max())
+        if "pcg32_ir" in res:
+            # the batched form with this one system: per-tile kernels, device-side replacement
+            b = E.BatchSolver("pcg32_ir", capacity=1, ctx=ctx)
+            torch.cuda.synchronize()
+            tb0 = time.perf_counter()
+            s = b.add(am, T0, nu, rtol=1e-10)
+            Tb, stb = b.run(graphs=8)[s]
+            tb = time.perf_counter() - tb0
+            b.close()
+            pcg["fp32_ir_batched"] = dict(stb, wall_s=tb)
+            if "pcg64" in res:
+                pcg["speedup_batched"] = res["pcg64"][0]["seconds"] / tb
+                pcg["batched_vs_fp64_rel_err_max"] = float(np.abs(Tb[:nu] - T64[:nu]).max() / np.abs(T64[:nu]).max())
+
+    # --- serving stream: p50/p99 at three arrival rates ------------------
+    serve = None
+    if not args.no_serve and rank == 0:
+        fr = [float(x) for x in args.serve_rates.split(",") if x]
+        serve = serve_bench(E, ctx, args.serve_requests, fr, args.serve_plain_sample)
+        serve["tuning"] = [t for t, _ in ctx.tuning()]
 
     # --- CPU baseline (oracle restatement on the host cores) --------------
     cpu = None
@@ -401,7 +494,7 @@ def main():
                       "elements": nel, "ndofs": n, "nnz": nnz_dev, "l2": "256 MB buffer written between timed steps",
                       "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU"},
            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 3 * args.steps, "clocks": clk,
-           "pcg": pcg, "pattern_build_s": pattern_s, "setup_phases_ms": {k: v[0] for k, v in setup_phases.items()},
+           "pcg": pcg, "serve": serve, "pattern_build_s": pattern_s, "setup_phases_ms": {k: v[0] for k, v in setup_phases.items()},
            "wall_s_timed": wall, "host_mesh_setup_s": host_setup_s}
     if rank == 0:
         print(json.dumps(out), flush=True)

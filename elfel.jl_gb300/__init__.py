@@ -10,6 +10,8 @@ that scripts written against Elfel.jl translate line by line.
 from . import _native
 from .assemblers import (SysmatAssemblerGPU, SysmatAssemblerSparse, SysvecAssembler, assemble, assemble_elasticity,
                          assemble_heat, assemble_stokes, finish, solve, start)
+from .batching import BatchSolver
+from .serving import HeatServer, heat_request
 from .feiterators import (FEIterator, QPIterator, bfun, bfungrad, bfungradpar, eldofcomps, eldofentmdims, eldofs,
                           eldofvals, elnodes, jacjac, location, weight)
 from .felements import FEH1_T3, FEH1_T6, Jacobian, nfeatofdim, ndofperfeat, refshape

@@ -76,6 +76,45 @@ class SolveStats(ctypes.Structure):
                 "relres": self.relres, "seconds": self.seconds}
 
 
+class BlockDesc(ctypes.Structure):
+    _fields_ = [("nodes_per_elem", ctypes.c_int32), ("orientation", ctypes.c_int32), ("nx", ctypes.c_int32),
+                ("ny", ctypes.c_int32), ("lx", ctypes.c_double), ("ly", ctypes.c_double), ("npts", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("qp_coords", _dp), ("qp_weights", _dp)]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("method", ctypes.c_int32), ("batched", ctypes.c_int32), ("max_active", ctypes.c_int32),
+                ("graphs_per_step", ctypes.c_int32), ("rtol", ctypes.c_double), ("maxit", ctypes.c_int32),
+                ("keep_idle", ctypes.c_int32), ("mem_budget", ctypes.c_int64)]
+
+
+class HeatRequest(ctypes.Structure):
+    _fields_ = [("nodes_per_elem", ctypes.c_int32), ("orientation", ctypes.c_int32), ("nx", ctypes.c_int32),
+                ("ny", ctypes.c_int32), ("lx", ctypes.c_double), ("ly", ctypes.c_double), ("kappa", ctypes.c_double),
+                ("Q", ctypes.c_double), ("dirichlet", ctypes.c_double * 6), ("t_arrival", ctypes.c_double),
+                ("keep_solution", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class ServeResult(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_int64), ("status", ctypes.c_int32), ("iterations", ctypes.c_int32),
+                ("refinements", ctypes.c_int32), ("converged", ctypes.c_int32), ("relres", ctypes.c_double),
+                ("t_arrival", ctypes.c_double), ("t_admit", ctypes.c_double), ("t_done", ctypes.c_double),
+                ("ndofs", ctypes.c_int64), ("nu", ctypes.c_int64), ("nel", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_int64) for k in ("submitted", "completed", "rejected", "systems_created",
+                                              "systems_reused", "systems_evicted", "resident_systems",
+                                              "resident_bytes", "graph_launches", "solver_kernel_launches",
+                                              "kernel_launches")] + [("busy_seconds", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 # name -> (restype, argtypes); the full exported surface of include/elfel_gpu.h
 SIGNATURES = {
     "elfel_abi_version": (ctypes.c_int, []),
@@ -106,6 +145,29 @@ SIGNATURES = {
     "elfel_fused_stokes": (ctypes.c_int, [_vp, ctypes.c_double]),
     "elfel_solve": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, ctypes.c_int32,
                                    ctypes.POINTER(SolveStats)]),
+    "elfel_batch_create": (ctypes.c_int, [_vp, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(_vp)]),
+    "elfel_batch_destroy": (ctypes.c_int, [_vp]),
+    "elfel_batch_add": (ctypes.c_int, [_vp, _vp, _dp, _dp, ctypes.c_int64, ctypes.c_double, ctypes.c_int32,
+                                       ctypes.POINTER(ctypes.c_int32)]),
+    "elfel_batch_step": (ctypes.c_int, [_vp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]),
+    "elfel_batch_done": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int32), ctypes.c_int32,
+                                        ctypes.POINTER(ctypes.c_int32)]),
+    "elfel_batch_result": (ctypes.c_int, [_vp, ctypes.c_int32, _dp, ctypes.POINTER(SolveStats)]),
+    "elfel_ctx_tuning": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int,
+                                        ctypes.POINTER(ctypes.c_int32)]),
+    "elfel_fused_setup_block": (ctypes.c_int, [_vp, ctypes.POINTER(BlockDesc), _i64p, _i64p]),
+    "elfel_block_dirichlet": (ctypes.c_int, [_vp, _dp, _dp]),
+    "elfel_fused_tables": (ctypes.c_int, [_vp, _i64p, _dp, _i64p]),
+    "elfel_fused_dims": (ctypes.c_int, [_vp, _i64p, _i64p, _i64p]),
+    "elfel_server_create": (ctypes.c_int, [_vp, ctypes.POINTER(ServerConfig), ctypes.POINTER(_vp)]),
+    "elfel_server_destroy": (ctypes.c_int, [_vp]),
+    "elfel_server_clock": (ctypes.c_int, [_vp, _dp]),
+    "elfel_server_submit": (ctypes.c_int, [_vp, ctypes.POINTER(HeatRequest), _i64p]),
+    "elfel_server_step": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
+    "elfel_server_poll": (ctypes.c_int, [_vp, ctypes.POINTER(ServeResult), ctypes.c_int32,
+                                         ctypes.POINTER(ctypes.c_int32)]),
+    "elfel_server_solution": (ctypes.c_int, [_vp, ctypes.c_int64, _dp, ctypes.c_int64]),
+    "elfel_server_stats_read": (ctypes.c_int, [_vp, ctypes.POINTER(ServerStats)]),
 }
 
 _LIB = None
@@ -200,9 +262,21 @@ class Context:
             i += 1
         return out
 
+    def tuning(self):
+        """Autotuner records: [(line, chosen index)], one per tuned key."""
+        out = []
+        buf = ctypes.create_string_buffer(512)
+        ch = ctypes.c_int32()
+        i = 0
+        while self.lib.elfel_ctx_tuning(self.h, i, buf, 512, ctypes.byref(ch)) == ELFEL_OK:
+            out.append((buf.value.decode(), ch.value))
+            i += 1
+        return out
+
     def close(self):
         if getattr(self, "h", None):
-            for ch in list(self._children):
+            # batches hold systems: close them before the systems
+            for ch in sorted(self._children, key=lambda o: 0 if getattr(o, "_holds_systems", False) else 1):
                 ch.close()
             self.lib.elfel_ctx_destroy(self.h)
             self.h = None

@@ -223,8 +223,49 @@ class SysmatAssemblerGPU:
         self.physics = physics
         self.nrow = self.ncol = n
         self.nel = elit.fesp.mesh.nel
+        self._nn = elit.fesp.mesh.nodes_per_elem
+        self._nedof = self._nn * elit.fesp.nfecopies
         self._setup_key = (id(elit.fesp), id(pelit.fesp) if pelit is not None else None, qr.npts, physics, n)
         return self
+
+    def setup_block(self, etype, nx, ny, lx=1.0, ly=1.0, orientation="a", npts=3):
+        """Heat set-up from a block mesh generated on the device (T3block /
+        T6block of [0,lx] x [0,ly], boundary fixed, numberdofs! order).
+        Returns (ndofs, nunknowns)."""
+        from .refshapes import quadrature
+
+        qr = quadrature(quadraturesettings={"npts": npts})
+        pc, w = N.f64(qr.param_coords), N.f64(qr.weights)
+        d = N.BlockDesc(3 if etype == "T3" else 6, {"a": 0, "alternate": 1}[orientation], int(nx), int(ny),
+                        float(lx), float(ly), int(npts), 0, N.ptr(pc), N.ptr(w))
+        n, nu = ctypes.c_int64(), ctypes.c_int64()
+        self._hd.check(self._hd.lib.elfel_fused_setup_block(self._hd.h, ctypes.byref(d), ctypes.byref(n),
+                                                            ctypes.byref(nu)))
+        self.physics = N.ELFEL_HEAT
+        self.nrow = self.ncol = n.value
+        self.nel = 2 * int(nx) * int(ny)
+        self._nn = self._nedof = 3 if etype == "T3" else 6
+        self._setup_key = ("block", etype, nx, ny, lx, ly, orientation, npts)
+        return n.value, nu.value
+
+    def block_dirichlet(self, coef):
+        """T (ndofs): 0 at free DOFs, c0 + c1 x + c2 y + c3 x^2 + c4 x y + c5 y^2 at data DOFs."""
+        c = N.f64(np.asarray(coef, dtype=np.float64).reshape(6))
+        T = np.empty(self.nrow)
+        self._hd.check(self._hd.lib.elfel_block_dirichlet(self._hd.h, N.ptr(c), N.ptr(T)))
+        return T
+
+    def tables(self):
+        """(conn, xy, eldofs) of the fused system, 1-based as the set-up takes them."""
+        nel, nnodes, nd = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        self._hd.check(self._hd.lib.elfel_fused_dims(self._hd.h, ctypes.byref(nel), ctypes.byref(nnodes),
+                                                     ctypes.byref(nd)))
+        conn = np.empty((nel.value, self._nn), dtype=np.int64)
+        dofs = np.empty((nel.value, self._nedof), dtype=np.int64)
+        xy = np.empty((nnodes.value, 2))
+        self._hd.check(self._hd.lib.elfel_fused_tables(self._hd.h, N.ptr(conn, N._i64p), N.ptr(xy),
+                                                       N.ptr(dofs, N._i64p)))
+        return conn, xy, dofs
 
     def _ensure(self, physics, elit, qpit, pelit=None):
         key = (id(elit.fesp), id(pelit.fesp) if pelit is not None else None, qpit.quadr.npts, physics, self.nrow)

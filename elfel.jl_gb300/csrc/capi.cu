@@ -116,6 +116,13 @@ static CooStage* stage_of(elfel_sysmat* m) {
     if (!(m) || !(m)->h) return ELFEL_ERR_ARG; \
   } while (0)
 
+// Calls that change a system refuse while a batch slot holds it.
+#define CHECK_FREE(m)                                                                             \
+  do {                                                                                            \
+    CHECK_M(m);                                                                                   \
+    if ((m)->busy) return fail(&(m)->h->c, ELFEL_ERR_STATE, "the system is held by a batch slot"); \
+  } while (0)
+
 extern "C" int elfel_sysmat_create(elfel_ctx* h, elfel_sysmat** out) {
   if (!h || !out) return ELFEL_ERR_ARG;
   elfel_sysmat* m = new elfel_sysmat();
@@ -144,6 +151,7 @@ static void release_all(elfel_sysmat* m) {
 
 extern "C" int elfel_sysmat_destroy(elfel_sysmat* m) {
   if (!m) return ELFEL_OK;
+  if (m->busy) return fail(&m->h->c, ELFEL_ERR_STATE, "destroy: the system is held by a batch slot");
   if (m->h) {
     cudaSetDevice(m->h->c.device);
     release_all(m);
@@ -155,7 +163,7 @@ extern "C" int elfel_sysmat_destroy(elfel_sysmat* m) {
 }
 
 extern "C" int elfel_sysmat_start(elfel_sysmat* m, int64_t nrow, int64_t ncol) {
-  CHECK_M(m);
+  CHECK_FREE(m);
   Ctx* c = &m->h->c;
   if (nrow < 0 || ncol < 0) return fail(c, ELFEL_ERR_ARG, "start!: negative dimensions");
   cudaSetDevice(c->device);
@@ -168,7 +176,7 @@ extern "C" int elfel_sysmat_start(elfel_sysmat* m, int64_t nrow, int64_t ncol) {
 
 extern "C" int elfel_sysmat_assemble_coo(elfel_sysmat* m, const int64_t* rows, const int64_t* cols,
                                          const double* vals, int64_t n) {
-  CHECK_M(m);
+  CHECK_FREE(m);
   Ctx* c = &m->h->c;
   if (!m->started || m->fused) return fail(c, ELFEL_ERR_STATE, "assemble!: call start! first (COO mode)");
   if (n < 0 || (n > 0 && (!rows || !cols || !vals))) return fail(c, ELFEL_ERR_ARG, "assemble!: bad arrays");
@@ -187,7 +195,7 @@ extern "C" int elfel_sysmat_assemble_coo(elfel_sysmat* m, const int64_t* rows, c
 }
 
 extern "C" int elfel_sysmat_finish(elfel_sysmat* m, int64_t* nnz) {
-  CHECK_M(m);
+  CHECK_FREE(m);
   Ctx* c = &m->h->c;
   if (!m->started) return fail(c, ELFEL_ERR_STATE, "finish!: call start! first");
   cudaSetDevice(c->device);
@@ -334,7 +342,7 @@ static int upload_space(Ctx* c, const elfel_space& s, int64_t ndofs, DBuf<int32_
 }
 
 extern "C" int elfel_fused_setup(elfel_sysmat* m, const elfel_fused_desc* d) {
-  CHECK_M(m);
+  CHECK_FREE(m);
   Ctx* c = &m->h->c;
   if (!d) return fail(c, ELFEL_ERR_ARG, "fused_setup: NULL descriptor");
   cudaSetDevice(c->device);
@@ -365,10 +373,25 @@ extern "C" int elfel_fused_setup(elfel_sysmat* m, const elfel_fused_desc* d) {
   F.nnodes_u = u.nnodes;
   ELFEL_TRY(make_tables(u.nodes_per_elem, d->npts, d->qp_coords, d->qp_weights, &F.tab));
   ELFEL_TRY(upload_space(c, u, d->ndofs, &F.conn_u, &F.xy_u, &F.dofs_u, "primary"));
-  const int nedof = u.nodes_per_elem * u.ncomp;
+  if (d->physics == ELFEL_STOKES) {
+    F.nn_p = 3;
+    F.nnodes_p = d->p.nnodes;
+    ELFEL_TRY(upload_space(c, d->p, d->ndofs, &F.conn_p, nullptr, &F.dofs_p, "pressure"));
+  }
+  return fused_build(m, d->ndofs);
+}
+
+namespace elfel {
+
+// Slot generators, patterns and value buffers of a fused system whose tables
+// (connectivity, coordinates, element DOFs) are already on the device.
+int fused_build(elfel_sysmat* m, int64_t ndofs) {
+  Ctx* c = &m->h->c;
+  Fused& F = m->F;
+  const int nedof = F.nn_u * F.ncomp_u;
   SlotGen& g = F.kgen;
   g = SlotGen();
-  g.nel = u.nel;
+  g.nel = F.nel;
   g.nblocks = 1;
   g.b[0].R = F.dofs_u.p;
   g.b[0].C = F.dofs_u.p;
@@ -376,10 +399,7 @@ extern "C" int elfel_fused_setup(elfel_sysmat* m, const elfel_fused_desc* d) {
   g.b[0].sym = 1;
   g.slots_per_elem = nedof * nedof;
   g.store_per_elem = nedof * (nedof + 1) / 2;
-  if (d->physics == ELFEL_STOKES) {
-    F.nn_p = 3;
-    F.nnodes_p = d->p.nnodes;
-    ELFEL_TRY(upload_space(c, d->p, d->ndofs, &F.conn_p, nullptr, &F.dofs_p, "pressure"));
+  if (F.physics == ELFEL_STOKES) {
     g.nblocks = 3;
     g.b[1].R = F.dofs_u.p;
     g.b[1].C = F.dofs_p.p;
@@ -393,15 +413,15 @@ extern "C" int elfel_fused_setup(elfel_sysmat* m, const elfel_fused_desc* d) {
     g.slots_per_elem = 216;
     g.store_per_elem = 78 + 36;
   }
-  m->nrow = m->ncol = d->ndofs;
+  m->nrow = m->ncol = ndofs;
   {
     Phase ph(c, "pattern_K");
-    ELFEL_TRY(build_pattern(c, g, d->ndofs, d->ndofs, &m->P));
+    ELFEL_TRY(build_pattern(c, g, ndofs, ndofs, &m->P));
   }
   // right-hand side: a 1 x ndofs "matrix" of the element vectors
   SlotGen& fg = F.fgen;
   fg = SlotGen();
-  fg.nel = u.nel;
+  fg.nel = F.nel;
   fg.nblocks = 1;
   fg.b[0].R = nullptr;
   fg.b[0].C = F.dofs_u.p;
@@ -409,10 +429,10 @@ extern "C" int elfel_fused_setup(elfel_sysmat* m, const elfel_fused_desc* d) {
   fg.b[0].nc = nedof;
   fg.slots_per_elem = nedof;
   fg.store_per_elem = nedof;
-  ELFEL_TRY(build_pattern(c, fg, 1, d->ndofs, &F.fpat));
-  if (d->physics == ELFEL_STOKES) {
+  ELFEL_TRY(build_pattern(c, fg, 1, ndofs, &F.fpat));
+  if (F.physics == ELFEL_STOKES) {
     SlotGen pg;
-    pg.nel = u.nel;
+    pg.nel = F.nel;
     pg.nblocks = 1;
     pg.b[0].R = nullptr;
     pg.b[0].C = F.dofs_p.p;
@@ -420,15 +440,15 @@ extern "C" int elfel_fused_setup(elfel_sysmat* m, const elfel_fused_desc* d) {
     pg.b[0].nc = 3;
     pg.slots_per_elem = 3;
     pg.store_per_elem = 3;
-    ELFEL_TRY(build_pattern(c, pg, 1, d->ndofs, &F.pmpat));
-    ELFEL_TRY(F.pmass_store.alloc(c, (size_t)(u.nel * 3 > 0 ? u.nel * 3 : 1)));
-    ELFEL_TRY(F.pmass_diag.alloc(c, (size_t)(d->ndofs > 0 ? d->ndofs : 1)));
+    ELFEL_TRY(build_pattern(c, pg, 1, ndofs, &F.pmpat));
+    ELFEL_TRY(F.pmass_store.alloc(c, (size_t)(F.nel * 3 > 0 ? F.nel * 3 : 1)));
+    ELFEL_TRY(F.pmass_diag.alloc(c, (size_t)(ndofs > 0 ? ndofs : 1)));
   }
-  ELFEL_TRY(F.kstore.alloc(c, (size_t)(u.nel * g.store_per_elem > 0 ? u.nel * g.store_per_elem : 1)));
-  ELFEL_TRY(F.fstore.alloc(c, (size_t)(u.nel * nedof > 0 ? u.nel * nedof : 1)));
+  ELFEL_TRY(F.kstore.alloc(c, (size_t)(F.nel * g.store_per_elem > 0 ? F.nel * g.store_per_elem : 1)));
+  ELFEL_TRY(F.fstore.alloc(c, (size_t)(F.nel * nedof > 0 ? F.nel * nedof : 1)));
   ELFEL_TRY(m->vals.alloc(c, (size_t)(m->P.nnz > 0 ? m->P.nnz : 1)));
-  ELFEL_TRY(m->rhs.alloc(c, (size_t)(d->ndofs > 0 ? d->ndofs : 1)));
-  ELFEL_TRY(F.coef.alloc(c, (size_t)(u.nel > 0 ? 2 * u.nel : 1)));
+  ELFEL_TRY(m->rhs.alloc(c, (size_t)(ndofs > 0 ? ndofs : 1)));
+  ELFEL_TRY(F.coef.alloc(c, (size_t)(F.nel > 0 ? 2 * F.nel : 1)));
   ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
   m->fused = 1;
   m->started = 1;
@@ -436,8 +456,69 @@ extern "C" int elfel_fused_setup(elfel_sysmat* m, const elfel_fused_desc* d) {
   return ELFEL_OK;
 }
 
-extern "C" int elfel_fused_set_geometry(elfel_sysmat* m, const double* xy) {
+}  // namespace elfel
+
+extern "C" int elfel_fused_setup_block(elfel_sysmat* m, const elfel_block_desc* d, int64_t* ndofs, int64_t* nu) {
+  CHECK_FREE(m);
+  Ctx* c = &m->h->c;
+  if (!d) return fail(c, ELFEL_ERR_ARG, "setup_block: NULL descriptor");
+  if (d->npts < 1 || d->npts > kMaxQP || !d->qp_coords || !d->qp_weights)
+    return fail(c, ELFEL_ERR_ARG, "setup_block: quadrature with %d points (1..%d)", d->npts, kMaxQP);
+  if (d->nodes_per_elem != 3 && d->nodes_per_elem != 6)
+    return fail(c, ELFEL_ERR_UNSUPPORTED, "setup_block: T3 or T6 blocks (nodes_per_elem %d)", d->nodes_per_elem);
+  cudaSetDevice(c->device);
+  release_all(m);
+  Fused& F = m->F;
+  F.physics = ELFEL_HEAT;
+  F.npts = d->npts;
+  ELFEL_TRY(make_tables(d->nodes_per_elem, d->npts, d->qp_coords, d->qp_weights, &F.tab));
+  int64_t nfree = 0;
+  ELFEL_TRY(block_tables(c, *d, &F, &nfree));
+  F.is_block = 1;
+  F.block = *d;
+  F.block.qp_coords = nullptr;  // not kept
+  F.block.qp_weights = nullptr;
+  ELFEL_TRY(fused_build(m, F.nnodes_u));
+  if (ndofs) *ndofs = F.nnodes_u;
+  if (nu) *nu = nfree;
+  return ELFEL_OK;
+}
+
+extern "C" int elfel_block_dirichlet(elfel_sysmat* m, const double* coef6, double* T) {
   CHECK_M(m);
+  Ctx* c = &m->h->c;
+  if (!m->fused || !m->F.is_block) return fail(c, ELFEL_ERR_STATE, "block_dirichlet: not a block system");
+  if (!coef6 || !T) return fail(c, ELFEL_ERR_ARG, "block_dirichlet: NULL argument");
+  cudaSetDevice(c->device);
+  const int64_t n = m->F.nnodes_u;
+  DBuf<double> d;
+  ELFEL_TRY(d.alloc(c, (size_t)n));
+  ELFEL_TRY(block_dirichlet(c, m->F.block, coef6, m->F, d.p));
+  ELFEL_CUDA(c, cudaMemcpyAsync(T, d.p, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+  ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+  d.release(c);
+  return ELFEL_OK;
+}
+
+extern "C" int elfel_fused_tables(elfel_sysmat* m, int64_t* conn, double* xy, int64_t* eldofs) {
+  CHECK_M(m);
+  Ctx* c = &m->h->c;
+  if (!m->fused) return fail(c, ELFEL_ERR_STATE, "fused_tables: not a fused system");
+  cudaSetDevice(c->device);
+  return tables_to_host(c, m->F, conn, xy, eldofs);
+}
+
+extern "C" int elfel_fused_dims(elfel_sysmat* m, int64_t* nel, int64_t* nnodes, int64_t* ndofs) {
+  CHECK_M(m);
+  if (!m->fused) return fail(&m->h->c, ELFEL_ERR_STATE, "fused_dims: not a fused system");
+  if (nel) *nel = m->F.nel;
+  if (nnodes) *nnodes = m->F.nnodes_u;
+  if (ndofs) *ndofs = m->nrow;
+  return ELFEL_OK;
+}
+
+extern "C" int elfel_fused_set_geometry(elfel_sysmat* m, const double* xy) {
+  CHECK_FREE(m);
   Ctx* c = &m->h->c;
   if (!m->fused) return fail(c, ELFEL_ERR_STATE, "set_geometry: call fused_setup first");
   if (!xy) return fail(c, ELFEL_ERR_ARG, "set_geometry: NULL coordinates");
@@ -465,7 +546,7 @@ static int finish_values(elfel_sysmat* m) {
 }
 
 extern "C" int elfel_fused_heat(elfel_sysmat* m, const double* kappa, double Q) {
-  CHECK_M(m);
+  CHECK_FREE(m);
   Ctx* c = &m->h->c;
   if (!m->fused || m->F.physics != ELFEL_HEAT) return fail(c, ELFEL_ERR_STATE, "heat: fused_setup(ELFEL_HEAT) first");
   cudaSetDevice(c->device);
@@ -482,7 +563,7 @@ extern "C" int elfel_fused_heat(elfel_sysmat* m, const double* kappa, double Q) 
 extern "C" int elfel_fused_elasticity(elfel_sysmat* m, double E, double nu, int32_t plane_strain,
                                       const double* bforce, const int64_t* trac_edges, int64_t ntrac,
                                       const double* traction) {
-  CHECK_M(m);
+  CHECK_FREE(m);
   Ctx* c = &m->h->c;
   if (!m->fused || m->F.physics != ELFEL_ELASTICITY)
     return fail(c, ELFEL_ERR_STATE, "elasticity: fused_setup(ELFEL_ELASTICITY) first");
@@ -556,7 +637,7 @@ extern "C" int elfel_fused_elasticity(elfel_sysmat* m, double E, double nu, int3
 }
 
 extern "C" int elfel_fused_stokes(elfel_sysmat* m, double mu) {
-  CHECK_M(m);
+  CHECK_FREE(m);
   Ctx* c = &m->h->c;
   if (!m->fused || m->F.physics != ELFEL_STOKES)
     return fail(c, ELFEL_ERR_STATE, "stokes: fused_setup(ELFEL_STOKES) first");

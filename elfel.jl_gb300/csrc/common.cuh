@@ -37,7 +37,18 @@ struct Ctx {
   // phase timing: CUDA events recorded on `stream` around each kernel launch
   int profiling = 0;
   std::vector<PhaseRec> phases;
+  // autotuner: on unless ELFEL_TUNE=0; one line per tuned key
+  int tune = 1;
+  std::vector<std::string> tune_lines;
+  std::vector<std::string> tune_keys;
+  std::vector<int> tune_choice;
 };
+
+// Record the autotuner's timings of the candidates (names comma-separated in
+// cand) for key and the chosen index; replaces an earlier record of the key.
+void tune_record(Ctx* c, const char* key, const std::string& cand, int best, const std::vector<double>& ms);
+// The recorded choice for key, or -1.
+int tune_lookup(const Ctx* c, const char* key);
 
 // Records a start event on construction and a stop event on destruction when
 // the context is profiling; otherwise does nothing.

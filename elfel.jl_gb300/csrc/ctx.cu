@@ -201,7 +201,51 @@ extern "C" int elfel_ctx_create(int device, int64_t mem_budget_bytes, elfel_ctx*
   h->c.own_stream = h->c.stream;
   const char* tr = getenv("ELFEL_TRACE");
   h->c.trace = (tr && tr[0] == '1') ? 1 : 0;
+  const char* tu = getenv("ELFEL_TUNE");
+  h->c.tune = (tu && tu[0] == '0') ? 0 : 1;
   *out = h;
+  return ELFEL_OK;
+}
+
+namespace elfel {
+
+void tune_record(Ctx* c, const char* key, const std::string& cand, int best, const std::vector<double>& ms) {
+  std::string line = std::string(key) + ":";
+  size_t pos = 0;
+  for (size_t k = 0; k < ms.size(); ++k) {
+    const size_t e = cand.find(',', pos);
+    const std::string name = cand.substr(pos, e == std::string::npos ? std::string::npos : e - pos);
+    pos = e == std::string::npos ? cand.size() : e + 1;
+    char one[96];
+    snprintf(one, sizeof(one), " %s=%.4fms", name.c_str(), ms[k]);
+    line += one;
+    if ((int)k == best) line += "*";
+  }
+  for (size_t i = 0; i < c->tune_keys.size(); ++i)
+    if (c->tune_keys[i] == key) {
+      c->tune_lines[i] = line;
+      c->tune_choice[i] = best;
+      return;
+    }
+  c->tune_keys.push_back(key);
+  c->tune_lines.push_back(line);
+  c->tune_choice.push_back(best);
+}
+
+int tune_lookup(const Ctx* c, const char* key) {
+  for (size_t i = 0; i < c->tune_keys.size(); ++i)
+    if (c->tune_keys[i] == key) return c->tune_choice[i];
+  return -1;
+}
+
+}  // namespace elfel
+
+extern "C" int elfel_ctx_tuning(const elfel_ctx* h, int index, char* line, int cap, int32_t* choice) {
+  if (!h) return ELFEL_ERR_ARG;
+  const Ctx* c = &h->c;
+  if (index < 0 || index >= (int)c->tune_lines.size()) return ELFEL_ERR_ARG;
+  if (line && cap > 0) snprintf(line, (size_t)cap, "%s", c->tune_lines[index].c_str());
+  if (choice) *choice = c->tune_choice[index];
   return ELFEL_OK;
 }
 

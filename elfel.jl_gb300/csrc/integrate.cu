@@ -115,12 +115,12 @@ __device__ __forceinline__ void stage_tables(const QPTab& t, SmemTab* s) {
 }
 
 // Load a CTA's connectivity tile (coalesced) and gather this thread's nodes.
-template <int NN>
+template <int NN, int NT = kIntThreads>
 __device__ __forceinline__ void load_geo(const int32_t* __restrict__ conn, const double2* __restrict__ xy, int64_t e0,
                                          int64_t nel, int32_t* sconn, Geo<NN>& g, int32_t* nodes) {
   const int64_t base = e0 * NN;
   const int64_t lim = nel * NN;
-  for (int k = threadIdx.x; k < kIntThreads * NN; k += kIntThreads) {
+  for (int k = threadIdx.x; k < NT * NN; k += NT) {
     int64_t gi = base + k;
     sconn[k] = gi < lim ? __ldg(conn + gi) : 0;
   }
@@ -135,33 +135,34 @@ __device__ __forceinline__ void load_geo(const int32_t* __restrict__ conn, const
   }
 }
 
-// Write a CTA's records, staged as acc[k * (kIntThreads + 1) + t], to
+// Write a CTA's records, staged as acc[k * (NT + 1) + t], to
 // out[(e0 + t) * rec + k] in one contiguous pass.
+template <int NT = kIntThreads>
 __device__ __forceinline__ void write_records(const double* acc, int rec, int64_t e0, int64_t nel, double* out) {
   __syncthreads();
-  const int64_t nvalid = min((int64_t)kIntThreads, nel - e0);
+  const int64_t nvalid = min((int64_t)NT, nel - e0);
   const int64_t total = nvalid * rec;
   double* dst = out + e0 * rec;
-  for (int64_t L = threadIdx.x; L < total; L += kIntThreads) {
+  for (int64_t L = threadIdx.x; L < total; L += NT) {
     int t = (int)(L / rec), k = (int)(L - (int64_t)t * rec);
-    dst[L] = acc[k * (kIntThreads + 1) + t];
+    dst[L] = acc[k * (NT + 1) + t];
   }
 }
 
 // ------------------------------------------------------------------ heat
-template <int NN>
-__global__ void __launch_bounds__(kIntThreads) heat_k(int64_t nel, const int32_t* __restrict__ conn,
-                                                     const double2* __restrict__ xy, const double* __restrict__ kappa,
-                                                     double Q, const __grid_constant__ QPTab tab,
-                                                     double* __restrict__ kstore, double* __restrict__ fstore) {
+// The NT elements e0 .. e0 + NT - 1 of one mesh, one per thread.
+template <int NN, int NT>
+__device__ __forceinline__ void heat_elems(int64_t e0, int64_t nel, const int32_t* __restrict__ conn,
+                                           const double2* __restrict__ xy, const double* __restrict__ kappa, double Q,
+                                           const QPTab& tab, double* __restrict__ kstore, double* __restrict__ fstore) {
   constexpr int NS = NN * (NN + 1) / 2;
-  constexpr int LD = kIntThreads + 1;
+  constexpr int LD = NT + 1;
   extern __shared__ double acc[];  // (NS + NN) * LD
   __shared__ SmemTab st;
-  __shared__ int32_t sconn[kIntThreads * NN];
+  __shared__ int32_t sconn[NT * NN];
   __shared__ double sS[3][NS];
   stage_tables(tab, &st);
-  for (int k = threadIdx.x; k < NS; k += kIntThreads) {
+  for (int k = threadIdx.x; k < NS; k += NT) {
     int j = 0;
     while ((j + 1) * (j + 2) / 2 <= k) ++j;
     int i = k - j * (j + 1) / 2;
@@ -169,9 +170,8 @@ __global__ void __launch_bounds__(kIntThreads) heat_k(int64_t nel, const int32_t
     sS[1][k] = tab.S[1][1][i * 6 + j];
     sS[2][k] = tab.S[0][1][i * 6 + j] + tab.S[1][0][i * 6 + j];
   }
-  const int64_t e0 = (int64_t)blockIdx.x * kIntThreads;
   Geo<NN> g;
-  load_geo<NN>(conn, xy, e0, nel, sconn, g, nullptr);  // contains __syncthreads
+  load_geo<NN, NT>(conn, xy, e0, nel, sconn, g, nullptr);  // contains __syncthreads
   const int t = threadIdx.x;
   const int64_t e = e0 + t;
   double* fa = acc + NS * LD;
@@ -229,21 +229,66 @@ __global__ void __launch_bounds__(kIntThreads) heat_k(int64_t nel, const int32_t
       for (int j = 0; j < NN; ++j) fa[j * LD + t] = fe[j];
     }
   }
-  write_records(acc, NS, e0, nel, kstore);
+  write_records<NT>(acc, NS, e0, nel, kstore);
   __syncthreads();
-  write_records(fa, NN, e0, nel, fstore);
+  write_records<NT>(fa, NN, e0, nel, fstore);
 }
+
+template <int NN>
+__global__ void __launch_bounds__(kIntThreads) heat_k(int64_t nel, const int32_t* __restrict__ conn,
+                                                     const double2* __restrict__ xy, const double* __restrict__ kappa,
+                                                     double Q, const __grid_constant__ QPTab tab,
+                                                     double* __restrict__ kstore, double* __restrict__ fstore) {
+  heat_elems<NN, kIntThreads>((int64_t)blockIdx.x * kIntThreads, nel, conn, xy, kappa, Q, tab, kstore, fstore);
+}
+
+// Many meshes in one launch: CTA b works on mesh k with jobs[k].blk0 <= b <
+// jobs[k + 1].blk0, elements (b - blk0) * NT onwards.
+template <int NN, int NT>
+__global__ void __launch_bounds__(NT) heat_batch_k(const HeatJob* __restrict__ jobs, int njobs,
+                                                   const __grid_constant__ QPTab tab) {
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {  // last job with blk0 <= blockIdx.x
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].blk0 <= (int64_t)blockIdx.x) lo = mid; else hi = mid - 1;
+  }
+  const HeatJob J = jobs[lo];
+  heat_elems<NN, NT>(((int64_t)blockIdx.x - J.blk0) * NT, J.nel, J.conn, (const double2*)J.xy, J.kappa, J.Q, tab,
+                     J.kstore, J.fstore);
+}
+
+static size_t heat_smem(int nn, int nt) { return (size_t)(nn == 3 ? 6 + 3 : 21 + 6) * (nt + 1) * sizeof(double); }
 
 int launch_heat(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* xy, const double* kappa, double Q,
                 const QPTab& tab, double* kstore, double* fstore) {
   if (nel == 0) return ELFEL_OK;
   const unsigned grid = grid_for(nel, kIntThreads);
-  if (nn == 3) {
-    const size_t sm = (size_t)(6 + 3) * (kIntThreads + 1) * sizeof(double);
-    heat_k<3><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, (const double2*)xy, kappa, Q, tab, kstore, fstore);
-  } else {
-    const size_t sm = (size_t)(21 + 6) * (kIntThreads + 1) * sizeof(double);
-    heat_k<6><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, (const double2*)xy, kappa, Q, tab, kstore, fstore);
+  if (nn == 3)
+    heat_k<3><<<grid, kIntThreads, heat_smem(3, kIntThreads), c->stream>>>(nel, conn, (const double2*)xy, kappa, Q,
+                                                                          tab, kstore, fstore);
+  else
+    heat_k<6><<<grid, kIntThreads, heat_smem(6, kIntThreads), c->stream>>>(nel, conn, (const double2*)xy, kappa, Q,
+                                                                          tab, kstore, fstore);
+  ELFEL_LAUNCH_CHECK(c);
+  return ELFEL_OK;
+}
+
+template <int NN, int NT>
+static void heat_batch_launch(Ctx* c, const HeatJob* jobs, int njobs, int64_t blocks, const QPTab& tab) {
+  heat_batch_k<NN, NT><<<(unsigned)blocks, NT, heat_smem(NN, NT), c->stream>>>(jobs, njobs, tab);
+}
+
+int launch_heat_batch(Ctx* c, int nn, int nt, const HeatJob* jobs_dev, int njobs, int64_t blocks, const QPTab& tab) {
+  if (njobs == 0 || blocks == 0) return ELFEL_OK;
+  if (blocks > 0x7fffffff) return fail(c, ELFEL_ERR_ARG, "batched heat: too many elements");
+  switch (nt) {
+    case 64: nn == 3 ? heat_batch_launch<3, 64>(c, jobs_dev, njobs, blocks, tab)
+                     : heat_batch_launch<6, 64>(c, jobs_dev, njobs, blocks, tab); break;
+    case 128: nn == 3 ? heat_batch_launch<3, 128>(c, jobs_dev, njobs, blocks, tab)
+                      : heat_batch_launch<6, 128>(c, jobs_dev, njobs, blocks, tab); break;
+    case 256: nn == 3 ? heat_batch_launch<3, 256>(c, jobs_dev, njobs, blocks, tab)
+                      : heat_batch_launch<6, 256>(c, jobs_dev, njobs, blocks, tab); break;
+    default: return fail(c, ELFEL_ERR_ARG, "batched heat: %d threads per CTA (64, 128 or 256)", nt);
   }
   ELFEL_LAUNCH_CHECK(c);
   return ELFEL_OK;

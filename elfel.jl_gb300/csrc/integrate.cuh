@@ -33,6 +33,21 @@ int make_tables(int nn, int npts, const double* pc, const double* w, QPTab* t);
 
 int launch_heat(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* xy, const double* kappa, double Q,
                 const QPTab& tab, double* kstore, double* fstore);
+
+// One mesh of a batched heat integration (device array, ordered by blk0).
+struct HeatJob {
+  int64_t blk0;  // first CTA of this mesh
+  int64_t nel;
+  const int32_t* conn;
+  const double* xy;
+  const double* kappa;
+  double Q;
+  double* kstore;
+  double* fstore;
+};
+// All meshes of jobs_dev (same element type nn and tables) in one launch of
+// `blocks` CTAs of nt threads (64, 128 or 256; one element per thread).
+int launch_heat_batch(Ctx* c, int nn, int nt, const HeatJob* jobs_dev, int njobs, int64_t blocks, const QPTab& tab);
 int launch_elasticity(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* xy, const Mat3& D,
                       const double* bforce, const QPTab& tab, double* kstore, double* fstore);
 int launch_traction(Ctx* c, int64_t ntrac, const int32_t* edges, const int32_t* conn, int nn, const double* xy,

@@ -21,7 +21,6 @@ namespace elfel {
 
 constexpr int kSortThreads = 256;           // 8 warps, one column each
 constexpr int kSortCap = 256;               // keys per warp sorted in shared memory
-constexpr uint64_t kKeyInf = ~0ull;
 
 __global__ void count_cols_k(SlotGen g, int64_t n, int32_t* colcnt, int64_t ncol, int64_t nrow, int* bad) {
   for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
@@ -225,6 +224,42 @@ __global__ void reduce_k(const int32_t* __restrict__ cptr, const int32_t* __rest
     for (int32_t t = b + 1; t < e; ++t) s += store[contrib[t]];
     out[k] = s;
   }
+}
+
+// Many reductions in one launch: CTA b serves job k with jobs[k].blk0 <= b <
+// jobs[k+1].blk0, items (b - blk0) * blockDim.x onwards.  A job with colptr
+// reduces a 1 x n pattern into a dense vector (the rhs), else the nnz values.
+// Each item adds its contributions in slot order, as reduce_k.
+__global__ void reduce_batch_k(const RedJob* __restrict__ jobs, int njobs) {
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].blk0 <= (int64_t)blockIdx.x) lo = mid; else hi = mid - 1;
+  }
+  const RedJob J = jobs[lo];
+  const int64_t k = ((int64_t)blockIdx.x - J.blk0) * blockDim.x + threadIdx.x;
+  if (k >= J.n) return;
+  int64_t slot = k;
+  if (J.colptr) {
+    const int64_t k0 = J.colptr[k], k1 = J.colptr[k + 1];
+    if (k1 == k0) {
+      J.out[k] = 0.0;
+      return;
+    }
+    slot = k0;
+  }
+  const int32_t b = J.cptr[slot], e = J.cptr[slot + 1];
+  double s = J.store[J.contrib[b]];
+  for (int32_t t = b + 1; t < e; ++t) s += J.store[J.contrib[t]];
+  J.out[k] = s;
+}
+
+int reduce_batch(Ctx* c, const RedJob* jobs_dev, int njobs, int64_t blocks) {
+  if (njobs == 0 || blocks == 0) return ELFEL_OK;
+  if (blocks > 0x7fffffff) return fail(c, ELFEL_ERR_ARG, "batched reduction: too many items");
+  reduce_batch_k<<<(unsigned)blocks, kRedJobThreads, 0, c->stream>>>(jobs_dev, njobs);
+  ELFEL_LAUNCH_CHECK(c);
+  return ELFEL_OK;
 }
 
 int reduce_values(Ctx* c, const Pattern& P, const double* store, double* vals_out) {

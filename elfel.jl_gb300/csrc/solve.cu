@@ -39,109 +39,6 @@
 
 namespace elfel {
 
-constexpr int kBlk = 256;
-constexpr int kGraphIters = 16;
-constexpr int kMaxRedBlocks = 2048;  // partial-sum slots per reduction area
-constexpr int kVecOcc = 8;           // register budget of vector kernels: 8 blocks/SM (32 registers)
-constexpr int kGridCap = 152 * kVecOcc;
-constexpr int kVecGridCap = 152 * kVecOcc;  // vector kernels: one full wave (4 blocks/SM measured slower)
-constexpr int kSellOcc = 4;           // FP64 SELL kernels: <= 64 registers, 4 blocks/SM
-// FP32 SELL kernels fit their 8-deep unroll in 40 registers: 6 blocks/SM.
-template <typename T>
-constexpr int sell_occ() { return sizeof(T) == 4 ? 6 : kSellOcc; }
-constexpr int kSigma = 256;          // row-sorting window
-
-// device scalar slots
-enum {
-  S_PQ = 0, S_RZ, S_RR, S_BETA, S_BN2, S_TOL2, S_RMAX, S_DELTA,
-  S_ALPHA,  // rz / pq, computed once by the SpMV's last block
-  S_SCALE,  // FP32 refinement: the FP32 residual is (FP64 residual) / S_SCALE
-  S_BN2S,   // ||b||^2 / S_SCALE^2: the FP32 recurrence's convergence threshold
-  // MINRES
-  S_GAM, S_GAMP, S_GAMN, S_DEL, S_C, S_CP, S_S, S_SP, S_ETA, S_ETA0, S_A1, S_A2, S_A3, S_CN,
-  S_COUNT
-};
-// device int flags
-enum { F_DONE = 0, F_RU, F_ITER, F_MAXIT, F_ROT, F_CONV, F_BRK, F_COUNT };
-
-struct Red4 {
-  double* partials;  // kMaxRedBlocks x 4
-  unsigned* ticket;
-};
-
-// CSR in the original order (rows 0..nu-1): free part (col < nu) and data part.
-struct Csr {
-  int64_t nrows = 0, nnz = 0;
-  DBuf<int32_t> rowptr, col, map;  // map: index into the CSC values
-  DBuf<double> v64;
-  void release(Ctx* c) {
-    rowptr.release(c); col.release(c); map.release(c); v64.release(c);
-    nrows = nnz = 0;
-  }
-};
-
-// SELL-C-sigma matrix of the free-free block (permuted rows and columns).
-struct Sell {
-  int64_t nrows = 0, nslices = 0, nnz_pad = 0;
-  int d16 = 0;
-  DBuf<int64_t> sptr;   // nslices + 1 entry offsets
-  DBuf<int32_t> sw;     // slice widths
-  DBuf<int16_t> dcol;   // d16: column - row (permuted)
-  DBuf<int32_t> col;    // !d16: column (permuted)
-  DBuf<int32_t> map;    // CSC index of each entry, -1 for padding
-  DBuf<int32_t> perm;   // permuted row -> original row
-  DBuf<double> v64;
-  DBuf<float> v32;
-  void release(Ctx* c) {
-    sptr.release(c); sw.release(c); dcol.release(c); col.release(c); map.release(c); perm.release(c);
-    v64.release(c); v32.release(c);
-    nrows = nslices = nnz_pad = 0;
-  }
-};
-
-// POD view passed to kernels.
-struct SellView {
-  int64_t nrows, nslices;
-  const int64_t* sptr;
-  const int32_t* sw;
-  const int16_t* d16;
-  const int32_t* c32;
-};
-
-struct SolverData {
-  int64_t nu = -1;
-  const void* pattern_id = nullptr;
-  int64_t pattern_nnz = -1;
-  int group = 4;  // lanes per row of the CSR kernels (lifting, final residual)
-  Csr ff, fd;
-  Sell A;
-  // original order
-  DBuf<double> T64, bo64, xo64, ro64, dinvo;
-  // permuted order
-  DBuf<double> dinv64, b64, x64, r64, z64, p64, q64, y64;
-  DBuf<float> dinv32, r32, p32, q32, z32, xa32, zz32, b32, x32;
-  DBuf<double> v64[3], w64[3];
-  DBuf<float> v32[3], w32[3];
-  DBuf<double> scal;
-  DBuf<int> flags;
-  DBuf<double> red;  // 3 reduction areas
-  DBuf<unsigned> tickets;
-  cudaGraphExec_t g_pcg64 = nullptr, g_pcg32 = nullptr, g_minres64 = nullptr, g_minres32 = nullptr;
-  SellView view() const {
-    return SellView{A.nrows, A.nslices, A.sptr.p, A.sw.p, A.d16 ? A.dcol.p : nullptr, A.d16 ? nullptr : A.col.p};
-  }
-  void release(Ctx* c) {
-    ff.release(c); fd.release(c); A.release(c);
-    for (DBuf<double>* b : {&T64, &bo64, &xo64, &ro64, &dinvo, &dinv64, &b64, &x64, &r64, &z64, &p64, &q64, &y64})
-      b->release(c);
-    for (DBuf<float>* b : {&dinv32, &r32, &p32, &q32, &z32, &xa32, &zz32, &b32, &x32}) b->release(c);
-    for (int i = 0; i < 3; ++i) { v64[i].release(c); w64[i].release(c); v32[i].release(c); w32[i].release(c); }
-    scal.release(c); flags.release(c); red.release(c); tickets.release(c);
-    for (cudaGraphExec_t* g : {&g_pcg64, &g_pcg32, &g_minres64, &g_minres32})
-      if (*g) { cudaGraphExecDestroy(*g); *g = nullptr; }
-  }
-};
-
 void solver_release(Ctx* c, elfel_sysmat* m) {
   if (m->solver) {
     m->solver->release(c);
@@ -208,25 +105,6 @@ __device__ __forceinline__ bool grid_sums(T (&v)[NV], Red4 red, double (&tot)[NV
 }
 
 // ------------------------------------------------------------------ SELL SpMV
-template <bool D16>
-__device__ __forceinline__ int sell_col(const SellView& A, int64_t k, int64_t row) {
-  if (D16) return (int)row + (int)__ldcs(A.d16 + k);
-  return __ldcs(A.c32 + k);
-}
-
-// The x term of one stored entry.  Plain form: x_c.  Difference form (DIFF):
-// the matrix is stored with its row sums s_i in the diagonal slots, and
-//   y_i = s_i x_i + sum_{j != i} a_ij (x_j - x_i),
-// an identity for any matrix; for slowly varying x the differences are exact
-// (Sterbenz), so in FP32 the near-zero row sums of stiffness matrices do not
-// cancel catastrophically and the smallest eigenvalues are kept.  Padding
-// entries have value 0 and column = row, so they add nothing either way.
-template <typename T, bool DIFF>
-__device__ __forceinline__ T xterm(const T xc, int c, int64_t row, T xi) {
-  if (!DIFF) return xc;
-  return (int64_t)c == row ? xi : xc - xi;
-}
-
 // y = A x over all slices (one warp per slice, lane = row).  Returns the
 // thread's partial of y.w (w = x when wdot is null); with rdot, also adds
 // rdot.x into *part2.
@@ -239,51 +117,9 @@ __device__ __forceinline__ T sell_rows(const SellView& A, const T* __restrict__ 
   const int64_t nwarps = ((int64_t)gridDim.x * kBlk) >> 5;
   T part = 0;
   for (int64_t s = warp; s < A.nslices; s += nwarps) {
-    const int64_t base = A.sptr[s] + lane;
     const int64_t row = s * 32 + lane;
-    const int w = row < A.nrows ? A.sw[s] : 0;  // lanes past the last row stay idle
     const T xi = (DIFF && row < A.nrows) ? x[row] : (T)0;
-    // 8 entries per lane in flight: all column and value loads of a group
-    // are issued before the dependent gathers of x
-    T a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-    int j = 0;
-    for (; j + 7 < w; j += 8) {
-      const int64_t k = base + (int64_t)j * 32;
-      int cc[8];
-      T vv[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) cc[u] = sell_col<D16>(A, k + 32 * u, row);
-#pragma unroll
-      for (int u = 0; u < 8; ++u) vv[u] = __ldcs(v + k + 32 * u);
-      T xx[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) xx[u] = xterm<T, DIFF>(__ldg(x + cc[u]), cc[u], row, xi);
-      a0 += vv[0] * xx[0];
-      a1 += vv[1] * xx[1];
-      a2 += vv[2] * xx[2];
-      a3 += vv[3] * xx[3];
-      a0 += vv[4] * xx[4];
-      a1 += vv[5] * xx[5];
-      a2 += vv[6] * xx[6];
-      a3 += vv[7] * xx[7];
-    }
-    if (j + 3 < w) {
-      const int64_t k = base + (int64_t)j * 32;
-      const int c0 = sell_col<D16>(A, k, row), c1 = sell_col<D16>(A, k + 32, row);
-      const int c2 = sell_col<D16>(A, k + 64, row), c3 = sell_col<D16>(A, k + 96, row);
-      const T v0 = __ldcs(v + k), v1 = __ldcs(v + k + 32), v2 = __ldcs(v + k + 64), v3 = __ldcs(v + k + 96);
-      a0 += v0 * xterm<T, DIFF>(__ldg(x + c0), c0, row, xi);
-      a1 += v1 * xterm<T, DIFF>(__ldg(x + c1), c1, row, xi);
-      a2 += v2 * xterm<T, DIFF>(__ldg(x + c2), c2, row, xi);
-      a3 += v3 * xterm<T, DIFF>(__ldg(x + c3), c3, row, xi);
-      j += 4;
-    }
-    for (; j < w; ++j) {
-      const int64_t k = base + (int64_t)j * 32;
-      const int cj = sell_col<D16>(A, k, row);
-      a0 += __ldcs(v + k) * xterm<T, DIFF>(__ldg(x + cj), cj, row, xi);
-    }
-    const T acc = (a0 + a1) + (a2 + a3);
+    const T acc = sell_row_acc<T, D16, DIFF>(A, v, x, s, lane, xi);
     if (row < A.nrows) {
       y[row] = acc;
       const T xr = x[row];
@@ -333,14 +169,8 @@ __global__ void __launch_bounds__(kBlk, kSellOcc) sell_resid_k(SellView A, const
   const int64_t nwarps = ((int64_t)gridDim.x * kBlk) >> 5;
   double part = 0.0;
   for (int64_t s = warp; s < A.nslices; s += nwarps) {
-    const int64_t base = A.sptr[s] + lane;
     const int64_t row = s * 32 + lane;
-    const int w = row < A.nrows ? A.sw[s] : 0;
-    double acc = 0.0;
-    for (int j = 0; j < w; ++j) {
-      const int64_t k = base + (int64_t)j * 32;
-      acc += __ldcs(v + k) * __ldg(x + sell_col<D16>(A, k, row));
-    }
+    const double acc = sell_row_resid<D16>(A, v, x, s, lane);
     if (row < A.nrows) {
       const double rv = b[row] - acc;
       r[row] = rv;
@@ -949,7 +779,7 @@ static int build_sell(Ctx* c, SolverData* S) {
   return ELFEL_OK;
 }
 
-static int build_solver(elfel_sysmat* m, int64_t nu) {
+int build_solver(elfel_sysmat* m, int64_t nu) {
   Ctx* c = &m->h->c;
   if (!m->solver) m->solver = new SolverData();
   SolverData* S = m->solver;
@@ -1035,7 +865,7 @@ static int build_solver(elfel_sysmat* m, int64_t nu) {
 
 // Values of the solver matrices from the CSC values (FP64, and the FP32 copy).
 // diff32: the FP32 copy is stored in difference form (for the FP32 CG).
-static int refresh_values(elfel_sysmat* m, int abs_diag, int diff32) {
+int refresh_values(elfel_sysmat* m, int abs_diag, int diff32) {
   Ctx* c = &m->h->c;
   SolverData* S = m->solver;
   const int64_t nu = S->nu;
@@ -1147,6 +977,35 @@ static int capture(Ctx* c, cudaGraphExec_t* out, F&& body) {
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return fail(c, ELFEL_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
   return ELFEL_OK;
+}
+
+int lift_rhs(elfel_sysmat* m, const double* Fh, const double* T, int t_dev) {
+  Ctx* c = &m->h->c;
+  SolverData* S = m->solver;
+  const int64_t n = m->nrow, nu = S->nu;
+  ELFEL_CUDA(c, cudaMemcpyAsync(S->T64.p, T, sizeof(double) * n,
+                                t_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream));
+  double* Fd = m->rhs.p;
+  DBuf<double> Ftmp;
+  if (Fh) {
+    ELFEL_TRY(Ftmp.alloc(c, (size_t)n));
+    ELFEL_CUDA(c, cudaMemcpyAsync(Ftmp.p, Fh, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    Fd = Ftmp.p;
+  }
+  ELFEL_TRY(launch_resid(c, S, S->T64.p, S->T64.p + nu, Fd, S->bo64.p, red_area(S, 2), S_BN2));
+  Ftmp.release(c);
+  permute_in_k<<<vec_grid(nu), kBlk, 0, c->stream>>>(nu, S->A.perm.p, S->bo64.p, S->b64.p);
+  ELFEL_LAUNCH_CHECK(c);
+  return ELFEL_OK;
+}
+
+int solution_residual(elfel_sysmat* m) {
+  Ctx* c = &m->h->c;
+  SolverData* S = m->solver;
+  const int64_t nu = S->nu;
+  permute_out_k<<<vec_grid(nu), kBlk, 0, c->stream>>>(nu, S->A.perm.p, S->x64.p, S->xo64.p);
+  ELFEL_LAUNCH_CHECK(c);
+  return launch_resid(c, S, S->xo64.p, nullptr, S->bo64.p, S->ro64.p, red_area(S, 2), S_RR);
 }
 
 // ------------------------------------------------------------------ drivers
@@ -1303,6 +1162,7 @@ extern "C" int elfel_solve(elfel_sysmat* m, const double* Fh, double* T, int64_t
   elfel_solve_stats st;
   memset(&st, 0, sizeof(st));
   if (!m->finished) return fail(c, ELFEL_ERR_STATE, "solve: finish! the matrix first");
+  if (m->busy) return fail(c, ELFEL_ERR_STATE, "solve: the system is held by a batch slot");
   if (m->nrow != m->ncol) return fail(c, ELFEL_ERR_ARG, "solve: K must be square");
   if (nu < 0 || nu > m->nrow || !T) return fail(c, ELFEL_ERR_ARG, "solve: nu outside 0..%lld", (long long)m->nrow);
   if (!Fh && !m->has_rhs) return fail(c, ELFEL_ERR_ARG, "solve: no right-hand side");
@@ -1314,24 +1174,12 @@ extern "C" int elfel_solve(elfel_sysmat* m, const double* Fh, double* T, int64_t
   SolverData* S = m->solver;
   const bool minres = method == ELFEL_MINRES64 || method == ELFEL_MINRES32_IR;
   ELFEL_TRY(refresh_values(m, minres ? 1 : 0, method == ELFEL_PCG32_IR ? 1 : 0));
-  const int64_t n = m->nrow;
   if (nu == 0) {
     if (stats) *stats = st;
     return ELFEL_OK;
   }
-  // lifted right-hand side in the original order: b = F_f - K_ff T_f - K_fd T_d
-  ELFEL_CUDA(c, cudaMemcpyAsync(S->T64.p, T, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
-  double* Fd = m->rhs.p;
-  DBuf<double> Ftmp;
-  if (Fh) {
-    ELFEL_TRY(Ftmp.alloc(c, (size_t)n));
-    ELFEL_CUDA(c, cudaMemcpyAsync(Ftmp.p, Fh, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
-    Fd = Ftmp.p;
-  }
-  ELFEL_TRY(launch_resid(c, S, S->T64.p, S->T64.p + nu, Fd, S->bo64.p, red_area(S, 2), S_BN2));
-  Ftmp.release(c);
-  permute_in_k<<<vec_grid(nu), kBlk, 0, c->stream>>>(nu, S->A.perm.p, S->bo64.p, S->b64.p);
-  ELFEL_LAUNCH_CHECK(c);
+  // lifted right-hand side: b = F_f - K_ff T_f - K_fd T_d
+  ELFEL_TRY(lift_rhs(m, Fh, T, 0));
   double bn2 = 0.0;
   ELFEL_CUDA(c, cudaMemcpyAsync(&bn2, S->scal.p + S_BN2, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -1421,9 +1269,7 @@ extern "C" int elfel_solve(elfel_sysmat* m, const double* Fh, double* T, int64_t
   }
   if (rc != ELFEL_OK) return rc;
   // solution back to the original order; final FP64 residual there
-  permute_out_k<<<vec_grid(nu), kBlk, 0, c->stream>>>(nu, S->A.perm.p, S->x64.p, S->xo64.p);
-  ELFEL_LAUNCH_CHECK(c);
-  ELFEL_TRY(launch_resid(c, S, S->xo64.p, nullptr, S->bo64.p, S->ro64.p, red_area(S, 2), S_RR));
+  ELFEL_TRY(solution_residual(m));
   double rr = 0.0;
   ELFEL_CUDA(c, cudaMemcpyAsync(&rr, S->scal.p + S_RR, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   ELFEL_CUDA(c, cudaMemcpyAsync(T, S->xo64.p, sizeof(double) * nu, cudaMemcpyDeviceToHost, c->stream));

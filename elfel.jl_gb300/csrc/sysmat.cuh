@@ -97,6 +97,21 @@ int build_pattern(Ctx* c, const SlotGen& g, int64_t nrow, int64_t ncol, Pattern*
 
 // vals_out[k] = sum of store[contrib[t]] over t in [cptr[k], cptr[k+1]), in order.
 int reduce_values(Ctx* c, const Pattern& P, const double* store, double* vals_out);
+// Dense vector of a 1 x n pattern (the rhs): out[c] = contributions of column c.
+int reduce_dense(Ctx* c, const Pattern& P, const double* store, double* out);
+
+// One reduction of a batched launch (device array ordered by blk0).
+constexpr int kRedJobThreads = 256;
+struct RedJob {
+  int64_t blk0;            // first CTA of this job
+  int64_t n;               // items: nnz, or columns of a dense rhs
+  const int64_t* colptr;   // dense rhs: the 1 x n pattern's column pointers; else null
+  const int32_t* cptr;
+  const int32_t* contrib;
+  const double* store;
+  double* out;
+};
+int reduce_batch(Ctx* c, const RedJob* jobs_dev, int njobs, int64_t blocks);
 
 // Convert 1-based int64 indices to 0-based int32 with a range check.
 int to_index32(Ctx* c, const int64_t* src_host, int64_t n, int64_t limit, DBuf<int32_t>* dst,
@@ -121,7 +136,10 @@ struct Fused {
   DBuf<double> pmass_store;          // Stokes: pressure mass diagonal per element (nel x 3)
   Pattern pmpat;
   DBuf<double> pmass_diag;           // ndofs (nonzero at pressure DOFs only)
+  int is_block = 0;                  // tables generated on the device from `block`
+  elfel_block_desc block;
   void release(Ctx* c) {
+    is_block = 0;
     conn_u.release(c); conn_p.release(c); xy_u.release(c); dofs_u.release(c); dofs_p.release(c);
     zero_rows.release(c); coef.release(c); kstore.release(c); fstore.release(c);
     fpat.release(c); pmass_store.release(c); pmpat.release(c); pmass_diag.release(c);
@@ -145,4 +163,23 @@ struct elfel_sysmat {
   elfel::Fused F;
   elfel::SolverData* solver = nullptr;
   uint64_t values_version = 0;  // bumped whenever vals change
+  int busy = 0;                 // held by a batch slot (its solver data is in use)
 };
+
+namespace elfel {
+
+// Slot generators, patterns and value buffers of a fused system whose tables
+// (F.conn_u, F.xy_u, F.dofs_u; F.physics, nn, ncomp, nel, tab set) are on the device.
+int fused_build(elfel_sysmat* m, int64_t ndofs);
+
+// Device tables of a block mesh of the rectangle [0,lx] x [0,ly]: nodes,
+// connectivity and the DOFs of a scalar field fixed on the whole boundary
+// (free DOFs numbered first, both in node order).  Sizes out: nel, nnodes, nu.
+int block_tables(Ctx* c, const elfel_block_desc& d, Fused* F, int64_t* nu);
+// T[dof] = Dirichlet polynomial at the data DOFs' nodes, 0 at free DOFs
+// (device vector of ndofs values).
+int block_dirichlet(Ctx* c, const elfel_block_desc& d, const double* coef6, const Fused& F, double* T);
+// The primary space's tables back on the host, 1-based (NULL skips one).
+int tables_to_host(Ctx* c, const Fused& F, int64_t* conn, double* xy, int64_t* eldofs);
+
+}  // namespace elfel

@@ -181,6 +181,38 @@ ELFEL_API int elfel_fused_elasticity(elfel_sysmat* m, double E, double nu, int32
  * F = 0, plus the pressure mass-matrix diagonal kept for preconditioning. */
 ELFEL_API int elfel_fused_stokes(elfel_sysmat* m, double mu);
 
+/* ------------------------------------------------------------------ device block meshes
+ * Mesh generation and DOF numbering on the device for the block meshes the
+ * reference's tests build with MeshSteward (T3block / T6block, e.g.
+ * test/test_heat.jl:28-33), with the whole boundary fixed: the scalar heat
+ * FESpace after setebc! on the boundary nodes and numberdofs!
+ * (src/FESpaces.jl:250-259, 287-291) -- free DOFs 1..nu, then data DOFs,
+ * both in node order -- with no host tables.  Node numbering, element order
+ * and coordinates are those of the host generators (nodes x-fastest; T6 on
+ * the refined grid; coordinates as numpy.linspace). */
+typedef struct {
+  int32_t nodes_per_elem; /* 3 (T3block) or 6 (T6block) */
+  int32_t orientation;    /* 0: cells cut on their (i,j)-(i+1,j+1) diagonal; 1: alternate diagonals */
+  int32_t nx, ny;         /* cells */
+  double lx, ly;          /* the rectangle [0,lx] x [0,ly] */
+  int32_t npts;           /* quadrature rule of the heat integration, as elfel_fused_desc */
+  int32_t reserved;
+  const double* qp_coords;
+  const double* qp_weights;
+} elfel_block_desc;
+/* Fused heat set-up from a device-generated block mesh; *ndofs and *nu (may
+ * be NULL) receive the sizes. */
+ELFEL_API int elfel_fused_setup_block(elfel_sysmat* m, const elfel_block_desc* d, int64_t* ndofs, int64_t* nu);
+/* Dirichlet vector of a block system: T[1:ndofs] = 0 at free DOFs and
+ * c[0] + c[1] x + c[2] y + c[3] x^2 + c[4] x y + c[5] y^2 at the data DOFs. */
+ELFEL_API int elfel_block_dirichlet(elfel_sysmat* m, const double* coef6, double* T);
+/* The tables of a fused system back on the host, 1-based as elfel_fused_desc
+ * takes them: conn[nel x nn], xy[nnodes x 2], eldofs[nel x nedof] of the
+ * primary space; a NULL pointer skips that table. */
+ELFEL_API int elfel_fused_tables(elfel_sysmat* m, int64_t* conn, double* xy, int64_t* eldofs);
+/* Sizes of a fused system: elements, nodes of the primary space, DOFs. */
+ELFEL_API int elfel_fused_dims(elfel_sysmat* m, int64_t* nel, int64_t* nnodes, int64_t* ndofs);
+
 /* ------------------------------------------------------------------ solve */
 enum elfel_solver {
   ELFEL_PCG64 = 0,      /* Jacobi-PCG, all FP64 */
@@ -204,6 +236,104 @@ typedef struct {
  * entries.  F = NULL uses the device right-hand side of the fused assembly. */
 ELFEL_API int elfel_solve(elfel_sysmat* m, const double* F, double* T, int64_t nu, int32_t method,
                 double rtol, int32_t maxit, elfel_solve_stats* stats);
+
+/* ------------------------------------------------------------------ batched solve
+ * No counterpart in the reference (which solves one system at a time with
+ * `\`, test/test_heat.jl:75): many assembled systems iterate together, each
+ * launch covering the row tiles of every active system, as captured CUDA
+ * graphs.  Each system's arithmetic is independent of the others in the
+ * batch, so its result is bit-identical alone and in any mix.  A system held
+ * by a slot (from add until its result is taken) refuses calls that change
+ * it, and its destroy. */
+typedef struct elfel_batch elfel_batch;
+/* method: ELFEL_PCG64 or ELFEL_PCG32_IR; capacity: slots (systems at once). */
+ELFEL_API int elfel_batch_create(elfel_ctx* ctx, int32_t method, int32_t capacity, elfel_batch** out);
+ELFEL_API int elfel_batch_destroy(elfel_batch* b);
+/* Admit system m with the arguments of elfel_solve (T: nrow values, host);
+ * *slot receives its slot. */
+ELFEL_API int elfel_batch_add(elfel_batch* b, elfel_sysmat* m, const double* F, const double* T, int64_t nu,
+                    double rtol, int32_t maxit, int32_t* slot);
+/* Run `graphs` graph launches (a fixed number of iterations each) over all
+ * active systems; *active = systems still iterating afterwards. */
+ELFEL_API int elfel_batch_step(elfel_batch* b, int32_t graphs, int32_t* active);
+/* Slots whose solve has finished and whose result is not yet taken: up to
+ * cap of them in slots[], their count in *n. */
+ELFEL_API int elfel_batch_done(elfel_batch* b, int32_t* slots, int32_t cap, int32_t* n);
+/* Result of a finished slot: T (nrow values, host) gets x in T[1:nu] and the
+ * data values in the rest; stats as elfel_solve (seconds = from add to the
+ * step that saw it finish).  Frees the slot. */
+ELFEL_API int elfel_batch_result(elfel_batch* b, int32_t slot, double* T, elfel_solve_stats* stats);
+
+/* ------------------------------------------------------------------ serving
+ * No counterpart in the reference.  A server takes heat solve requests --
+ * the problem of test/test_heat.jl:89-111 on a T3/T6 block mesh of a
+ * rectangle, with conductivity kappa, source Q and a Dirichlet polynomial on
+ * the whole boundary -- as they arrive, and each elfel_server_step:
+ *   admits queued requests (first come, first served) while a batch slot is
+ *   free and the device-memory budget allows, reusing a resident idle system
+ *   of the same mesh (mesh, pattern and solver structures stay on the device)
+ *   or generating one on the device, evicting idle systems (least recently
+ *   used) for room; assembles all admitted requests in batched launches;
+ *   adds them to the batched solver, where they iterate together with the
+ *   requests already running; runs graphs_per_step graph launches; and
+ *   completes the requests that finished.
+ * Times are seconds on the server clock (elfel_server_clock).  With
+ * batched = 0 the server solves one request at a time through elfel_solve
+ * (the plain path), for comparison. */
+typedef struct elfel_server elfel_server;
+typedef struct {
+  int32_t method;          /* ELFEL_PCG32_IR or ELFEL_PCG64 */
+  int32_t batched;         /* 1: batched solver; 0: one request at a time via elfel_solve */
+  int32_t max_active;      /* requests iterating at once (batch slots) */
+  int32_t graphs_per_step; /* graph launches per step */
+  double rtol;             /* relative residual of every solve */
+  int32_t maxit;
+  int32_t keep_idle;       /* keep finished systems resident for reuse by the same mesh */
+  int64_t mem_budget;      /* device bytes resident systems may hold; 0: the context's budget only */
+} elfel_server_config;
+typedef struct {
+  int32_t nodes_per_elem; /* 3 or 6 */
+  int32_t orientation;    /* as elfel_block_desc */
+  int32_t nx, ny;
+  double lx, ly;
+  double kappa, Q;
+  double dirichlet[6];    /* T = c0 + c1 x + c2 y + c3 x^2 + c4 x y + c5 y^2 on the boundary */
+  double t_arrival;       /* arrival time on the server clock; < 0: now */
+  int32_t keep_solution;  /* keep T (ndofs values) for elfel_server_solution */
+  int32_t reserved;
+} elfel_heat_request;
+typedef struct {
+  int64_t id;
+  int32_t status;         /* ELFEL_OK or the error of this request */
+  int32_t iterations, refinements, converged;
+  double relres;          /* FP64 ||b - K_ff x|| / ||b|| */
+  double t_arrival, t_admit, t_done;
+  int64_t ndofs, nu, nel;
+} elfel_serve_result;
+typedef struct {
+  int64_t submitted, completed, rejected;
+  int64_t systems_created, systems_reused, systems_evicted;
+  int64_t resident_systems, resident_bytes;
+  int64_t graph_launches, solver_kernel_launches, kernel_launches;
+  double busy_seconds;    /* host time spent inside elfel_server_step */
+} elfel_server_stats;
+ELFEL_API int elfel_server_create(elfel_ctx* ctx, const elfel_server_config* cfg, elfel_server** out);
+ELFEL_API int elfel_server_destroy(elfel_server* s);
+ELFEL_API int elfel_server_clock(elfel_server* s, double* t);
+ELFEL_API int elfel_server_submit(elfel_server* s, const elfel_heat_request* r, int64_t* id);
+/* One step of the loop; *active: requests iterating, *queued: waiting. */
+ELFEL_API int elfel_server_step(elfel_server* s, int32_t* active, int32_t* queued);
+/* Completed requests since the last poll (up to cap; *n = how many returned). */
+ELFEL_API int elfel_server_poll(elfel_server* s, elfel_serve_result* out, int32_t cap, int32_t* n);
+/* The kept solution of a completed request (n = its ndofs); frees it. */
+ELFEL_API int elfel_server_solution(elfel_server* s, int64_t id, double* T, int64_t n);
+ELFEL_API int elfel_server_stats_read(elfel_server* s, elfel_server_stats* out);
+
+/* Autotuner records of the context (batched grids, batched assembly CTA
+ * size): line index (0-based) as "key: candidate=ms ..." with the chosen one
+ * starred, and its index in *choice.  ELFEL_ERR_ARG past the last line.  The
+ * tuner is on unless the environment sets ELFEL_TUNE=0. */
+ELFEL_API int elfel_ctx_tuning(const elfel_ctx* ctx, int index, char* line, int cap, int32_t* choice);
 
 #ifdef __cplusplus
 }
