@@ -109,7 +109,9 @@ class ServerStats(ctypes.Structure):
     _fields_ = [(k, ctypes.c_int64) for k in ("submitted", "completed", "rejected", "systems_created",
                                               "systems_reused", "systems_evicted", "resident_systems",
                                               "resident_bytes", "graph_launches", "solver_kernel_launches",
-                                              "kernel_launches")] + [("busy_seconds", ctypes.c_double)]
+                                              "kernel_launches")] + \
+        [(k, ctypes.c_double) for k in ("busy_seconds", "create_seconds", "assemble_seconds", "join_seconds",
+                                        "iterate_seconds", "harvest_seconds")]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -4,17 +4,18 @@
 //
 // Layout.  Each system keeps its own SELL-C-sigma matrix and Krylov vectors
 // (the one-system solver data).  A tile is kBlk consecutive permuted rows of
-// one system (kBlk / 32 SELL slices).  A device tile map lists (slot, tile)
-// for every active system; the three kernels of an iteration loop over it
-// with a fixed grid, so one captured CUDA graph of kIters iterations serves
-// any mix of systems, and systems join or leave between graph launches by
-// rewriting the map.
+// one system (kBlk / 32 SELL slices); a work item is a run of consecutive
+// tiles of one system.  A device item map lists the items of all active
+// systems; the three kernels of an iteration loop over it with a fixed grid,
+// so one captured CUDA graph of kIters iterations serves any mix of systems,
+// and systems join or leave between graph launches by rewriting the map.
 //
 // Reductions are per system and deterministic: each tile writes its partial
-// sums (a fixed tree inside the tile), and the block that finishes a system's
-// last tile adds that system's partials in tile order with a fixed tree.
-// Nothing depends on which other systems share the launch or on the grid size,
-// so a system's iterates are bit-identical alone and in any mix.
+// sums (a fixed tree inside the tile), and the block that completes a
+// system's last work item adds that system's tile partials in tile order
+// with a fixed tree.  Nothing depends on which other systems share the
+// launch, on how tiles are grouped into items or on the grid size, so a
+// system's iterates are bit-identical alone and in any mix.
 //
 // Methods.  ELFEL_PCG64: Jacobi PCG in FP64.  ELFEL_PCG32_IR: Jacobi CG on the
 // FP32 difference-form copy of K with FP64 residual replacement (reliable
@@ -54,49 +55,96 @@ struct BSys {
   double *x64, *r64, *z64, *p64, *q64;
   const double* b64;
   int64_t ntiles;
-  double* part;      // ntiles x 4 partial sums
-  unsigned* ticket;  // tiles finished in the current kernel
-  double* sc;        // B_COUNT scalars
-  int* st;           // I_COUNT ints
+  double* part;        // ntiles x 4 partial sums
+  unsigned* ticket;    // work items finished in the current kernel
+  const int* nitems;   // work items of this system in the current map
+  double* sc;          // B_COUNT scalars
+  int* st;             // I_COUNT ints
 };
 
-// Sum NV per-thread values over the tile (warp stage in T, then FP64), store
-// the tile's partials; in the block that finished the system's last tile,
-// thread 0 returns true with the system totals.
+constexpr int kItemMax = 32;  // tiles per work item (bounds the shared staging)
+constexpr int kWarps = kBlk / 32;
+
+// Warp sums of the warp's NV per-lane values (the warp's slice or rows of
+// tile jt of the item) in the working precision T, staged in shared memory
+// wsum[(jt * 4 + a) * kWarps + warp].  Warps run through the item's tiles
+// independently; the tile partials are formed once per item (item_finish).
 template <int NV, typename T>
-__device__ __forceinline__ bool tile_sums(T (&v)[NV], const BSys& S, int64_t j, double (&tot)[NV]) {
-  __shared__ double sh[NV][kBlk / 32];
-  __shared__ bool last;
+__device__ __forceinline__ void warp_part(T (&v)[NV], double* wsum, int jt) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int a = 0; a < NV; ++a) {
     T x = v[a];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-    if (lane == 0) sh[a][wid] = (double)x;
+    if (lane == 0) wsum[(jt * 4 + a) * kWarps + wid] = (double)x;
   }
+}
+
+// After the tiles first .. first+nt-1 of a work item: tile partials (the
+// warp sums of each tile added in warp order, FP64) into S.part; count the
+// item; in the block that completed the system's last item (target items),
+// thread 0 returns true with the totals over all of the system's tiles (in
+// tile order, fixed tree).
+template <int NV>
+__device__ __forceinline__ bool item_finish(const BSys& S, const double* wsum, int64_t first, int nt, unsigned target,
+                                            double (&tot)[NV]) {
+  __shared__ double sh2[NV][kWarps];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if ((int)threadIdx.x < nt) {
 #pragma unroll
     for (int a = 0; a < NV; ++a) {
       double s = 0.0;
 #pragma unroll
-      for (int w = 0; w < kBlk / 32; ++w) s += sh[a][w];
-      S.part[j * 4 + a] = s;
+      for (int w = 0; w < kWarps; ++w) s += wsum[(threadIdx.x * 4 + a) * kWarps + w];
+      S.part[(first + threadIdx.x) * 4 + a] = s;
     }
-    __threadfence();
-    last = atomicAdd(S.ticket, 1u) == (unsigned)(S.ntiles - 1);
+    __threadfence();  // the tile partials before the count
   }
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(S.ticket, 1u) == target - 1u;
   __syncthreads();
   if (!last) return false;
   __threadfence();
+  // thread t adds tiles t, t + kBlk, ... in order; eight tiles' loads in flight
+  double acc[NV];
+#pragma unroll
+  for (int a = 0; a < NV; ++a) acc[a] = 0.0;
+  const double2* P = reinterpret_cast<const double2*>(S.part);
+  int64_t b = threadIdx.x;
+  for (; b + 7 * kBlk < S.ntiles; b += 8 * kBlk) {
+    double2 lo[8], hi[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      lo[u] = __ldcg(P + (b + u * kBlk) * 2);
+      if (NV > 2) hi[u] = __ldcg(P + (b + u * kBlk) * 2 + 1);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      acc[0] += lo[u].x;
+      if (NV > 1) acc[NV > 1 ? 1 : 0] += lo[u].y;
+      if (NV > 2) acc[NV > 2 ? 2 : 0] += hi[u].x;
+      if (NV > 3) acc[NV > 3 ? 3 : 0] += hi[u].y;
+    }
+  }
+  for (; b < S.ntiles; b += kBlk) {
+    const double2 lo = __ldcg(P + b * 2);
+    acc[0] += lo.x;
+    if (NV > 1) acc[NV > 1 ? 1 : 0] += lo.y;
+    if (NV > 2) {
+      const double2 hi = __ldcg(P + b * 2 + 1);
+      acc[NV > 2 ? 2 : 0] += hi.x;
+      if (NV > 3) acc[NV > 3 ? 3 : 0] += hi.y;
+    }
+  }
 #pragma unroll
   for (int a = 0; a < NV; ++a) {
-    double s = 0.0;
-    for (int64_t b = threadIdx.x; b < S.ntiles; b += kBlk) s += __ldcg(S.part + b * 4 + a);
+    double s = acc[a];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if (lane == 0) sh[a][wid] = s;
+    if (lane == 0) sh2[a][wid] = s;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -104,7 +152,7 @@ __device__ __forceinline__ bool tile_sums(T (&v)[NV], const BSys& S, int64_t j, 
     for (int a = 0; a < NV; ++a) {
       double s = 0.0;
 #pragma unroll
-      for (int w = 0; w < kBlk / 32; ++w) s += sh[a][w];
+      for (int w = 0; w < kBlk / 32; ++w) s += sh2[a][w];
       tot[a] = s;
     }
     *S.ticket = 0u;
@@ -114,54 +162,102 @@ __device__ __forceinline__ bool tile_sums(T (&v)[NV], const BSys& S, int64_t j, 
 }
 
 // ------------------------------------------------------------------ kernels
+// Programmatic dependent launch: the iteration kernels are captured with
+// programmatic stream serialization, so the next kernel is scheduled while
+// this one runs; it stages its first work item and system descriptor, then
+// waits (griddepcontrol.wait) until this grid has completed and its writes
+// are visible.  Without the launch attribute both instructions are no-ops.
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// Copy a system descriptor into shared memory (one 8-byte word per thread).
+__device__ __forceinline__ void stage_sys(const BSys* __restrict__ src, BSys* dst) {
+  static_assert(sizeof(BSys) % 8 == 0 && sizeof(BSys) / 8 <= kBlk, "descriptor staging");
+  if (threadIdx.x < sizeof(BSys) / 8)
+    reinterpret_cast<uint64_t*>(dst)[threadIdx.x] = __ldg(reinterpret_cast<const uint64_t*>(src) + threadIdx.x);
+  __syncthreads();
+}
+
+// body(it, S) for each work item it = (slot, first tile, tiles) of this
+// block, S its system's descriptor staged in shared memory.  The first
+// item's descriptor is staged before the wait on the previous kernel (the
+// item map and the descriptors are written before the graph runs).
+template <typename F>
+__device__ __forceinline__ void for_items(const BSys* __restrict__ sys, const int4* __restrict__ items,
+                                          const int* __restrict__ ntot, F&& body) {
+  __shared__ BSys S;
+  pdl_launch_dependents();
+  const int total = *ntot;
+  int t = blockIdx.x;
+  int4 it = make_int4(0, 0, 0, 0);
+  if (t < total) {
+    it = items[t];
+    stage_sys(sys + it.x, &S);
+  }
+  pdl_wait();
+  while (t < total) {
+    body(it, (const BSys&)S);
+    t += gridDim.x;
+    if (t >= total) break;
+    it = items[t];
+    __syncthreads();  // every thread is done with the previous descriptor
+    stage_sys(sys + it.x, &S);
+  }
+}
+
 // spmv slot: CG step length, or the FP64 residual of a replacement.
 template <bool IR>
-__global__ void __launch_bounds__(kBlk) b_spmv_k(const BSys* __restrict__ sys, const int2* __restrict__ tmap,
-                                                 const int* __restrict__ ntot) {
-  const int total = *ntot;
+__global__ void __launch_bounds__(kBlk, 5) b_spmv_k(const BSys* __restrict__ sys, const int4* __restrict__ items,
+                                                 const int* __restrict__ nitems_total) {
+  __shared__ double wsum[kItemMax * 4 * kWarps];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int t = blockIdx.x; t < total; t += gridDim.x) {
-    const int2 e = tmap[t];
-    const BSys& S = sys[e.x];
-    const int64_t j = e.y;
+  for_items(sys, items, nitems_total, [&](const int4& it, const BSys& S) {
     const int mode = S.st[I_MODE];
-    const int64_t s = j * (kBlk / 32) + wid;
-    const int64_t row = s * 32 + lane;
-    const bool in = s < S.A.nslices && row < S.A.nrows;
     if (IR) {
       if (mode == M_CG || mode == M_STARTED) {
-        float pq = 0.f, rp = 0.f;
-        if (s < S.A.nslices) {
-          const float xi = in ? S.p32[row] : 0.f;
-          const float acc = S.A.d16 ? sell_row_acc<float, true, true>(S.A, S.v32, S.p32, s, lane, xi)
-                                    : sell_row_acc<float, false, true>(S.A, S.v32, S.p32, s, lane, xi);
-          if (in) {
-            S.q32[row] = acc;
-            pq = acc * xi;
-            rp = S.r32[row] * xi;
+        for (int64_t j = it.y; j < it.y + it.z; ++j) {
+          const int64_t s = j * (kBlk / 32) + wid;
+          const int64_t row = s * 32 + lane;
+          float pq = 0.f, rp = 0.f;
+          if (s < S.A.nslices) {
+            const bool in = row < S.A.nrows;
+            const float xi = in ? S.p32[row] : 0.f;
+            const float acc = S.A.d16 ? sell_row_acc<float, true, true>(S.A, S.v32, S.p32, s, lane, xi)
+                                      : sell_row_acc<float, false, true>(S.A, S.v32, S.p32, s, lane, xi);
+            if (in) {
+              S.q32[row] = acc;
+              pq = acc * xi;
+              rp = S.r32[row] * xi;
+            }
           }
+          float v[2] = {pq, rp};
+          warp_part<2>(v, wsum, (int)(j - it.y));
         }
-        float v[2] = {pq, rp};
         double tot[2];
-        if (tile_sums<2>(v, S, j, tot)) {
+        if (item_finish<2>(S, wsum, it.y, it.z, (unsigned)*S.nitems, tot)) {
           S.sc[B_PQ] = tot[0];
           S.sc[B_ALPHA] = (tot[0] > 0.0 && isfinite(tot[0])) ? tot[1] / tot[0] : 0.0;
           if (mode == M_STARTED) S.st[I_MODE] = M_CG;
         }
       } else if (mode == M_FOLD) {
-        double rr = 0.0;
-        if (s < S.A.nslices) {
-          const double acc = S.A.d16 ? sell_row_resid<true>(S.A, S.v64, S.x64, s, lane)
-                                     : sell_row_resid<false>(S.A, S.v64, S.x64, s, lane);
-          if (in) {
-            const double rv = S.b64[row] - acc;
-            S.r64[row] = rv;
-            rr = rv * rv;
+        for (int64_t j = it.y; j < it.y + it.z; ++j) {
+          const int64_t s = j * (kBlk / 32) + wid;
+          const int64_t row = s * 32 + lane;
+          double rr = 0.0;
+          if (s < S.A.nslices) {
+            const double acc = S.A.d16 ? sell_row_resid<true>(S.A, S.v64, S.x64, s, lane)
+                                       : sell_row_resid<false>(S.A, S.v64, S.x64, s, lane);
+            if (row < S.A.nrows) {
+              const double rv = S.b64[row] - acc;
+              S.r64[row] = rv;
+              rr = rv * rv;
+            }
           }
+          double v[1] = {rr};
+          warp_part<1>(v, wsum, (int)(j - it.y));
         }
-        double v[1] = {rr};
         double tot[1];
-        if (tile_sums<1>(v, S, j, tot)) {
+        if (item_finish<1>(S, wsum, it.y, it.z, (unsigned)*S.nitems, tot)) {
           const double rrt = tot[0];
           S.sc[B_RRT] = rrt;
           S.st[I_REPL] += 1;
@@ -181,63 +277,67 @@ __global__ void __launch_bounds__(kBlk) b_spmv_k(const BSys* __restrict__ sys, c
         }
       }
     } else if (mode == M_CG) {
-      double pq = 0.0;
-      if (s < S.A.nslices) {
-        const double acc = S.A.d16 ? sell_row_acc<double, true, false>(S.A, S.v64, S.p64, s, lane, 0.0)
-                                   : sell_row_acc<double, false, false>(S.A, S.v64, S.p64, s, lane, 0.0);
-        if (in) {
-          S.q64[row] = acc;
-          pq = acc * S.p64[row];
+      for (int64_t j = it.y; j < it.y + it.z; ++j) {
+        const int64_t s = j * (kBlk / 32) + wid;
+        const int64_t row = s * 32 + lane;
+        double pq = 0.0;
+        if (s < S.A.nslices) {
+          const double acc = S.A.d16 ? sell_row_acc<double, true, false>(S.A, S.v64, S.p64, s, lane, 0.0)
+                                     : sell_row_acc<double, false, false>(S.A, S.v64, S.p64, s, lane, 0.0);
+          if (row < S.A.nrows) {
+            S.q64[row] = acc;
+            pq = acc * S.p64[row];
+          }
         }
+        double v[1] = {pq};
+        warp_part<1>(v, wsum, (int)(j - it.y));
       }
-      double v[1] = {pq};
       double tot[1];
-      if (tile_sums<1>(v, S, j, tot)) {
+      if (item_finish<1>(S, wsum, it.y, it.z, (unsigned)*S.nitems, tot)) {
         S.sc[B_PQ] = tot[0];
         S.sc[B_ALPHA] = (tot[0] > 0.0 && isfinite(tot[0])) ? S.sc[B_RZ] / tot[0] : 0.0;
       }
     }
-  }
+  });
 }
 
 // update slot: x, r, z and beta; or the restart after a replacement.
 template <bool IR>
-__global__ void __launch_bounds__(kBlk) b_update_k(const BSys* __restrict__ sys, const int2* __restrict__ tmap,
-                                                   const int* __restrict__ ntot) {
-  const int total = *ntot;
-  for (int t = blockIdx.x; t < total; t += gridDim.x) {
-    const int2 e = tmap[t];
-    const BSys& S = sys[e.x];
-    const int64_t j = e.y;
+__global__ void __launch_bounds__(kBlk) b_update_k(const BSys* __restrict__ sys, const int4* __restrict__ items,
+                                                   const int* __restrict__ nitems_total) {
+  __shared__ double wsum[kItemMax * 4 * kWarps];
+  for_items(sys, items, nitems_total, [&](const int4& it, const BSys& S) {
     const int mode = S.st[I_MODE];
-    const int64_t row = j * kBlk + threadIdx.x;
-    const bool in = row < S.A.nrows;
     if (IR) {
       if (mode == M_CG) {
         const double pq = S.sc[B_PQ];
         const bool brk = !(pq > 0.0) || !isfinite(pq);
         const float alpha = brk ? 0.f : (float)S.sc[B_ALPHA];
-        float prz = 0.f, prr = 0.f, pzo = 0.f;
-        if (in) {
-          const float pi = S.p32[row];
-          S.x32[row] += alpha * pi;
-          const float ro = S.r32[row];
-          const float ri = ro - alpha * S.q32[row];
-          S.r32[row] = ri;
-          const float zi = S.dinv32[row] * ri;
-          S.z32[row] = zi;
-          prz = ri * zi;
-          prr = ri * ri;
-          pzo = zi * ro;
+        for (int64_t j = it.y; j < it.y + it.z; ++j) {
+          const int64_t row = j * kBlk + threadIdx.x;
+          float prz = 0.f, prr = 0.f, pzo = 0.f;
+          if (row < S.A.nrows) {
+            const float pi = S.p32[row];
+            S.x32[row] += alpha * pi;
+            const float ro = S.r32[row];
+            const float ri = ro - alpha * S.q32[row];
+            S.r32[row] = ri;
+            const float zi = S.dinv32[row] * ri;
+            S.z32[row] = zi;
+            prz = ri * zi;
+            prr = ri * ri;
+            pzo = zi * ro;
+          }
+          float v[3] = {prz, prr, pzo};
+          warp_part<3>(v, wsum, (int)(j - it.y));
         }
-        float v[3] = {prz, prr, pzo};
         double tot[3];
-        if (tile_sums<3>(v, S, j, tot)) {
+        if (item_finish<3>(S, wsum, it.y, it.z, (unsigned)*S.nitems, tot)) {
           const double rz = tot[0], rr = tot[1];
           S.sc[B_BETA] = (rz - tot[2]) / S.sc[B_RZ];
           S.sc[B_RZ] = rz;
           S.sc[B_RR] = rr;
-          const int it = ++S.st[I_ITER];
+          const int itn = ++S.st[I_ITER];
           // the recurrence works on r / s with s = ||b||: converged at rtol^2
           const bool conv = rr <= S.sc[B_TOL2];
           const bool bad = brk || !isfinite(rz) || !isfinite(rr);
@@ -249,7 +349,7 @@ __global__ void __launch_bounds__(kBlk) b_update_k(const BSys* __restrict__ sys,
             const double rn = sqrt(rr);
             if (rn > S.sc[B_RMAX]) S.sc[B_RMAX] = rn;
             if (conv) S.st[I_BRK] = 2;  // spent directions: restart from p = z
-            ru = conv || it >= S.st[I_MAXIT] || rn < S.sc[B_DELTA] * S.sc[B_RMAX];
+            ru = conv || itn >= S.st[I_MAXIT] || rn < S.sc[B_DELTA] * S.sc[B_RMAX];
           }
           if (ru) {
             const double sc2 = S.sc[B_SCALE] * S.sc[B_SCALE];
@@ -260,18 +360,22 @@ __global__ void __launch_bounds__(kBlk) b_update_k(const BSys* __restrict__ sys,
       } else if (mode == M_RESTART) {
         const double inv = 1.0 / S.sc[B_SCALE];
         const int restart = S.st[I_RESTART];
-        float prz = 0.f;
-        if (in) {
-          const float ri = (float)(S.r64[row] * inv);
-          S.r32[row] = ri;
-          const float zi = S.dinv32[row] * ri;
-          S.z32[row] = zi;
-          if (restart) S.p32[row] = zi;
-          prz = ri * zi;
+        for (int64_t j = it.y; j < it.y + it.z; ++j) {
+          const int64_t row = j * kBlk + threadIdx.x;
+          float prz = 0.f;
+          if (row < S.A.nrows) {
+            const float ri = (float)(S.r64[row] * inv);
+            S.r32[row] = ri;
+            const float zi = S.dinv32[row] * ri;
+            S.z32[row] = zi;
+            if (restart) S.p32[row] = zi;
+            prz = ri * zi;
+          }
+          float v[1] = {prz};
+          warp_part<1>(v, wsum, (int)(j - it.y));
         }
-        float v[1] = {prz};
         double tot[1];
-        if (tile_sums<1>(v, S, j, tot)) {
+        if (item_finish<1>(S, wsum, it.y, it.z, (unsigned)*S.nitems, tot)) {
           S.sc[B_RZ] = tot[0];
           S.sc[B_RMAX] = sqrt(S.sc[B_RRT]) / S.sc[B_SCALE];
           S.st[I_MODE] = M_STARTED;
@@ -281,72 +385,77 @@ __global__ void __launch_bounds__(kBlk) b_update_k(const BSys* __restrict__ sys,
       const double pq = S.sc[B_PQ];
       const bool brk = !(pq > 0.0) || !isfinite(pq);
       const double alpha = brk ? 0.0 : S.sc[B_ALPHA];
-      double prz = 0.0, prr = 0.0;
-      if (in) {
-        S.x64[row] += alpha * S.p64[row];
-        const double ri = S.r64[row] - alpha * S.q64[row];
-        S.r64[row] = ri;
-        const double zi = S.dinv64[row] * ri;
-        S.z64[row] = zi;
-        prz = ri * zi;
-        prr = ri * ri;
+      for (int64_t j = it.y; j < it.y + it.z; ++j) {
+        const int64_t row = j * kBlk + threadIdx.x;
+        double prz = 0.0, prr = 0.0;
+        if (row < S.A.nrows) {
+          S.x64[row] += alpha * S.p64[row];
+          const double ri = S.r64[row] - alpha * S.q64[row];
+          S.r64[row] = ri;
+          const double zi = S.dinv64[row] * ri;
+          S.z64[row] = zi;
+          prz = ri * zi;
+          prr = ri * ri;
+        }
+        double v[2] = {prz, prr};
+        warp_part<2>(v, wsum, (int)(j - it.y));
       }
-      double v[2] = {prz, prr};
       double tot[2];
-      if (tile_sums<2>(v, S, j, tot)) {
+      if (item_finish<2>(S, wsum, it.y, it.z, (unsigned)*S.nitems, tot)) {
         const double rz = tot[0], rr = tot[1];
         S.sc[B_BETA] = rz / S.sc[B_RZ];
         S.sc[B_RZ] = rz;
         S.sc[B_RR] = rr;
-        const int it = ++S.st[I_ITER];
+        const int itn = ++S.st[I_ITER];
         const bool conv = rr <= S.sc[B_TOL2] * S.sc[B_BN2];
         const bool bad = brk || !isfinite(rz) || !isfinite(rr);
-        if (conv || bad || it >= S.st[I_MAXIT]) {
+        if (conv || bad || itn >= S.st[I_MAXIT]) {
           S.st[I_CONV] = (conv && !bad) ? 1 : 0;
           S.st[I_MODE] = M_DONE;
         }
       }
     }
-  }
+  });
 }
 
 // p slot: p = z + beta p; in M_FOLD also x64 += s x32, x32 = 0.
 template <bool IR>
-__global__ void __launch_bounds__(kBlk) b_p_k(const BSys* __restrict__ sys, const int2* __restrict__ tmap,
-                                              const int* __restrict__ ntot) {
-  const int total = *ntot;
-  for (int t = blockIdx.x; t < total; t += gridDim.x) {
-    const int2 e = tmap[t];
-    const BSys& S = sys[e.x];
+__global__ void __launch_bounds__(kBlk) b_p_k(const BSys* __restrict__ sys, const int4* __restrict__ items,
+                                              const int* __restrict__ nitems_total) {
+  for_items(sys, items, nitems_total, [&](const int4& it, const BSys& S) {
     const int mode = S.st[I_MODE];
-    const int64_t row = (int64_t)e.y * kBlk + threadIdx.x;
-    if (row >= S.A.nrows) continue;
     if (IR) {
-      if (mode != M_CG && mode != M_FOLD) continue;
+      if (mode != M_CG && mode != M_FOLD) return;
       const float beta = (float)S.sc[B_BETA];
-      S.p32[row] = S.z32[row] + beta * S.p32[row];
-      if (mode == M_FOLD) {
-        S.x64[row] += S.sc[B_SCALE] * (double)S.x32[row];
-        S.x32[row] = 0.f;
+      const double s = S.sc[B_SCALE];
+      for (int64_t row = (int64_t)it.y * kBlk + threadIdx.x; row < (int64_t)(it.y + it.z) * kBlk && row < S.A.nrows;
+           row += kBlk) {
+        S.p32[row] = S.z32[row] + beta * S.p32[row];
+        if (mode == M_FOLD) {
+          S.x64[row] += s * (double)S.x32[row];
+          S.x32[row] = 0.f;
+        }
       }
     } else if (mode == M_CG) {
       const double beta = S.sc[B_BETA];
-      S.p64[row] = S.z64[row] + beta * S.p64[row];
+      for (int64_t row = (int64_t)it.y * kBlk + threadIdx.x; row < (int64_t)(it.y + it.z) * kBlk && row < S.A.nrows;
+           row += kBlk)
+        S.p64[row] = S.z64[row] + beta * S.p64[row];
     }
-  }
+  });
 }
 
-// Start of one system (its own launch, before it joins the tile map): x = 0,
+// Start of one system (its own launch, before it joins the item map): x = 0,
 // r = b (scaled by s = ||b|| for the FP32 recurrence), z = D r, p = z, r.z.
+// Each tile is its own work item here.
 template <bool IR>
 __global__ void __launch_bounds__(kBlk) b_init_k(const BSys* __restrict__ sysp, const double* __restrict__ bn2p) {
+  __shared__ double wsum[4 * kWarps];
   const BSys& S = *sysp;
   const double bn2 = *bn2p;
   for (int64_t j = blockIdx.x; j < S.ntiles; j += gridDim.x) {
     const int64_t row = j * kBlk + threadIdx.x;
     const bool in = row < S.A.nrows;
-    double tot[1];
-    bool fin;
     if (IR) {
       const double inv = bn2 > 0.0 ? 1.0 / sqrt(bn2) : 0.0;
       float prz = 0.f;
@@ -361,7 +470,7 @@ __global__ void __launch_bounds__(kBlk) b_init_k(const BSys* __restrict__ sysp, 
         prz = ri * zi;
       }
       float v[1] = {prz};
-      fin = tile_sums<1>(v, S, j, tot);
+      warp_part<1>(v, wsum, 0);
     } else {
       double prz = 0.0;
       if (in) {
@@ -374,9 +483,10 @@ __global__ void __launch_bounds__(kBlk) b_init_k(const BSys* __restrict__ sysp, 
         prz = ri * zi;
       }
       double v[1] = {prz};
-      fin = tile_sums<1>(v, S, j, tot);
+      warp_part<1>(v, wsum, 0);
     }
-    if (fin) {
+    double tot[1];
+    if (item_finish<1>(S, wsum, j, 1, (unsigned)S.ntiles, tot)) {
       S.sc[B_RZ] = tot[0];
       S.sc[B_BN2] = bn2;
       S.sc[B_SCALE] = bn2 > 0.0 ? sqrt(bn2) : 1.0;
@@ -387,18 +497,23 @@ __global__ void __launch_bounds__(kBlk) b_init_k(const BSys* __restrict__ sysp, 
   }
 }
 
-// tile map: entry t of active system k (off[k] <= t < off[k+1]) = (slot[k], t - off[k])
-__global__ void b_map_k(const int* __restrict__ off, const int* __restrict__ slot, int nact, int2* __restrict__ tmap,
-                        int* __restrict__ ntot) {
+// Item map: active system k owns items off[k] .. off[k+1]-1, each of up to
+// item_tiles consecutive tiles; item t = (slot, first tile, tiles).
+__global__ void b_map_k(const int* __restrict__ off, const int* __restrict__ slot, const int* __restrict__ ntl,
+                        int nact, int item_tiles, int4* __restrict__ items, int* __restrict__ ntot,
+                        int* __restrict__ nitems) {
   const int total = off[nact];
-  if (blockIdx.x == 0 && threadIdx.x == 0) *ntot = total;
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid == 0) *ntot = total;
+  if (tid < nact) nitems[slot[tid]] = off[tid + 1] - off[tid];
+  for (int t = tid; t < total; t += gridDim.x * blockDim.x) {
     int lo = 0, hi = nact - 1;
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
       if (off[mid] <= t) lo = mid; else hi = mid - 1;
     }
-    tmap[t] = make_int2(slot[lo], t - off[lo]);
+    const int t0 = (t - off[lo]) * item_tiles;
+    items[t] = make_int4(slot[lo], t0, min(item_tiles, ntl[lo] - t0), 0);
   }
 }
 
@@ -434,18 +549,18 @@ struct elfel_batch {
   DBuf<double> sc;
   DBuf<int> st;
   DBuf<unsigned> tickets;
-  DBuf<int2> tmap;
-  int64_t tmap_cap = 0;
+  DBuf<int> nitems;  // work items per slot in the current map
+  DBuf<int4> items;
+  int64_t items_cap = 0;
   DBuf<int> ntot;
-  DBuf<int> act;  // off[cap + 1], slot[cap]
-  int64_t total_tiles = 0;
+  DBuf<int> act;  // off[cap + 1], slot[cap], ntiles[cap]
+  int64_t total_tiles = 0, total_items = 0;
   bool map_dirty = false;
   std::vector<int> hst;
   std::vector<int> done;
-  // captured graphs per grid configuration, valid for the current tile-map buffer
+  // captured graphs per grid configuration, valid for the current item-map buffer
   std::vector<GridCfg> cfgs;
   std::vector<cudaGraphExec_t> graphs;
-  int cfg = 0;
   int occ_spmv = 1, occ_vec = 1;
   std::map<int, int> tuned;  // log2(tiles) bucket -> chosen configuration
   int64_t launches = 0, kernel_launches = 0;
@@ -463,12 +578,28 @@ void drop_graphs(elfel_batch* b) {
     }
 }
 
+// Launch with programmatic stream serialization (see pdl_wait).
+void launch_pdl(void (*k)(const BSys*, const int4*, const int*), unsigned grid, cudaStream_t s, const BSys* sys,
+                const int4* items, const int* ntot) {
+  cudaLaunchConfig_t cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kBlk);
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k, sys, items, ntot);
+}
+
 template <bool IR>
 void launch_iteration(cudaStream_t s, elfel_batch* b, const GridCfg& g, int sms) {
   const unsigned g1 = (unsigned)(sms * g.spmv), g2 = (unsigned)(sms * g.vec);
-  b_spmv_k<IR><<<g1, kBlk, 0, s>>>(b->sys.p, b->tmap.p, b->ntot.p);
-  b_update_k<IR><<<g2, kBlk, 0, s>>>(b->sys.p, b->tmap.p, b->ntot.p);
-  b_p_k<IR><<<g2, kBlk, 0, s>>>(b->sys.p, b->tmap.p, b->ntot.p);
+  launch_pdl(b_spmv_k<IR>, g1, s, b->sys.p, b->items.p, b->ntot.p);
+  launch_pdl(b_update_k<IR>, g2, s, b->sys.p, b->items.p, b->ntot.p);
+  launch_pdl(b_p_k<IR>, g2, s, b->sys.p, b->items.p, b->ntot.p);
 }
 
 int graph_for(elfel_batch* b, int k, cudaGraphExec_t* out) {
@@ -490,31 +621,45 @@ int graph_for(elfel_batch* b, int k, cudaGraphExec_t* out) {
   return ELFEL_OK;
 }
 
-// Rebuild the device tile map from the active slots (in slot order).
+// Rebuild the device item map from the active slots (in slot order).  Items
+// hold item_tiles tiles, sized so that the map has about two items per
+// resident block: few completion counts per system, balanced blocks.
 int rebuild_map(elfel_batch* b) {
   Ctx* c = ctx_of(b);
-  std::vector<int> off(1, 0), sl;
+  std::vector<int> sl, ntl;
+  int64_t tiles = 0;
   for (int i = 0; i < b->cap; ++i)
     if (b->slots[i].state == 1) {
       sl.push_back(i);
-      off.push_back(off.back() + (int)b->slots[i].ntiles);
+      ntl.push_back((int)b->slots[i].ntiles);
+      tiles += b->slots[i].ntiles;
     }
   const int nact = (int)sl.size();
-  b->total_tiles = off.back();
-  if (b->total_tiles > b->tmap_cap) {
-    int64_t cap = std::max<int64_t>(b->tmap_cap * 2, 1024);
-    while (cap < b->total_tiles) cap *= 2;
-    b->tmap.release(c);
-    ELFEL_TRY(b->tmap.alloc(c, (size_t)cap));
-    b->tmap_cap = cap;
+  const int64_t target = 2LL * c->sm_count * std::max(b->occ_spmv, b->occ_vec);
+  const int item_tiles = (int)std::min<int64_t>(kItemMax, std::max<int64_t>(1, tiles / std::max<int64_t>(target, 1)));
+  std::vector<int> h(3 * (size_t)b->cap + 1, 0);
+  int64_t nit = 0;
+  for (int k = 0; k < nact; ++k) {
+    h[k] = (int)nit;
+    nit += (ntl[k] + item_tiles - 1) / item_tiles;
+    h[b->cap + 1 + k] = sl[k];
+    h[2 * b->cap + 1 + k] = ntl[k];
+  }
+  h[nact] = (int)nit;
+  b->total_tiles = tiles;
+  b->total_items = nit;
+  if (nit > b->items_cap) {
+    int64_t cap = std::max<int64_t>(b->items_cap * 2, 1024);
+    while (cap < nit) cap *= 2;
+    b->items.release(c);
+    ELFEL_TRY(b->items.alloc(c, (size_t)cap));
+    b->items_cap = cap;
     drop_graphs(b);  // graphs hold the old buffer
   }
-  std::vector<int> h(2 * (size_t)b->cap + 1, 0);
-  for (int k = 0; k <= nact; ++k) h[k] = off[k];
-  for (int k = 0; k < nact; ++k) h[b->cap + 1 + k] = sl[k];
   ELFEL_CUDA(c, cudaMemcpyAsync(b->act.p, h.data(), sizeof(int) * h.size(), cudaMemcpyHostToDevice, c->stream));
-  b_map_k<<<grid_for(std::max<int64_t>(b->total_tiles, 1), 256, (int64_t)c->sm_count * 8), 256, 0, c->stream>>>(
-      b->act.p, b->act.p + b->cap + 1, nact, b->tmap.p, b->ntot.p);
+  b_map_k<<<grid_for(std::max<int64_t>(std::max<int64_t>(nit, nact), 1), 256, (int64_t)c->sm_count * 8), 256, 0,
+            c->stream>>>(b->act.p, b->act.p + b->cap + 1, b->act.p + 2 * b->cap + 1, nact, item_tiles, b->items.p,
+                         b->ntot.p, b->nitems.p);
   ELFEL_LAUNCH_CHECK(c);
   b->map_dirty = false;
   return ELFEL_OK;
@@ -649,6 +794,7 @@ int batch_add_dev(elfel_batch* b, elfel_sysmat* m, const double* F, const double
   d.ntiles = s.ntiles;
   d.part = s.part.p;
   d.ticket = b->tickets.p + k;
+  d.nitems = b->nitems.p + k;
   d.sc = b->sc.p + (size_t)k * B_COUNT;
   d.st = b->st.p + (size_t)k * I_COUNT;
   double hsc[B_COUNT] = {0};
@@ -717,8 +863,8 @@ int batch_step(elfel_batch* b, int32_t graphs, int32_t* active) {
   for (const Slot& s : b->slots) n += s.state == 1;
   if (active) *active = n;
   if (c->trace)
-    fprintf(stderr, "[elfel batch] step: %d active, %lld tiles, %zu finished waiting\n", n,
-            (long long)b->total_tiles, b->done.size());
+    fprintf(stderr, "[elfel batch] step: %d active, %lld tiles in %lld items, %zu finished waiting\n", n,
+            (long long)b->total_tiles, (long long)b->total_items, b->done.size());
   return ELFEL_OK;
 }
 
@@ -788,12 +934,14 @@ extern "C" int elfel_batch_create(elfel_ctx* h, int32_t method, int32_t capacity
   int rc = ELFEL_OK;
   if ((rc = b->sys.alloc(c, (size_t)capacity)) || (rc = b->sc.alloc(c, (size_t)capacity * B_COUNT)) ||
       (rc = b->st.alloc(c, (size_t)capacity * I_COUNT)) || (rc = b->tickets.alloc(c, (size_t)capacity)) ||
-      (rc = b->ntot.alloc(c, 1)) || (rc = b->act.alloc(c, 2 * (size_t)capacity + 1))) {
+      (rc = b->nitems.alloc(c, (size_t)capacity)) || (rc = b->ntot.alloc(c, 1)) ||
+      (rc = b->act.alloc(c, 3 * (size_t)capacity + 1))) {
     delete b;
     return rc;
   }
   cudaMemsetAsync(b->st.p, 0, sizeof(int) * capacity * I_COUNT, c->stream);
   cudaMemsetAsync(b->tickets.p, 0, sizeof(unsigned) * capacity, c->stream);
+  cudaMemsetAsync(b->nitems.p, 0, sizeof(int) * capacity, c->stream);
   cudaMemsetAsync(b->ntot.p, 0, sizeof(int), c->stream);
   // resident blocks per SM of the kernels: the grid configurations tried
   int o1 = 1, o2 = 1;
@@ -832,7 +980,8 @@ extern "C" int elfel_batch_destroy(elfel_batch* b) {
   b->sc.release(c);
   b->st.release(c);
   b->tickets.release(c);
-  b->tmap.release(c);
+  b->nitems.release(c);
+  b->items.release(c);
   b->ntot.release(c);
   b->act.release(c);
   delete b;

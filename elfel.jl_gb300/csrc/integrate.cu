@@ -275,6 +275,8 @@ int launch_heat(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* 
 
 template <int NN, int NT>
 static void heat_batch_launch(Ctx* c, const HeatJob* jobs, int njobs, int64_t blocks, const QPTab& tab) {
+  // T6 with 256-thread CTAs stages more than the default 48 KB of dynamic shared memory
+  cudaFuncSetAttribute(heat_batch_k<NN, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)heat_smem(NN, NT));
   heat_batch_k<NN, NT><<<(unsigned)blocks, NT, heat_smem(NN, NT), c->stream>>>(jobs, njobs, tab);
 }
 

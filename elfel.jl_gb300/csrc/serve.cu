@@ -121,6 +121,14 @@ namespace {
 
 double now_s(const elfel_server* s) { return std::chrono::duration<double>(Clock::now() - s->t0).count(); }
 
+// Adds the host time of a scope to a counter.
+struct Timed {
+  double& acc;
+  Clock::time_point a = Clock::now();
+  explicit Timed(double& t) : acc(t) {}
+  ~Timed() { acc += std::chrono::duration<double>(Clock::now() - a).count(); }
+};
+
 Key key_of(const elfel_heat_request& r) { return Key{r.nodes_per_elem, r.orientation, r.nx, r.ny, r.lx, r.ly}; }
 
 int64_t estimate(elfel_server* s, const Key& k) {
@@ -163,6 +171,7 @@ Sys* take_idle(elfel_server* s, const Key& k) {
 
 int create_sys(elfel_server* s, const Key& k, int npts, Sys** out) {
   Ctx* c = &s->h->c;
+  Timed tm(s->st.create_seconds);
   const int64_t before = c->in_use;
   std::unique_ptr<Sys> y(new Sys());
   y->key = k;
@@ -204,6 +213,7 @@ int create_sys(elfel_server* s, const Key& k, int npts, Sys** out) {
 int assemble_batch(elfel_server* s, const std::vector<Sys*>& ys) {
   Ctx* c = &s->h->c;
   if (ys.empty()) return ELFEL_OK;
+  Timed tm(s->st.assemble_seconds);
   for (Sys* y : ys) {
     Fused& F = y->m->F;
     fill_k<<<grid_for(F.nel, 256, (int64_t)c->sm_count * 8), 256, 0, c->stream>>>(F.coef.p, F.nel, y->req.r.kappa);
@@ -419,6 +429,7 @@ int step_batched(elfel_server* s, int32_t* active) {
   ELFEL_TRY(admit(s, &adm));
   ELFEL_TRY(assemble_batch(s, adm));
   for (Sys* y : adm) {
+    Timed tm(s->st.join_seconds);
     const int64_t before = c->in_use;
     int32_t slot = -1;
     int rc = batch_add_dev(s->batch, y->m, nullptr, y->T.p, 1, y->nu, s->cfg.rtol, s->cfg.maxit, &slot);
@@ -440,8 +451,12 @@ int step_batched(elfel_server* s, int32_t* active) {
     s->by_slot[slot] = y;
   }
   int32_t act = 0;
-  if (!s->by_slot.empty()) ELFEL_TRY(batch_step(s->batch, s->cfg.graphs_per_step, &act));
+  if (!s->by_slot.empty()) {
+    Timed tm(s->st.iterate_seconds);
+    ELFEL_TRY(batch_step(s->batch, s->cfg.graphs_per_step, &act));
+  }
   // harvest
+  Timed tm(s->st.harvest_seconds);
   int32_t nd = 0;
   std::vector<int32_t> ready(s->cfg.max_active);
   ELFEL_TRY(elfel_batch_done(s->batch, ready.data(), (int32_t)ready.size(), &nd));
@@ -476,6 +491,7 @@ int step_plain(elfel_server* s, int32_t* active) {
   ELFEL_TRY(rc);
   ELFEL_TRY(assemble_batch(s, adm));
   for (Sys* y : adm) {
+    Timed tm(s->st.iterate_seconds);
     const int64_t before = c->in_use;
     std::vector<double> T((size_t)y->n);
     ELFEL_CUDA(c, cudaMemcpyAsync(T.data(), y->T.p, sizeof(double) * y->n, cudaMemcpyDeviceToHost, c->stream));

@@ -316,6 +316,10 @@ typedef struct {
   int64_t resident_systems, resident_bytes;
   int64_t graph_launches, solver_kernel_launches, kernel_launches;
   double busy_seconds;    /* host time spent inside elfel_server_step */
+  /* its parts: creating systems (mesh, pattern), batched assembly, joining
+   * the solver (solver structures, values, lifted rhs), graph launches with
+   * the state readback, completing requests */
+  double create_seconds, assemble_seconds, join_seconds, iterate_seconds, harvest_seconds;
 } elfel_server_stats;
 ELFEL_API int elfel_server_create(elfel_ctx* ctx, const elfel_server_config* cfg, elfel_server** out);
 ELFEL_API int elfel_server_destroy(elfel_server* s);

@@ -94,6 +94,19 @@ def test_served_equals_alone(E, gpu):
     srv.close()
 
 
+def test_large_wave_autotuned_assembly(E, gpu):
+    """A wave above the tuner's threshold: every candidate CTA size of the
+    batched integration runs, and the result is still the alone result."""
+    srv = E.HeatServer("pcg32_ir", max_active=4)
+    rid = srv.submit(E.heat_request("T6", 190, kappa=1.1, Q=-5.0, keep_solution=True))
+    srv.submit(E.heat_request("T6", 7, kappa=0.9, Q=-2.0))
+    res = {r["id"]: r for r in srv.drain()}
+    assert res[rid]["converged"]
+    assert np.array_equal(srv.solution(rid), alone_in_batch(E, "T6", 190, 1.1, -5.0))
+    assert any(line.startswith("heat_batch_T6") for line, _ in gpu.tuning())
+    srv.close()
+
+
 def test_exact_quadratic_and_plain_mode(E, gpu):
     srvb = E.HeatServer("pcg32_ir", max_active=8)
     srvp = E.HeatServer("pcg64", batched=False)
