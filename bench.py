@@ -219,6 +219,18 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x, dist, device="cpu"):
+    """The largest x over all ranks (the step time every replica reports is the
+    slowest one's); x itself without a process group."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def reference_arm(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -272,7 +284,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=512, help="requests of the serving stream (4096: all)")
-    ap.add_argument("--serve-rates", default="0.3,0.6,0.9", help="arrival rates as fractions of the capacity")
+    ap.add_argument("--serve-rates", default="0.5,0.7,0.9", help="arrival rates as fractions of the capacity")
     ap.add_argument("--serve-plain-sample", type=int, default=48)
     args = ap.parse_args()
     if args.impl == "reference":
@@ -350,10 +362,7 @@ def main():
     ctx.profile(False)
     step_ms = [a.elapsed_time(b) for a, b in evs]
     t_step = sum(step_ms) / len(step_ms) / 1e3
-    if dist:
-        tt = torch.tensor([t_step], device=f"cuda:{local}")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step = float(tt.item())
+    t_step = max_over_ranks(t_step, dist, f"cuda:{local}" if torch.cuda.is_available() else "cpu")
     value = ws * nel / t_step
 
     # --- roofline of the dominant kernel (live CUDA events) ---------------

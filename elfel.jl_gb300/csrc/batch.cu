@@ -162,13 +162,9 @@ __device__ __forceinline__ bool item_finish(const BSys& S, const double* wsum, i
 }
 
 // ------------------------------------------------------------------ kernels
-// Programmatic dependent launch: the iteration kernels are captured with
-// programmatic stream serialization, so the next kernel is scheduled while
-// this one runs; it stages its first work item and system descriptor, then
-// waits (griddepcontrol.wait) until this grid has completed and its writes
-// are visible.  Without the launch attribute both instructions are no-ops.
-__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// With programmatic dependent launch (launch_pdl, pdl_wait) the kernels stage
+// their first work item and its system descriptor before waiting on the
+// previous kernel.
 
 // Copy a system descriptor into shared memory (one 8-byte word per thread).
 __device__ __forceinline__ void stage_sys(const BSys* __restrict__ src, BSys* dst) {
@@ -199,9 +195,12 @@ __device__ __forceinline__ void for_items(const BSys* __restrict__ sys, const in
     body(it, (const BSys&)S);
     t += gridDim.x;
     if (t >= total) break;
+    const int prev = it.x;
     it = items[t];
-    __syncthreads();  // every thread is done with the previous descriptor
-    stage_sys(sys + it.x, &S);
+    if (it.x != prev) {  // consecutive items of one system share the staged descriptor
+      __syncthreads();   // every thread is done with the previous descriptor
+      stage_sys(sys + it.x, &S);
+    }
   }
 }
 
@@ -578,28 +577,15 @@ void drop_graphs(elfel_batch* b) {
     }
 }
 
-// Launch with programmatic stream serialization (see pdl_wait).
-void launch_pdl(void (*k)(const BSys*, const int4*, const int*), unsigned grid, cudaStream_t s, const BSys* sys,
-                const int4* items, const int* ntot) {
-  cudaLaunchConfig_t cfg;
-  memset(&cfg, 0, sizeof(cfg));
-  cfg.gridDim = dim3(grid);
-  cfg.blockDim = dim3(kBlk);
-  cfg.stream = s;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, k, sys, items, ntot);
-}
-
 template <bool IR>
 void launch_iteration(cudaStream_t s, elfel_batch* b, const GridCfg& g, int sms) {
   const unsigned g1 = (unsigned)(sms * g.spmv), g2 = (unsigned)(sms * g.vec);
-  launch_pdl(b_spmv_k<IR>, g1, s, b->sys.p, b->items.p, b->ntot.p);
-  launch_pdl(b_update_k<IR>, g2, s, b->sys.p, b->items.p, b->ntot.p);
-  launch_pdl(b_p_k<IR>, g2, s, b->sys.p, b->items.p, b->ntot.p);
+  const BSys* sy = b->sys.p;
+  const int4* it = b->items.p;
+  const int* nt = b->ntot.p;
+  launch_pdl(b_spmv_k<IR>, g1, kBlk, s, sy, it, nt);
+  launch_pdl(b_update_k<IR>, g2, kBlk, s, sy, it, nt);
+  launch_pdl(b_p_k<IR>, g2, kBlk, s, sy, it, nt);
 }
 
 int graph_for(elfel_batch* b, int k, cudaGraphExec_t* out) {

@@ -82,10 +82,22 @@ __device__ __forceinline__ bool grid_sums(T (&v)[NV], Red4 red, double (&tot)[NV
   // blocks t, t + kBlk, ... in order, then a fixed-shape tree; the order
   // depends only on gridDim, so the result is deterministic.
   __threadfence();
+  double acc[NV];
+#pragma unroll
+  for (int a = 0; a < NV; ++a) acc[a] = 0.0;
+  // one pass over the partials, all NV values of a block together (the loads
+  // of several blocks in flight); each sum still runs over b in order
+#pragma unroll 4
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += kBlk) {
+    double v[NV];
+#pragma unroll
+    for (int a = 0; a < NV; ++a) v[a] = __ldcg(red.partials + b * 4 + a);
+#pragma unroll
+    for (int a = 0; a < NV; ++a) acc[a] += v[a];
+  }
 #pragma unroll
   for (int a = 0; a < NV; ++a) {
-    double s = 0.0;
-    for (unsigned b = threadIdx.x; b < gridDim.x; b += kBlk) s += __ldcg(red.partials + b * 4 + a);
+    double s = acc[a];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
     if (lane == 0) sh[a][wid] = s;
@@ -139,6 +151,8 @@ template <typename T, bool D16, bool DIFF, bool FLEX>
 __global__ void __launch_bounds__(kBlk, sell_occ<T>()) sell_cg_spmv_k(SellView A, const T* __restrict__ v, const T* __restrict__ x,
                                                       T* __restrict__ y, const T* __restrict__ r, Red4 red,
                                                       double* scal, int slot, int* flags) {
+  pdl_launch_dependents();
+  pdl_wait();
   if (flags[F_DONE] || flags[F_RU]) {
     // F_RU = 1: requested by the previous update; p has been advanced once by
     // cg_p_k since.  Mark it 2 so the rest of the graph skips until the host
@@ -236,6 +250,8 @@ __global__ void __launch_bounds__(kBlk, kVecOcc) cg_update_k(int64_t n, T* __res
                                                    const T* __restrict__ p, const T* __restrict__ q,
                                                    T* __restrict__ z, const T* __restrict__ dinv, Red4 red,
                                                    double* scal, int* flags) {
+  pdl_launch_dependents();
+  pdl_wait();
   if (flags[F_DONE] || flags[F_RU]) return;
   // breakdown (p.Ap not positive or not finite): no update, report below
   const double pq = scal[S_PQ];
@@ -294,6 +310,8 @@ __global__ void __launch_bounds__(kBlk, kVecOcc) cg_p_k(int64_t n, T* __restrict
                                               const double* scal, const int* flags) {
   // runs once more after a replacement request (F_RU = 1), so that p is the
   // recurrence's next direction when the residual gets replaced
+  pdl_launch_dependents();
+  pdl_wait();
   if (flags[F_DONE] || flags[F_RU] == 2) return;
   const T beta = (T)scal[S_BETA];
   FOR4(i, n) p[i] = z[i] + beta * p[i];
@@ -936,11 +954,11 @@ template <typename T, bool DIFF, bool FLEX>
 static void launch_cg_spmv(Ctx* c, SolverData* S, const T* v, const T* x, T* y, const T* r, Red4 red, int slot) {
   const SellView V = S->view();
   if (S->A.d16)
-    sell_cg_spmv_k<T, true, DIFF, FLEX><<<sell_grid<T>(S), kBlk, 0, c->stream>>>(V, v, x, y, r, red, S->scal.p, slot,
-                                                                              S->flags.p);
+    launch_pdl(sell_cg_spmv_k<T, true, DIFF, FLEX>, sell_grid<T>(S), kBlk, c->stream, V, v, x, y, r, red, S->scal.p,
+               slot, S->flags.p);
   else
-    sell_cg_spmv_k<T, false, DIFF, FLEX><<<sell_grid<T>(S), kBlk, 0, c->stream>>>(V, v, x, y, r, red, S->scal.p,
-                                                                               slot, S->flags.p);
+    launch_pdl(sell_cg_spmv_k<T, false, DIFF, FLEX>, sell_grid<T>(S), kBlk, c->stream, V, v, x, y, r, red, S->scal.p,
+               slot, S->flags.p);
 }
 
 template <typename T>
@@ -1023,9 +1041,9 @@ static int run_pcg64(elfel_sysmat* m, int maxit, elfel_solve_stats* st) {
   ELFEL_LAUNCH_CHECK(c);
   ELFEL_TRY(capture(c, &S->g_pcg64, [&]() {
     launch_cg_spmv<double, false, false>(c, S, S->A.v64.p, S->p64.p, S->q64.p, nullptr, red_area(S, 0), S_PQ);
-    cg_update_k<double, false><<<vg, kBlk, 0, c->stream>>>(nu, S->x64.p, S->r64.p, S->p64.p, S->q64.p, S->z64.p,
-                                                            S->dinv64.p, red_area(S, 1), S->scal.p, S->flags.p);
-    cg_p_k<double><<<vg, kBlk, 0, c->stream>>>(nu, S->p64.p, S->z64.p, S->scal.p, S->flags.p);
+    launch_pdl(cg_update_k<double, false>, vg, kBlk, c->stream, nu, S->x64.p, S->r64.p, S->p64.p, S->q64.p, S->z64.p,
+               S->dinv64.p, red_area(S, 1), S->scal.p, S->flags.p);
+    launch_pdl(cg_p_k<double>, vg, kBlk, c->stream, nu, S->p64.p, S->z64.p, S->scal.p, S->flags.p);
   }));
   while (true) {
     ELFEL_CUDA(c, cudaGraphLaunch(S->g_pcg64, c->stream));
@@ -1062,9 +1080,9 @@ static int run_pcg32(elfel_sysmat* m, int maxit, elfel_solve_stats* st) {
   ELFEL_LAUNCH_CHECK(c);
   ELFEL_TRY(capture(c, &S->g_pcg32, [&]() {
     launch_cg_spmv<float, true, true>(c, S, S->A.v32.p, S->p32.p, S->q32.p, S->r32.p, red_area(S, 0), S_PQ);
-    cg_update_k<float, true><<<vg, kBlk, 0, c->stream>>>(nu, S->xa32.p, S->r32.p, S->p32.p, S->q32.p, S->z32.p,
-                                                         S->dinv32.p, red_area(S, 1), S->scal.p, S->flags.p);
-    cg_p_k<float><<<vg, kBlk, 0, c->stream>>>(nu, S->p32.p, S->z32.p, S->scal.p, S->flags.p);
+    launch_pdl(cg_update_k<float, true>, vg, kBlk, c->stream, nu, S->xa32.p, S->r32.p, S->p32.p, S->q32.p, S->z32.p,
+               S->dinv32.p, red_area(S, 1), S->scal.p, S->flags.p);
+    launch_pdl(cg_p_k<float>, vg, kBlk, c->stream, nu, S->p32.p, S->z32.p, S->scal.p, S->flags.p);
   }));
   int refinements = 0;
   int launches = 0;

@@ -127,6 +127,41 @@ int lift_rhs(elfel_sysmat* m, const double* F, const double* T, int t_dev);
 // (device).
 int solution_residual(elfel_sysmat* m);
 
+// ------------------------------------------------------------------ launches
+// Programmatic dependent launch: the iteration kernels of the captured graphs
+// are launched with programmatic stream serialization, so the next kernel is
+// scheduled while this one runs; it waits (griddepcontrol.wait) until this
+// grid has completed and its writes are visible before touching its data.
+// Without the launch attribute both instructions are no-ops.
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// Off by default: measured on GB300 it gained nothing over plain graph
+// launches and slowed the FP64 one-system iteration at mid sizes; ELFEL_PDL=1
+// in the environment switches it on (for comparison).
+inline bool pdl_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("ELFEL_PDL");
+    return e && e[0] == '1';
+  }();
+  return on;
+}
+
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*k)(KArgs...), unsigned grid, unsigned block, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 // ------------------------------------------------------------------ SELL rows
 template <bool D16>
 __device__ __forceinline__ int sell_col(const SellView& A, int64_t k, int64_t row) {
