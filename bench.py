@@ -120,6 +120,106 @@ def serve_bench(E, ctx, nreq, fracs, plain_sample):
     return out
 
 
+def build_elasticity(E, nx, ny, seed=20261205):
+    """Plane strain on [0,2]x[0,1]: left edge clamped, unit traction on the right
+    edge, body force per element uniform in [-0.1, 0.1]^2 (seeded)."""
+    Lx, Ly = 2.0, 1.0
+    mesh = E.T6block(Lx, Ly, nx, ny)
+    fesp = E.FESpace(float, mesh, E.FEH1_T6(), 2)
+    left = E.vselect(mesh.xy, [0.0, 0.0, 0.0, Ly], inflate=Lx / nx / 100)
+    E.setebc(fesp, 0, left, 1, 0.0)
+    E.setebc(fesp, 0, left, 2, 0.0)
+    E.numberdofs(fesp)
+    bforce = np.random.default_rng(seed).uniform(-0.1, 0.1, size=(mesh.nel, 2))
+    be = E.boundary_edges(mesh)
+    c = mesh.conn - 1
+    le = be[:, 1] - 1
+    a, b = c[be[:, 0] - 1, le], c[be[:, 0] - 1, (le + 1) % 3]
+    right = be[(np.abs(mesh.xy[a, 0] - Lx) < 1e-12) & (np.abs(mesh.xy[b, 0] - Lx) < 1e-12)]
+    return mesh, fesp, bforce, right
+
+
+def build_cavity(E, N):
+    """Lid-driven cavity, Taylor-Hood (vector T6 velocity, T3 pressure): u = (1, 0)
+    on the top edge, 0 on the other walls, pressure pinned at one corner."""
+    vmesh = E.T6block(1.0, 1.0, N, N)
+    pmesh = E.T6toT3(vmesh)
+    ufesp = E.FESpace(float, vmesh, E.FEH1_T6(), 2)
+    pfesp = E.FESpace(float, pmesh, E.FEH1_T3(), 1)
+    infl = 1.0 / N / 100
+    for box in ([0.0, 1.0, 0.0, 0.0], [0.0, 0.0, 0.0, 1.0], [1.0, 1.0, 0.0, 1.0]):
+        vl = E.vselect(vmesh.xy, box, infl)
+        E.setebc(ufesp, 0, vl, 1, 0.0)
+        E.setebc(ufesp, 0, vl, 2, 0.0)
+    vl = E.vselect(vmesh.xy, [0.0, 1.0, 1.0, 1.0], infl)
+    E.setebc(ufesp, 0, vl, 1, 1.0)
+    E.setebc(ufesp, 0, vl, 2, 0.0)
+    E.setebc(pfesp, 0, 1, 1, 0.0)
+    E.numberdofs([ufesp, pfesp])
+    return vmesh, pmesh, ufesp, pfesp
+
+
+def problem_bench(E, ctx, args):
+    """Elasticity (plane strain T6) or Stokes (Taylor-Hood cavity) at scale:
+    fused assembly rate, and the FP64 vs FP32-refinement solves."""
+    import torch
+
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    t0 = time.perf_counter()
+    if args.problem == "elasticity":
+        nx = args.n or 1000
+        mesh, fesp, bforce, right = build_elasticity(E, nx, nx // 2)
+        n, nu = E.ndofs(fesp), E.nunknowns(fesp)
+        elit, qpit = E.FEIterator(fesp), E.QPIterator(fesp, {"npts": 3})
+        am = E.start(E.SysmatAssemblerGPU(ctx), n, n)
+        step = lambda: E.assemble_elasticity(am, elit, qpit, 1.0, 0.3, True, bforce, right, (1.0, 0.0))
+        methods, rtol = ("pcg64", "pcg32_ir"), 1e-10
+        work = f"plane-strain elasticity T6 {nx}x{nx // 2} on [0,2]x[0,1] ({mesh.nel} elements, {n} DOFs)"
+        spaces = fesp
+    else:
+        N = args.n or 600
+        vmesh, pmesh, ufesp, pfesp = build_cavity(E, N)
+        n = E.ndofs(ufesp) + E.ndofs(pfesp)
+        nu = E.nunknowns(ufesp) + E.nunknowns(pfesp)
+        elit, pelit, qpit = E.FEIterator(ufesp), E.FEIterator(pfesp), E.QPIterator(ufesp, {"npts": 3})
+        am = E.start(E.SysmatAssemblerGPU(ctx), n, n)
+        step = lambda: E.assemble_stokes(am, elit, pelit, qpit, 1.0)
+        methods, rtol = ("minres64", "minres32_ir"), 1e-8
+        mesh = vmesh
+        work = f"Stokes Taylor-Hood lid-driven cavity {N}x{N} ({vmesh.nel} elements, {n} DOFs)"
+        spaces = [ufesp, pfesp]
+    host_s = time.perf_counter() - t0
+    step()  # set-up (tables, pattern) and a first assembly
+    ctx.synchronize()
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(args.steps):
+            step()
+        b.record(stream)
+        torch.cuda.synchronize()
+    t_asm = a.elapsed_time(b) / 1e3 / args.steps
+    U0 = np.zeros(n)
+    E.gathersysvec(U0, spaces)
+    sols = {}
+    for m in methods:
+        U = U0.copy()
+        st = am.solve(U, nu, None, method=m, rtol=rtol, maxit=500000)
+        sols[m] = (st, U)
+    (s64, U64), (s32, U32) = sols[methods[0]], sols[methods[1]]
+    out = {"problem": args.problem, "workload": work, "elements": mesh.nel, "ndofs": n, "nunknowns": nu,
+           "assembly_elements_per_s": mesh.nel / t_asm, "assembly_ms": t_asm * 1e3, "host_setup_s": host_s,
+           "rtol": rtol, methods[0]: s64, methods[1]: s32, "speedup": s64["seconds"] / s32["seconds"],
+           "fp32_vs_fp64_rel_err_max": float(np.abs(U32[:nu] - U64[:nu]).max() / np.abs(U64[:nu]).max()),
+           "data": "synthetic (seeded)"}
+    print(json.dumps(out), flush=True)
+    del am
+    return 0
+
+
 def read_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -277,7 +377,9 @@ def main():
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--n", type=int, default=1000, help="cells per side")
+    ap.add_argument("--n", type=int, default=None, help="cells per side (heat, elasticity: 1000; Stokes: 600)")
+    ap.add_argument("--problem", default="heat", choices=["heat", "elasticity", "stokes"],
+                    help="heat: the contract line; elasticity / stokes: assembly rate and solves at scale")
     ap.add_argument("--no-pcg", action="store_true")
     ap.add_argument("--pcg-methods", default="pcg64,pcg32_ir", help="solves to run, in order")
     ap.add_argument("--no-cpu", action="store_true")
@@ -286,6 +388,7 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=512, help="requests of the serving stream (4096: all)")
     ap.add_argument("--serve-rates", default="0.5,0.7,0.9", help="arrival rates as fractions of the capacity")
     ap.add_argument("--serve-plain-sample", type=int, default=48)
+    ap.add_argument("--probe-rates", action="store_true", help="print the device's FP64/FP32 FMA rates and exit")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -309,8 +412,18 @@ def main():
         dist.barrier()
     E._native.load()
     ctx = E.Context(local)
+    rates = {"fp64_tflops": ctx.fma_rate(64), "fp32_tflops": ctx.fma_rate(32)}
+    if args.probe_rates:
+        if rank == 0:
+            print(json.dumps(rates), flush=True)
+        ctx.close()
+        return 0
+    if args.problem != "heat":
+        rc = problem_bench(E, ctx, args) if rank == 0 else 0
+        ctx.close()
+        return rc
     stream = torch.cuda.ExternalStream(ctx.stream())
-    N = args.n
+    N = args.n or 1000
     t_setup0 = time.perf_counter()
     mesh, fesp, kappa = build_problem(E, N)
     host_setup_s = time.perf_counter() - t_setup0
@@ -382,16 +495,14 @@ def main():
     # whole-assembly algorithmic bytes (conn + coords + coefficient + K values + F)
     asm_bytes = nel * 6 * 4 + mesh.nnodes * 16 + nel * 8 + nnz_est * 8 + n * 8
     ach = alg[dom] / (per[dom] * 1e-3) / 1e9
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            tr = json.load(f)
-        ent = tr.get(dom)
-        if ent:
-            traffic = ent["bytes_per_element"] * nel
+    # DRAM traffic of one heat_k<6> launch (dram__bytes_read.sum + dram__bytes_write.sum) measured
+    # with ncu on the 700 x 700 case of this workload (980,000 elements: 63.04 + 152.40 MB), scaled
+    # by the element count; writes still dirty in L2 when the kernel ends are not counted
+    HEAT_K_TRAFFIC_PER_ELEMENT = (63.04128e6 + 152.398592e6) / 980000
+    traffic = HEAT_K_TRAFFIC_PER_ELEMENT * nel if dom == "integrate_heat" else None
     roofline = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
                 "traffic": traffic, "kernel": dom, "peak_kind": peak_kind,
+                "traffic_source": "ncu DRAM bytes of heat_k<6> at 980,000 elements, scaled per element",
                 "assembly": {"alg_bytes": asm_bytes, "achieved": asm_bytes / t_step / 1e9,
                              "frac": asm_bytes / t_step / 1e9 / hbm},
                 "kernels": kernel_rows}
@@ -503,7 +614,7 @@ def main():
                       "elements": nel, "ndofs": n, "nnz": nnz_dev, "l2": "256 MB buffer written between timed steps",
                       "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU"},
            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 3 * args.steps, "clocks": clk,
-           "pcg": pcg, "serve": serve, "pattern_build_s": pattern_s, "setup_phases_ms": {k: v[0] for k, v in setup_phases.items()},
+           "pcg": pcg, "serve": serve, "fma_rates": rates, "pattern_build_s": pattern_s, "setup_phases_ms": {k: v[0] for k, v in setup_phases.items()},
            "wall_s_timed": wall, "host_mesh_setup_s": host_setup_s}
     if rank == 0:
         print(json.dumps(out), flush=True)

@@ -157,6 +157,7 @@ SIGNATURES = {
     "elfel_batch_result": (ctypes.c_int, [_vp, ctypes.c_int32, _dp, ctypes.POINTER(SolveStats)]),
     "elfel_ctx_tuning": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int,
                                         ctypes.POINTER(ctypes.c_int32)]),
+    "elfel_ctx_fma_rate": (ctypes.c_int, [_vp, ctypes.c_int32, _dp]),
     "elfel_fused_setup_block": (ctypes.c_int, [_vp, ctypes.POINTER(BlockDesc), _i64p, _i64p]),
     "elfel_block_dirichlet": (ctypes.c_int, [_vp, _dp, _dp]),
     "elfel_fused_tables": (ctypes.c_int, [_vp, _i64p, _dp, _i64p]),
@@ -263,6 +264,12 @@ class Context:
             out[buf.value.decode()] = (ms.value, k.value)
             i += 1
         return out
+
+    def fma_rate(self, bits=64):
+        """Measured FMA throughput of the device, TFLOP/s (bits = 32 or 64)."""
+        t = ctypes.c_double()
+        self.check(self.lib.elfel_ctx_fma_rate(self.h, int(bits), ctypes.byref(t)))
+        return t.value
 
     def tuning(self):
         """Autotuner records: [(line, chosen index)], one per tuned key."""

@@ -212,8 +212,8 @@ __global__ void __launch_bounds__(kBlk, 5) b_spmv_k(const BSys* __restrict__ sys
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for_items(sys, items, nitems_total, [&](const int4& it, const BSys& S) {
     const int mode = S.st[I_MODE];
-    if (IR) {
-      if (mode == M_CG || mode == M_STARTED) {
+    if (IR && (mode == M_CG || mode == M_STARTED)) {
+      {
         for (int64_t j = it.y; j < it.y + it.z; ++j) {
           const int64_t s = j * (kBlk / 32) + wid;
           const int64_t row = s * 32 + lane;
@@ -238,7 +238,11 @@ __global__ void __launch_bounds__(kBlk, 5) b_spmv_k(const BSys* __restrict__ sys
           S.sc[B_ALPHA] = (tot[0] > 0.0 && isfinite(tot[0])) ? tot[1] / tot[0] : 0.0;
           if (mode == M_STARTED) S.st[I_MODE] = M_CG;
         }
-      } else if (mode == M_FOLD) {
+      }
+    } else if (mode == M_FOLD) {
+      // FP64 residual check (both methods): FP32 refinement replacement, or
+      // the FP64 recurrence's claim of convergence
+      {
         for (int64_t j = it.y; j < it.y + it.z; ++j) {
           const int64_t s = j * (kBlk / 32) + wid;
           const int64_t row = s * 32 + lane;
@@ -262,20 +266,21 @@ __global__ void __launch_bounds__(kBlk, 5) b_spmv_k(const BSys* __restrict__ sys
           S.st[I_REPL] += 1;
           const bool exact = !(rrt > 0.0) && isfinite(rrt);
           const bool conv = exact || rrt <= S.sc[B_TOL2] * S.sc[B_BN2];
-          if (conv || !isfinite(rrt) || S.st[I_ITER] >= S.st[I_MAXIT]) {
+          if (conv || !isfinite(rrt) || S.st[I_ITER] >= S.st[I_MAXIT] || (!IR && S.st[I_REPL] > 50)) {
             S.st[I_CONV] = conv ? 1 : 0;
             S.st[I_MODE] = M_DONE;
           } else {
-            // keep the search direction unless the FP32 recurrence broke down
-            // or its residual drifted far below the true one
+            // FP32 refinement: keep the search direction unless the
+            // recurrence broke down or its residual drifted far below the
+            // true one; FP64: restart from the true residual
             const double rrec = S.sc[B_RREC];
-            S.st[I_RESTART] = (S.st[I_BRK] || !(rrec > 0.0) || !(rrec >= 1e-6 * rrt)) ? 1 : 0;
+            S.st[I_RESTART] = (!IR || S.st[I_BRK] || !(rrec > 0.0) || !(rrec >= 1e-6 * rrt)) ? 1 : 0;
             S.st[I_BRK] = 0;
             S.st[I_MODE] = M_RESTART;
           }
         }
       }
-    } else if (mode == M_CG) {
+    } else if (!IR && (mode == M_CG || mode == M_STARTED)) {
       for (int64_t j = it.y; j < it.y + it.z; ++j) {
         const int64_t s = j * (kBlk / 32) + wid;
         const int64_t row = s * 32 + lane;
@@ -295,6 +300,7 @@ __global__ void __launch_bounds__(kBlk, 5) b_spmv_k(const BSys* __restrict__ sys
       if (item_finish<1>(S, wsum, it.y, it.z, (unsigned)*S.nitems, tot)) {
         S.sc[B_PQ] = tot[0];
         S.sc[B_ALPHA] = (tot[0] > 0.0 && isfinite(tot[0])) ? S.sc[B_RZ] / tot[0] : 0.0;
+        if (mode == M_STARTED) S.st[I_MODE] = M_CG;
       }
     }
   });
@@ -408,10 +414,32 @@ __global__ void __launch_bounds__(kBlk) b_update_k(const BSys* __restrict__ sys,
         const int itn = ++S.st[I_ITER];
         const bool conv = rr <= S.sc[B_TOL2] * S.sc[B_BN2];
         const bool bad = brk || !isfinite(rz) || !isfinite(rr);
-        if (conv || bad || itn >= S.st[I_MAXIT]) {
+        if (conv && !bad && itn < S.st[I_MAXIT]) {
+          S.st[I_MODE] = M_FOLD;  // the recurrence says converged: check the true residual
+        } else if (conv || bad || itn >= S.st[I_MAXIT]) {
           S.st[I_CONV] = (conv && !bad) ? 1 : 0;
           S.st[I_MODE] = M_DONE;
         }
+      }
+    } else if (mode == M_RESTART) {
+      // restart from the true residual: z = D r, p = z
+      double prz = 0.0;
+      for (int64_t j = it.y; j < it.y + it.z; ++j) {
+        const int64_t row = j * kBlk + threadIdx.x;
+        prz = 0.0;
+        if (row < S.A.nrows) {
+          const double zi = S.dinv64[row] * S.r64[row];
+          S.z64[row] = zi;
+          S.p64[row] = zi;
+          prz = S.r64[row] * zi;
+        }
+        double v[1] = {prz};
+        warp_part<1>(v, wsum, (int)(j - it.y));
+      }
+      double tot[1];
+      if (item_finish<1>(S, wsum, it.y, it.z, (unsigned)*S.nitems, tot)) {
+        S.sc[B_RZ] = tot[0];
+        S.st[I_MODE] = M_STARTED;
       }
     }
   });

@@ -240,6 +240,51 @@ int tune_lookup(const Ctx* c, const char* key) {
 
 }  // namespace elfel
 
+// FMA throughput probe: 8 independent FMA chains per thread, one full wave.
+template <typename T>
+__global__ void __launch_bounds__(256) fma_rate_k(T* out, int iters, T a, T b) {
+  T x[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = (T)(threadIdx.x + k);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+  }
+  T s = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += x[k];
+  if (s == (T)-1) out[0] = s;  // never true for these inputs; keeps the chains live
+}
+
+extern "C" int elfel_ctx_fma_rate(elfel_ctx* h, int32_t bits, double* tflops) {
+  if (!h || !tflops || (bits != 32 && bits != 64)) return ELFEL_ERR_ARG;
+  Ctx* c = &h->c;
+  cudaSetDevice(c->device);
+  DBuf<double> out;
+  ELFEL_TRY(out.alloc(c, 1));
+  const unsigned grid = (unsigned)c->sm_count * 8;
+  const int iters = bits == 64 ? 1 << 12 : 1 << 15;
+  cudaEvent_t e0, e1;
+  ELFEL_CUDA(c, cudaEventCreate(&e0));
+  ELFEL_CUDA(c, cudaEventCreate(&e1));
+  float best = 1e30f;
+  for (int rep = 0; rep < 4; ++rep) {  // the first run warms up
+    ELFEL_CUDA(c, cudaEventRecord(e0, c->stream));
+    if (bits == 64) fma_rate_k<double><<<grid, 256, 0, c->stream>>>(out.p, iters, 0.999999, 1e-7);
+    else fma_rate_k<float><<<grid, 256, 0, c->stream>>>((float*)out.p, iters, 0.999999f, 1e-7f);
+    ELFEL_CUDA(c, cudaEventRecord(e1, c->stream));
+    ELFEL_CUDA(c, cudaEventSynchronize(e1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0 && ms < best) best = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  out.release(c);
+  *tflops = 2.0 * 8.0 * iters * (double)grid * 256.0 / (best * 1e-3) / 1e12;
+  return ELFEL_OK;
+}
+
 extern "C" int elfel_ctx_tuning(const elfel_ctx* h, int index, char* line, int cap, int32_t* choice) {
   if (!h) return ELFEL_ERR_ARG;
   const Ctx* c = &h->c;

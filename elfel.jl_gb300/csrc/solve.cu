@@ -1045,13 +1045,34 @@ static int run_pcg64(elfel_sysmat* m, int maxit, elfel_solve_stats* st) {
                S->dinv64.p, red_area(S, 1), S->scal.p, S->flags.p);
     launch_pdl(cg_p_k<double>, vg, kBlk, c->stream, nu, S->p64.p, S->z64.p, S->scal.p, S->flags.p);
   }));
+  // When the recurrence residual says converged, the true residual b - K x is
+  // checked in FP64; if the two have drifted apart (ill-conditioned systems
+  // at tight tolerances) the true residual replaces the recurrence one and
+  // CG restarts from it.
+  int replacements = 0;
   while (true) {
     ELFEL_CUDA(c, cudaGraphLaunch(S->g_pcg64, c->stream));
     ELFEL_TRY(read_flags(c, S, hf));
-    if (hf[F_DONE]) break;
+    if (!hf[F_DONE]) continue;
+    if (!hf[F_CONV] || hf[F_ITER] >= maxit || replacements >= 50) break;
+    ELFEL_TRY(launch_sell_resid(c, S, S->x64.p, S->b64.p, S->r64.p, red_area(S, 2), S_RR));
+    double hsc[S_COUNT];
+    ELFEL_CUDA(c, cudaMemcpyAsync(hsc, S->scal.p, sizeof(hsc), cudaMemcpyDeviceToHost, c->stream));
+    ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (hsc[S_RR] <= hsc[S_TOL2] * hsc[S_BN2]) break;
+    ++replacements;
+    if (c->trace)
+      fprintf(stderr, "[elfel pcg64] it %d: true residual %.3e above the recurrence's; restart\n", hf[F_ITER],
+              sqrt(hsc[S_RR] / hsc[S_BN2]));
+    hf[F_DONE] = 0;
+    hf[F_CONV] = 0;
+    ELFEL_CUDA(c, cudaMemcpyAsync(S->flags.p, hf, sizeof(hf), cudaMemcpyHostToDevice, c->stream));
+    cg_start_k<double><<<vg, kBlk, 0, c->stream>>>(nu, S->r64.p, S->z64.p, S->p64.p, S->dinv64.p, red_area(S, 0),
+                                                   S->scal.p, S->flags.p, 1, 1.0);
+    ELFEL_LAUNCH_CHECK(c);
   }
   st->iterations = hf[F_ITER];
-  st->refinements = 0;
+  st->refinements = replacements;
   return ELFEL_OK;
 }
 

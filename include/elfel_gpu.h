@@ -339,6 +339,12 @@ ELFEL_API int elfel_server_stats_read(elfel_server* s, elfel_server_stats* out);
  * tuner is on unless the environment sets ELFEL_TUNE=0. */
 ELFEL_API int elfel_ctx_tuning(const elfel_ctx* ctx, int index, char* line, int cap, int32_t* choice);
 
+/* Diagnostics (no counterpart in the reference): the device's FMA throughput
+ * in TFLOP/s for bits = 32 or 64, timed with CUDA events on a full wave of
+ * independent FMA chains -- the figure behind the FP64-bound reading of the
+ * assembly kernels. */
+ELFEL_API int elfel_ctx_fma_rate(elfel_ctx* ctx, int32_t bits, double* tflops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -66,6 +66,31 @@ def test_heat_solve_vs_direct(E, O, gpu, method, etype, N, orient, jit):
     assert np.abs(T - T0).max() / np.abs(T0).max() < ERR_TOL
 
 
+def test_high_contrast_reaches_tolerance(E, O, gpu):
+    """Conductivity over eight decades at rtol 1e-12: the FP64 recurrence can
+    claim convergence before the true residual gets there; the one-system and
+    the batched FP64 PCG check the true residual and continue, so both end at
+    rtol (true FP64 residual) and at the direct solution."""
+    rng = np.random.default_rng(17)
+    mesh, fesp, am, kappa = heat_system(E, "T3", 64, "alternate", 0.0,
+                                        kappa=np.exp(rng.uniform(np.log(1e-4), np.log(1e4), 2 * 64 * 64)))
+    n, nu = E.ndofs(fesp), E.nunknowns(fesp)
+    K0, F0 = heat_oracle(E, O, mesh, fesp, 3, kappa, -6.0)
+    T = np.zeros(n)
+    E.gathersysvec(T, fesp)
+    T0 = O.solve_lifted(K0, F0, T.copy(), nu)
+    T1 = T.copy()
+    st = E.solve(T1, am, None, nu, method="pcg64", rtol=1e-12, maxit=200000)
+    assert st["converged"] and st["relres"] <= 1e-12
+    b = E.BatchSolver("pcg64", capacity=1)
+    s = b.add(am, T, nu, rtol=1e-12, maxit=200000)
+    T2, st2 = b.run()[s]
+    b.close()
+    assert st2["converged"] and st2["relres"] <= 1e-12
+    for Tx in (T1, T2):  # error bar of this conditioning (contrast 1e8): 1e-4
+        assert np.abs(Tx - T0).max() / np.abs(T0).max() < 1e-4
+
+
 def test_heat_t3_exact_config0(E, gpu):
     """The 100 x 100 T3 heat problem (uniform diagonals) reproduces the exact quadratic."""
     mesh, fesp, am, _ = heat_system(E, "T3", 100, kappa=1.0)
