@@ -444,6 +444,8 @@ int fused_build(elfel_sysmat* m, int64_t ndofs) {
     ELFEL_TRY(F.pmass_store.alloc(c, (size_t)(F.nel * 3 > 0 ? F.nel * 3 : 1)));
     ELFEL_TRY(F.pmass_diag.alloc(c, (size_t)(ndofs > 0 ? ndofs : 1)));
   }
+  ELFEL_TRY(F.straight.alloc(c, (size_t)(F.nel > 0 ? F.nel : 1)));
+  ELFEL_TRY(launch_straight(c, F.nn_u, F.nel, F.conn_u.p, F.xy_u.p, F.straight.p));
   ELFEL_TRY(F.kstore.alloc(c, (size_t)(F.nel * g.store_per_elem > 0 ? F.nel * g.store_per_elem : 1)));
   ELFEL_TRY(F.fstore.alloc(c, (size_t)(F.nel * nedof > 0 ? F.nel * nedof : 1)));
   ELFEL_TRY(m->vals.alloc(c, (size_t)(m->P.nnz > 0 ? m->P.nnz : 1)));
@@ -526,7 +528,7 @@ extern "C" int elfel_fused_set_geometry(elfel_sysmat* m, const double* xy) {
   if (m->F.nnodes_u)
     ELFEL_CUDA(c, cudaMemcpyAsync(m->F.xy_u.p, xy, sizeof(double) * 2 * m->F.nnodes_u, cudaMemcpyHostToDevice,
                                   c->stream));
-  return ELFEL_OK;
+  return launch_straight(c, m->F.nn_u, m->F.nel, m->F.conn_u.p, m->F.xy_u.p, m->F.straight.p);
 }
 
 static int finish_values(elfel_sysmat* m) {
@@ -555,7 +557,8 @@ extern "C" int elfel_fused_heat(elfel_sysmat* m, const double* kappa, double Q) 
     ELFEL_CUDA(c, cudaMemcpyAsync(F.coef.p, kappa, sizeof(double) * F.nel, cudaMemcpyHostToDevice, c->stream));
   {
     Phase ph(c, "integrate_heat");
-    ELFEL_TRY(launch_heat(c, F.nn_u, F.nel, F.conn_u.p, F.xy_u.p, F.coef.p, Q, F.tab, F.kstore.p, F.fstore.p));
+    ELFEL_TRY(launch_heat(c, F.nn_u, F.nel, F.conn_u.p, F.xy_u.p, F.coef.p, Q, F.straight.p, F.tab, F.kstore.p,
+                          F.fstore.p));
   }
   return finish_values(m);
 }

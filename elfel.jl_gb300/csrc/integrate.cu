@@ -150,11 +150,75 @@ __device__ __forceinline__ void write_records(const double* acc, int rec, int64_
 }
 
 // ------------------------------------------------------------------ heat
-// The NT elements e0 .. e0 + NT - 1 of one mesh, one per thread.
-template <int NN, int NT>
+// Structural zeros of the T6 reference tensors for quadrature rules that
+// integrate the products of the (linear) parametric gradients exactly, e.g.
+// the 3-point rule: bit k = stored entry k (k = j(j+1)/2 + i, i <= j) has a
+// nonzero coefficient in S11, S22, S12 + S21; bit j of kT6P = the element
+// load vector entry j, sum_q w_q N_j, is nonzero (the vertex functions of P2
+// integrate to zero).  With pattern kPatT6 the straight-sided branch skips
+// the zero terms: 34 of 63 FP64 multiply-adds remain.
+constexpr uint32_t kT6S11 = 0x1842c7u, kT6S22 = 0x12e229u, kT6S12 = 0x1efadbu, kT6P = 0x38u;
+constexpr int kPatGeneric = 0, kPatT6 = 1;
+
+// Per-element flag: 1 when the element is straight-sided (the Jacobian is
+// constant and the reference-tensor form applies).  Computed once per
+// geometry, not per assembly.
+template <int NN>
+__global__ void straight_k(int64_t nel, const int32_t* __restrict__ conn, const double2* __restrict__ xy,
+                           uint8_t* __restrict__ flag) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nel; e += (int64_t)gridDim.x * blockDim.x) {
+    Geo<NN> g;
+#pragma unroll
+    for (int j = 0; j < NN; ++j) {
+      const double2 p = xy[conn[e * NN + j]];
+      g.x[j] = p.x;
+      g.y[j] = p.y;
+    }
+    flag[e] = straight_sided<NN>(g) ? 1 : 0;
+  }
+}
+
+int launch_straight(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* xy, uint8_t* flag) {
+  if (nel == 0) return ELFEL_OK;
+  const unsigned grid = grid_for(nel, 256, (int64_t)c->sm_count * 16);
+  if (nn == 3) straight_k<3><<<grid, 256, 0, c->stream>>>(nel, conn, (const double2*)xy, flag);
+  else straight_k<6><<<grid, 256, 0, c->stream>>>(nel, conn, (const double2*)xy, flag);
+  ELFEL_LAUNCH_CHECK(c);
+  return ELFEL_OK;
+}
+
+// The T6 zero pattern of a table, when its tensors have exactly the zeros of
+// kT6S11/kT6S22/kT6S12/kT6P (entries below 1e-13 of the largest count as
+// zero: quadrature residues); else the generic pattern.
+int heat_pattern(int nn, const QPTab& t) {
+  if (nn != 6) return kPatGeneric;
+  double mx = 0.0;
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b)
+      for (int k = 0; k < 36; ++k) mx = fmax(mx, fabs(t.S[a][b][k]));
+  const double tiny = 1e-13 * mx;
+  uint32_t m11 = 0, m22 = 0, m12 = 0, mp = 0;
+  for (int j = 0; j < 6; ++j)
+    for (int i = 0; i <= j; ++i) {
+      const int k = j * (j + 1) / 2 + i;
+      if (fabs(t.S[0][0][i * 6 + j]) > tiny) m11 |= 1u << k;
+      if (fabs(t.S[1][1][i * 6 + j]) > tiny) m22 |= 1u << k;
+      if (fabs(t.S[0][1][i * 6 + j] + t.S[1][0][i * 6 + j]) > tiny) m12 |= 1u << k;
+    }
+  double pmax = 0.0;
+  for (int j = 0; j < 6; ++j) pmax = fmax(pmax, fabs(t.P[j]));
+  for (int j = 0; j < 6; ++j)
+    if (fabs(t.P[j]) > 1e-13 * pmax) mp |= 1u << j;
+  return (m11 == kT6S11 && m22 == kT6S22 && m12 == kT6S12 && mp == kT6P) ? kPatT6 : kPatGeneric;
+}
+
+// The NT elements e0 .. e0 + NT - 1 of one mesh, one per thread.  straight:
+// per-element flags (straight_k); PAT: the tensors' zero pattern.
+template <int NN, int NT, int PAT>
 __device__ __forceinline__ void heat_elems(int64_t e0, int64_t nel, const int32_t* __restrict__ conn,
                                            const double2* __restrict__ xy, const double* __restrict__ kappa, double Q,
-                                           const QPTab& tab, double* __restrict__ kstore, double* __restrict__ fstore) {
+                                           const uint8_t* __restrict__ straight, const QPTab& tab,
+                                           double* __restrict__ kstore, double* __restrict__ fstore) {
   constexpr int NS = NN * (NN + 1) / 2;
   constexpr int LD = NT + 1;
   extern __shared__ double acc[];  // (NS + NN) * LD
@@ -177,7 +241,7 @@ __device__ __forceinline__ void heat_elems(int64_t e0, int64_t nel, const int32_
   double* fa = acc + NS * LD;
   if (e < nel) {
     const double kap = kappa[e];
-    if (straight_sided<NN>(g)) {
+    if (NN == 3 || straight[e]) {
       const double J11 = g.x[1] - g.x[0], J12 = g.x[2] - g.x[0];
       const double J21 = g.y[1] - g.y[0], J22 = g.y[2] - g.y[0];
       const double det = J11 * J22 - J21 * J12;
@@ -185,11 +249,24 @@ __device__ __forceinline__ void heat_elems(int64_t e0, int64_t nel, const int32_
       const double c11 = (J22 * J22 + J12 * J12) * s;
       const double c22 = (J21 * J21 + J11 * J11) * s;
       const double c12 = -(J22 * J21 + J12 * J11) * s;
-#pragma unroll
-      for (int k = 0; k < NS; ++k) acc[k * LD + t] = c11 * sS[0][k] + c22 * sS[1][k] + c12 * sS[2][k];
       const double qd = Q * det;
+      if (PAT == kPatT6) {
 #pragma unroll
-      for (int j = 0; j < NN; ++j) fa[j * LD + t] = qd * tab.P[j];
+        for (int k = 0; k < NS; ++k) {
+          double a = 0.0;
+          if ((kT6S12 >> k) & 1u) a = c12 * sS[2][k];
+          if ((kT6S22 >> k) & 1u) a = fma(c22, sS[1][k], a);
+          if ((kT6S11 >> k) & 1u) a = fma(c11, sS[0][k], a);
+          acc[k * LD + t] = a;
+        }
+#pragma unroll
+        for (int j = 0; j < NN; ++j) fa[j * LD + t] = ((kT6P >> j) & 1u) ? qd * tab.P[j] : 0.0;
+      } else {
+#pragma unroll
+        for (int k = 0; k < NS; ++k) acc[k * LD + t] = c11 * sS[0][k] + c22 * sS[1][k] + c12 * sS[2][k];
+#pragma unroll
+        for (int j = 0; j < NN; ++j) fa[j * LD + t] = qd * tab.P[j];
+      }
     } else {
       double ke[NS], fe[NN];
 #pragma unroll
@@ -234,17 +311,19 @@ __device__ __forceinline__ void heat_elems(int64_t e0, int64_t nel, const int32_
   write_records<NT>(fa, NN, e0, nel, fstore);
 }
 
-template <int NN>
+template <int NN, int PAT>
 __global__ void __launch_bounds__(kIntThreads) heat_k(int64_t nel, const int32_t* __restrict__ conn,
                                                      const double2* __restrict__ xy, const double* __restrict__ kappa,
-                                                     double Q, const __grid_constant__ QPTab tab,
-                                                     double* __restrict__ kstore, double* __restrict__ fstore) {
-  heat_elems<NN, kIntThreads>((int64_t)blockIdx.x * kIntThreads, nel, conn, xy, kappa, Q, tab, kstore, fstore);
+                                                     double Q, const uint8_t* __restrict__ straight,
+                                                     const __grid_constant__ QPTab tab, double* __restrict__ kstore,
+                                                     double* __restrict__ fstore) {
+  heat_elems<NN, kIntThreads, PAT>((int64_t)blockIdx.x * kIntThreads, nel, conn, xy, kappa, Q, straight, tab, kstore,
+                                   fstore);
 }
 
 // Many meshes in one launch: CTA b works on mesh k with jobs[k].blk0 <= b <
 // jobs[k + 1].blk0, elements (b - blk0) * NT onwards.
-template <int NN, int NT>
+template <int NN, int NT, int PAT>
 __global__ void __launch_bounds__(NT) heat_batch_k(const HeatJob* __restrict__ jobs, int njobs,
                                                    const __grid_constant__ QPTab tab) {
   int lo = 0, hi = njobs - 1;
@@ -253,43 +332,49 @@ __global__ void __launch_bounds__(NT) heat_batch_k(const HeatJob* __restrict__ j
     if (jobs[mid].blk0 <= (int64_t)blockIdx.x) lo = mid; else hi = mid - 1;
   }
   const HeatJob J = jobs[lo];
-  heat_elems<NN, NT>(((int64_t)blockIdx.x - J.blk0) * NT, J.nel, J.conn, (const double2*)J.xy, J.kappa, J.Q, tab,
-                     J.kstore, J.fstore);
+  heat_elems<NN, NT, PAT>(((int64_t)blockIdx.x - J.blk0) * NT, J.nel, J.conn, (const double2*)J.xy, J.kappa, J.Q,
+                          J.straight, tab, J.kstore, J.fstore);
 }
 
 static size_t heat_smem(int nn, int nt) { return (size_t)(nn == 3 ? 6 + 3 : 21 + 6) * (nt + 1) * sizeof(double); }
 
 int launch_heat(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* xy, const double* kappa, double Q,
-                const QPTab& tab, double* kstore, double* fstore) {
+                const uint8_t* straight, const QPTab& tab, double* kstore, double* fstore) {
   if (nel == 0) return ELFEL_OK;
   const unsigned grid = grid_for(nel, kIntThreads);
+  const double2* p = (const double2*)xy;
+  const size_t sm = heat_smem(nn, kIntThreads);
   if (nn == 3)
-    heat_k<3><<<grid, kIntThreads, heat_smem(3, kIntThreads), c->stream>>>(nel, conn, (const double2*)xy, kappa, Q,
-                                                                          tab, kstore, fstore);
+    heat_k<3, kPatGeneric><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, p, kappa, Q, straight, tab, kstore, fstore);
+  else if (heat_pattern(6, tab) == kPatT6)
+    heat_k<6, kPatT6><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, p, kappa, Q, straight, tab, kstore, fstore);
   else
-    heat_k<6><<<grid, kIntThreads, heat_smem(6, kIntThreads), c->stream>>>(nel, conn, (const double2*)xy, kappa, Q,
-                                                                          tab, kstore, fstore);
+    heat_k<6, kPatGeneric><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, p, kappa, Q, straight, tab, kstore, fstore);
   ELFEL_LAUNCH_CHECK(c);
   return ELFEL_OK;
 }
 
-template <int NN, int NT>
+template <int NN, int NT, int PAT>
 static void heat_batch_launch(Ctx* c, const HeatJob* jobs, int njobs, int64_t blocks, const QPTab& tab) {
   // T6 with 256-thread CTAs stages more than the default 48 KB of dynamic shared memory
-  cudaFuncSetAttribute(heat_batch_k<NN, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)heat_smem(NN, NT));
-  heat_batch_k<NN, NT><<<(unsigned)blocks, NT, heat_smem(NN, NT), c->stream>>>(jobs, njobs, tab);
+  cudaFuncSetAttribute(heat_batch_k<NN, NT, PAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)heat_smem(NN, NT));
+  heat_batch_k<NN, NT, PAT><<<(unsigned)blocks, NT, heat_smem(NN, NT), c->stream>>>(jobs, njobs, tab);
+}
+
+template <int NT>
+static void heat_batch_launch_nn(Ctx* c, int nn, const HeatJob* jobs, int njobs, int64_t blocks, const QPTab& tab) {
+  if (nn == 3) heat_batch_launch<3, NT, kPatGeneric>(c, jobs, njobs, blocks, tab);
+  else if (heat_pattern(6, tab) == kPatT6) heat_batch_launch<6, NT, kPatT6>(c, jobs, njobs, blocks, tab);
+  else heat_batch_launch<6, NT, kPatGeneric>(c, jobs, njobs, blocks, tab);
 }
 
 int launch_heat_batch(Ctx* c, int nn, int nt, const HeatJob* jobs_dev, int njobs, int64_t blocks, const QPTab& tab) {
   if (njobs == 0 || blocks == 0) return ELFEL_OK;
   if (blocks > 0x7fffffff) return fail(c, ELFEL_ERR_ARG, "batched heat: too many elements");
   switch (nt) {
-    case 64: nn == 3 ? heat_batch_launch<3, 64>(c, jobs_dev, njobs, blocks, tab)
-                     : heat_batch_launch<6, 64>(c, jobs_dev, njobs, blocks, tab); break;
-    case 128: nn == 3 ? heat_batch_launch<3, 128>(c, jobs_dev, njobs, blocks, tab)
-                      : heat_batch_launch<6, 128>(c, jobs_dev, njobs, blocks, tab); break;
-    case 256: nn == 3 ? heat_batch_launch<3, 256>(c, jobs_dev, njobs, blocks, tab)
-                      : heat_batch_launch<6, 256>(c, jobs_dev, njobs, blocks, tab); break;
+    case 64: heat_batch_launch_nn<64>(c, nn, jobs_dev, njobs, blocks, tab); break;
+    case 128: heat_batch_launch_nn<128>(c, nn, jobs_dev, njobs, blocks, tab); break;
+    case 256: heat_batch_launch_nn<256>(c, nn, jobs_dev, njobs, blocks, tab); break;
     default: return fail(c, ELFEL_ERR_ARG, "batched heat: %d threads per CTA (64, 128 or 256)", nt);
   }
   ELFEL_LAUNCH_CHECK(c);

@@ -31,8 +31,13 @@ struct Mat3 {
 
 int make_tables(int nn, int npts, const double* pc, const double* w, QPTab* t);
 
+// straight: per-element straight-sided flags of the geometry (launch_straight;
+// unused for T3, whose elements always are).
 int launch_heat(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* xy, const double* kappa, double Q,
-                const QPTab& tab, double* kstore, double* fstore);
+                const uint8_t* straight, const QPTab& tab, double* kstore, double* fstore);
+// Per-element straight-sided flags (1: every midside node is the exact
+// midpoint of its edge) of a mesh; recomputed whenever the coordinates change.
+int launch_straight(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* xy, uint8_t* flag);
 
 // One mesh of a batched heat integration (device array, ordered by blk0).
 struct HeatJob {
@@ -41,6 +46,7 @@ struct HeatJob {
   const int32_t* conn;
   const double* xy;
   const double* kappa;
+  const uint8_t* straight;
   double Q;
   double* kstore;
   double* fstore;

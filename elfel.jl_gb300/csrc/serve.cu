@@ -248,6 +248,7 @@ int assemble_batch(elfel_server* s, const std::vector<Sys*>& ys) {
           j.conn = F.conn_u.p;
           j.xy = F.xy_u.p;
           j.kappa = F.coef.p;
+          j.straight = F.straight.p;
           j.Q = y->req.r.Q;
           j.kstore = F.kstore.p;
           j.fstore = F.fstore.p;

@@ -138,8 +138,10 @@ struct Fused {
   DBuf<double> pmass_diag;           // ndofs (nonzero at pressure DOFs only)
   int is_block = 0;                  // tables generated on the device from `block`
   elfel_block_desc block;
+  DBuf<uint8_t> straight;            // nel: 1 = straight-sided element (of the current coordinates)
   void release(Ctx* c) {
     is_block = 0;
+    straight.release(c);
     conn_u.release(c); conn_p.release(c); xy_u.release(c); dofs_u.release(c); dofs_p.release(c);
     zero_rows.release(c); coef.release(c); kstore.release(c); fstore.release(c);
     fpat.release(c); pmass_store.release(c); pmpat.release(c); pmass_diag.release(c);
