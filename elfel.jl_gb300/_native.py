@@ -158,6 +158,7 @@ SIGNATURES = {
     "elfel_ctx_tuning": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int,
                                         ctypes.POINTER(ctypes.c_int32)]),
     "elfel_ctx_fma_rate": (ctypes.c_int, [_vp, ctypes.c_int32, _dp]),
+    "elfel_error_l2": (ctypes.c_int, [_vp, _dp, ctypes.c_int32, _dp, ctypes.c_int32, _dp, _dp, _dp]),
     "elfel_fused_setup_block": (ctypes.c_int, [_vp, ctypes.POINTER(BlockDesc), _i64p, _i64p]),
     "elfel_block_dirichlet": (ctypes.c_int, [_vp, _dp, _dp]),
     "elfel_fused_tables": (ctypes.c_int, [_vp, _i64p, _dp, _i64p]),

@@ -267,6 +267,29 @@ class SysmatAssemblerGPU:
                                                        N.ptr(dofs, N._i64p)))
         return conn, xy, dofs
 
+    def error_l2(self, U, exact, space=0, npts=3):
+        """evaluate_pressure_error / evaluate_velocity_error of test/test_stokes.jl:438-496
+        on the device: the L2 norm of u_h - u_exact over space 0 (primary) or 1
+        (Taylor-Hood pressure).  exact: one dict {(a, b): c} per component, the
+        polynomial sum c x^a y^b of degree <= 4."""
+        from .refshapes import quadrature
+
+        if isinstance(exact, dict):
+            exact = [exact]
+        poly = np.zeros((len(exact), 15))
+        order = [(a, d - a) for d in range(5) for a in range(d, -1, -1)]
+        for k, terms in enumerate(exact):
+            for (a, b), v in terms.items():
+                poly[k, order.index((a, b))] = v
+        qr = quadrature(quadraturesettings={"npts": npts})
+        pc, w = N.f64(qr.param_coords), N.f64(qr.weights)
+        U = N.f64(U)
+        poly = N.f64(poly)
+        e = ctypes.c_double()
+        self._hd.check(self._hd.lib.elfel_error_l2(self._hd.h, N.ptr(U), int(space), N.ptr(poly), int(npts),
+                                                   N.ptr(pc), N.ptr(w), ctypes.byref(e)))
+        return e.value
+
     def _ensure(self, physics, elit, qpit, pelit=None):
         key = (id(elit.fesp), id(pelit.fesp) if pelit is not None else None, qpit.quadr.npts, physics, self.nrow)
         if key != self._setup_key:

@@ -213,6 +213,18 @@ ELFEL_API int elfel_fused_tables(elfel_sysmat* m, int64_t* conn, double* xy, int
 /* Sizes of a fused system: elements, nodes of the primary space, DOFs. */
 ELFEL_API int elfel_fused_dims(elfel_sysmat* m, int64_t* nel, int64_t* nnodes, int64_t* ndofs);
 
+/* ------------------------------------------------------------------ error integrals
+ * evaluate_pressure_error / evaluate_velocity_error of test/test_stokes.jl:438-496
+ * on the device: err = sqrt(sum_e sum_q w_q det J |u_h(x_q) - u_exact(x_q)|^2)
+ * over the elements of a fused system's space 0 (the primary space: 1 or 2
+ * components) or space 1 (the Taylor-Hood pressure, on the vertex triangles).
+ * U: the system vector (ndofs values, host).  poly: 15 coefficients per
+ * component of u_exact = sum c_ab x^a y^b, a + b <= 4, in the order
+ * (0,0),(1,0),(0,1),(2,0),(1,1),(0,2),(3,0),(2,1),(1,2),(0,3),(4,0),(3,1),(2,2),(1,3),(0,4).
+ * The quadrature rule is given as in elfel_fused_desc. */
+ELFEL_API int elfel_error_l2(elfel_sysmat* m, const double* U, int32_t space, const double* poly, int32_t npts,
+                   const double* qp_coords, const double* qp_weights, double* err);
+
 /* ------------------------------------------------------------------ solve */
 enum elfel_solver {
   ELFEL_PCG64 = 0,      /* Jacobi-PCG, all FP64 */
