@@ -14,8 +14,14 @@ reduction into the device CSC built once).  The JSON line reports
           upload of mesh, DOF table and coefficients, pattern build,
           assembly, download of the CSC and F, every step;
   pcg     the solve of the same system to relative residual 1e-10 with
-          FP64 Jacobi-PCG and with FP32 CG + FP64 residual replacement;
-  roofline / cpu_baseline / clocks as described in DESIGN.md.
+          FP64 Jacobi-PCG and with FP32 CG + FP64 residual replacement
+          (one system, and the same in the batched engine);
+  serve   the serving stream: capacity, p50/p99 latency at three arrival
+          rates, batched vs plain FP64 one request at a time;
+  roofline the dominant kernel's algorithmic bytes over its CUDA-event time
+          against the measured HBM copy peak, with its measured DRAM traffic;
+  cpu_baseline the CPU restatement of the reference path on the host cores;
+  clocks  SM clocks and throttle reasons sampled during the timed region.
 
 ``--impl reference`` times the CPU restatement of the reference path (the
 oracle: element loop, COO triplets, SparseArrays.sparse semantics) on the
@@ -239,9 +245,10 @@ class Clocks:
     def __init__(self, index=0):
         self.p = None
         self.window = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        import tempfile
+
+        self.path = os.path.join(tempfile.gettempdir(), f"elfel_clocks_{os.getpid()}.csv")
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={self.Q}", "--format=csv,noheader",
                                        "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
