@@ -14,14 +14,16 @@ from .batching import BatchSolver
 from .serving import HeatServer, heat_request
 from .feiterators import (FEIterator, QPIterator, bfun, bfungrad, bfungradpar, eldofcomps, eldofentmdims, eldofs,
                           eldofvals, elnodes, jacjac, location, weight)
-from .felements import FEH1_T3, FEH1_T6, Jacobian, nfeatofdim, ndofperfeat, refshape
+from .felements import (FEH1_L2, FEH1_Q4, FEH1_T3, FEH1_T3_BUBBLE, FEH1_T4, FEH1_T6, FEL2_Q4, FEL2_T3, FEL2_T4,
+                        Jacobian, manifdim, nfeatofdim, ndofperfeat, ndofsperel as fe_ndofsperel, refshape, shapedesc)
 from .fespaces import (FEField, FESpace, dofnum, doftype, edofbfnum, edofcompnt, edofmdim, gathersysvec,
                        highestdatadofnum, highestfreedofnum, makeattribute, ndofs, ndofsperel, numberdatadofs,
                        numberdofs, numberfreedofs, nunknowns, scattersysvec, setdofval, setebc)
 from .local_assemblers import LocalMatrixAssembler, LocalVectorAssembler, init, transpose
-from .meshes import (Mesh, T3block, T6block, T6toT3, boundary_edges, boundary_nodes, jitter, vselect,
-                     vselect_nearest)
-from .refshapes import IntegRule, RefShapeTriangle, quadrature
+from .meshes import (L2block, Mesh, Q4block, T3block, T4block, T6block, T6toT3, boundary_edges, boundary_nodes, jitter,
+                     vselect, vselect_nearest)
+from .refshapes import (IntegRule, RefShapeCube, RefShapeInterval, RefShapePoint, RefShapeSquare, RefShapeTetrahedron,
+                        RefShapeTriangle, npts, param_coords, quadrature, weights)
 from ._native import Context, ElfelError, NotConverged, default_context
 
 

@@ -104,9 +104,16 @@ class FEField:
 class FESpace:
     """Mesh + scalar FE x nfecopies components (src/FESpaces.jl:25-40).
 
-    For T3/T6 all DOFs live on the vertices of the element's shape (the base
-    incidence relation's nodes), so the space holds one FEField over the mesh
-    nodes (manifold dimension 0).
+    One FEField per manifold dimension m that carries DOFs
+    (ndofperfeat(fe, m) > 0; src/FESpaces.jl:73-83): m = 0 holds one term per
+    mesh node, m = manifdim(fe) one term per element (the identity incidence
+    relation of the cells, ``ir_identity`` in the reference's scripts).  The
+    library's elements carry no DOFs on edges or faces.
+
+    Fields are numbered in ascending m.  The reference iterates its
+    Dict{Int} of fields (src/FESpaces.jl:141-173), whose order for the keys
+    {0, 2} or {0, 3} is Julia's hash order; for spaces with a single field
+    (all nodal and all cell-constant elements) the two agree.
     """
 
     def __init__(self, T, mesh, fe: FE, nfecopies=1):
@@ -114,14 +121,27 @@ class FESpace:
         self.fe = fe
         self.nfecopies = int(nfecopies)
         self.T = T
-        if mesh.nodes_per_elem != fe.nodes_per_elem:
-            raise ValueError(f"mesh of {mesh.nodes_per_elem}-node cells for {fe}")
-        self._fields = {0: FEField(self.nfecopies, mesh.nnodes, dtype=T)}
+        if mesh.nodes_per_elem != fe.nodes_per_elem or (fe.shape != mesh.etype and mesh.etype in ("T3", "T6", "Q4",
+                                                                                                   "T4", "L2")):
+            raise ValueError(f"mesh of {mesh.etype} cells ({mesh.nodes_per_elem} nodes) for {fe}")
+        self._fields = {}
+        md = fe.manifdim()
+        for m in range(0, md + 1):
+            if fe.ndofperfeat(m) == 0:
+                continue
+            if m == 0:
+                nterms = mesh.nnodes
+            elif m == md:
+                nterms = mesh.nel
+            else:
+                raise NotImplementedError(f"DOFs on features of dimension {m} of {fe}")
+            self._fields[m] = FEField(self.nfecopies, nterms, dtype=T)  # one DOF per feature
         self._edofmdim, self._edofbfnum, self._edofcompnt = _number_edofs(fe, self.nfecopies)
 
     @property
     def field(self):
-        return self._fields[0]
+        """The nodal field (manifold dimension 0), or the only field of the space."""
+        return self._fields[0] if 0 in self._fields else next(iter(self._fields.values()))
 
     def ndofsperel(self):
         return self.fe.ndofsperel() * self.nfecopies
@@ -132,7 +152,7 @@ def _number_edofs(fe, nfecopies):
     emdim, bfnum, compnt = [], [], []
     bfn = 1
     for m in range(0, 4):
-        for _ in range(fe.nfeatofdim(m) if m <= 2 else 0):
+        for _ in range(fe.nfeatofdim(m)):
             for _k in range(fe.ndofperfeat(m)):
                 for j in range(1, nfecopies + 1):
                     emdim.append(m)
@@ -240,9 +260,10 @@ def scattersysvec(fesp, v):
 
 
 def makeattribute(fesp, name, comp):
-    """Node attribute of component(s) comp (1-based): returns nnodes x len(comp) values."""
+    """Attribute of component(s) comp (1-based) over the entities of the space's
+    first field (nodes, or cells for cell-constant elements): nterms x len(comp) values."""
     c = np.atleast_1d(np.asarray(comp)) - 1
-    vals = fesp._fields[0].dofvals[:, c]
+    vals = fesp.field.dofvals[:, c]
     if not hasattr(fesp.mesh, "attributes"):
         fesp.mesh.attributes = {}
     fesp.mesh.attributes[name] = vals

@@ -1,8 +1,9 @@
-"""Triangle block meshes and node selection.
+"""Block meshes (L2, T3, T6, Q4, T4) and node selection.
 
-The reference takes these from MeshSteward 1.1.3 (T3block, T6block, T6toT3,
-boundary/connectedv, vselect; used e.g. at Elfel.jl test/test_heat.jl:28-33 and
-test/test_stokes.jl:28-39), which is not vendored with it.  The conventions
+The reference takes these from MeshSteward 1.1.3 (L2block, T3block, T6block,
+T6toT3, Q4block, T4block, boundary/connectedv, vselect; used e.g. at Elfel.jl
+test/test_heat.jl:28-33, 143-148 and test/test_stokes.jl:28-39,
+examples/heat/poisson/t4.jl:24-30), which is not vendored with it.  The conventions
 below follow the reference's mesh fixtures (test/qmesh-conn.dat): nodes are
 numbered x-fastest, cells are visited with the x index outer and the y index
 inner, and each cell (n1, n2, n3, n4) = ((i,j), (i+1,j), (i+1,j+1), (i,j+1))
@@ -18,12 +19,18 @@ import numpy as np
 
 
 class Mesh:
-    """Connectivity (nel x nn, 1-based node numbers) plus node coordinates."""
+    """Connectivity (nel x nn, 1-based node numbers) plus node coordinates
+    (nnodes x sdim: 1 for L2 meshes, 2 for T3/T6/Q4, 3 for T4)."""
 
     def __init__(self, etype, conn, xy):
         self.etype = etype
         self.conn = np.ascontiguousarray(conn, dtype=np.int64)
-        self.xy = np.ascontiguousarray(xy, dtype=np.float64)
+        xy = np.asarray(xy, dtype=np.float64)
+        self.xy = np.ascontiguousarray(xy.reshape(xy.shape[0], -1))
+
+    @property
+    def sdim(self):
+        return self.xy.shape[1]
 
     @property
     def nel(self):
@@ -115,29 +122,90 @@ def T6toT3(mesh):
     return m
 
 
-def _edges(mesh):
+def Q4block(A, B, nx, ny):
+    """nx x ny bilinear quadrilaterals of [0,A] x [0,B]; cell (i,j) =
+    ((i,j), (i+1,j), (i+1,j+1), (i,j+1)) counter-clockwise, cells x outer /
+    y inner, nodes x-fastest (the T3block conventions without the split)."""
+    xs = np.linspace(0.0, A, nx + 1)
+    ys = np.linspace(0.0, B, ny + 1)
+    X, Y = np.meshgrid(xs, ys, indexing="xy")
+    xy = np.stack([X.ravel(), Y.ravel()], axis=1)
+    i, j, _ = _cells(nx, ny, "a")
+    nid = lambda a, b: b * (nx + 1) + a + 1
+    conn = np.stack([nid(i, j), nid(i + 1, j), nid(i + 1, j + 1), nid(i, j + 1)], axis=1)
+    return Mesh("Q4", conn, xy)
+
+
+def L2block(A, n):
+    """n two-node segments of [0, A] on the x axis (1-D coordinates)."""
+    x = np.linspace(0.0, A, n + 1).reshape(-1, 1)
+    k = np.arange(1, n + 1)
+    return Mesh("L2", np.stack([k, k + 1], axis=1), x)
+
+
+def T4block(A, B, C, nx, ny, nz):
+    """nx x ny x nz hexahedral cells of [0,A] x [0,B] x [0,C], each split into
+    the six tetrahedra around its (0,0,0)-(1,1,1) diagonal (Kuhn's
+    subdivision; every cell split the same way, so faces match).  Nodes
+    x-fastest, then y, then z; cells x outer, y, z inner; every tetrahedron
+    positively oriented."""
+    xs = np.linspace(0.0, A, nx + 1)
+    ys = np.linspace(0.0, B, ny + 1)
+    zs = np.linspace(0.0, C, nz + 1)
+    Z, Y, X = np.meshgrid(zs, ys, xs, indexing="ij")
+    xyz = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+    i, j, k = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    i, j, k = i.ravel(), j.ravel(), k.ravel()
+    nid = lambda a, b, c: (c * (ny + 1) + b) * (nx + 1) + a + 1
+    unit = np.eye(3, dtype=np.int64)
+    tets = []
+    # one tetrahedron per permutation (p, q, r) of the axes: the path
+    # 0 -> e_p -> e_p + e_q -> (1,1,1); odd permutations swap two vertices
+    for (p, q, r), odd in (((0, 1, 2), 0), ((0, 2, 1), 1), ((1, 0, 2), 1), ((1, 2, 0), 0), ((2, 0, 1), 0),
+                           ((2, 1, 0), 1)):
+        o = np.zeros(3, dtype=np.int64)
+        a = unit[p]
+        b = unit[p] + unit[q]
+        d = np.ones(3, dtype=np.int64)
+        vs = [nid(i + v[0], j + v[1], k + v[2]) for v in (o, a, b, d)]
+        if odd:
+            vs[1], vs[2] = vs[2], vs[1]
+        tets.append(np.stack(vs, axis=1))
+    conn = np.stack(tets, axis=1).reshape(-1, 4)
+    return Mesh("T4", conn, xyz)
+
+
+# Local boundary features of each cell: edges of 2-D cells, faces of
+# tetrahedra, end points of segments.  T6 edges list their midside node third.
+_FACETS = {
+    "L2": [[0], [1]],
+    "T3": [[0, 1], [1, 2], [2, 0]],
+    "T6": [[0, 1, 3], [1, 2, 4], [2, 0, 5]],
+    "Q4": [[0, 1], [1, 2], [2, 3], [3, 0]],
+    "T4": [[0, 2, 1], [0, 1, 3], [0, 3, 2], [1, 2, 3]],
+}
+
+
+def _facets(mesh):
+    """(facet vertex keys, all facet nodes) of every (cell, local facet), local facet outer."""
+    fl = _FACETS[mesh.etype]
     c = mesh.conn
-    e = np.concatenate([c[:, [0, 1]], c[:, [1, 2]], c[:, [2, 0]]], axis=0)
-    mids = c[:, 3:6].T.ravel() if c.shape[1] == 6 else None
-    return e, mids
+    nv = 2 if mesh.etype == "T6" else len(fl[0])
+    nodes = np.concatenate([c[:, f] for f in fl], axis=0)
+    return np.sort(nodes[:, :nv], axis=1), nodes
 
 
 def boundary_nodes(mesh):
-    """Nodes on edges used by exactly one element (connectedv(boundary(mesh))), 1-based, ascending."""
-    e, mids = _edges(mesh)
-    key = np.sort(e, axis=1)
+    """Nodes on facets used by exactly one cell (connectedv(boundary(mesh))), 1-based, ascending."""
+    key, nodes = _facets(mesh)
     _, inv, cnt = np.unique(key, axis=0, return_inverse=True, return_counts=True)
     on = cnt[inv.ravel()] == 1
-    nodes = [e[on].ravel()]
-    if mids is not None:
-        nodes.append(mids[on])
-    return np.unique(np.concatenate(nodes))
+    return np.unique(nodes[on].ravel())
 
 
 def boundary_edges(mesh):
-    """(element, local edge) pairs, 1-based, of the edges used by one element only."""
-    e, _ = _edges(mesh)
-    key = np.sort(e, axis=1)
+    """(element, local facet) pairs, 1-based, of the facets used by one element only."""
+    key, _ = _facets(mesh)
     _, inv, cnt = np.unique(key, axis=0, return_inverse=True, return_counts=True)
     on = np.nonzero(cnt[inv.ravel()] == 1)[0]
     nel = mesh.nel
@@ -145,10 +213,12 @@ def boundary_edges(mesh):
 
 
 def vselect(xy, box, inflate=0.0):
-    """Nodes inside box = [xmin, xmax, ymin, ymax] grown by inflate (1-based)."""
+    """Nodes inside box = [xmin, xmax, ymin, ymax(, zmin, zmax)] grown by inflate (1-based)."""
     b = np.asarray(box, dtype=np.float64).ravel()
-    x, y = xy[:, 0], xy[:, 1]
-    ok = (x >= b[0] - inflate) & (x <= b[1] + inflate) & (y >= b[2] - inflate) & (y <= b[3] + inflate)
+    xy = np.asarray(xy).reshape(len(xy), -1)
+    ok = np.ones(xy.shape[0], dtype=bool)
+    for d in range(min(xy.shape[1], b.size // 2)):
+        ok &= (xy[:, d] >= b[2 * d] - inflate) & (xy[:, d] <= b[2 * d + 1] + inflate)
     return np.nonzero(ok)[0] + 1
 
 
@@ -159,7 +229,7 @@ def vselect_nearest(xy, point):
 
 
 def jitter(mesh, amount, seed, curved=False):
-    """Move interior vertex nodes by a seeded uniform offset in [-amount, amount]^2.
+    """Move interior vertex nodes by a seeded uniform offset in [-amount, amount]^sdim.
 
     T6 midside nodes are then put back at the midpoints of their (moved)
     edges, which keeps the elements straight-sided; curved=True jitters the
@@ -169,9 +239,10 @@ def jitter(mesh, amount, seed, curved=False):
     xy = mesh.xy.copy()
     bnd = np.zeros(mesh.nnodes, dtype=bool)
     bnd[boundary_nodes(mesh) - 1] = True
-    verts = np.unique(mesh.conn[:, :3]) - 1
+    nv = 3 if mesh.etype == "T6" else mesh.nodes_per_elem
+    verts = np.unique(mesh.conn[:, :nv]) - 1
     inner = verts[~bnd[verts]]
-    xy[inner] += rng.uniform(-amount, amount, size=(inner.size, 2))
+    xy[inner] += rng.uniform(-amount, amount, size=(inner.size, mesh.sdim))
     if mesh.nodes_per_elem == 6:
         c = mesh.conn - 1
         for k in range(3):

@@ -16,6 +16,10 @@ Restated from the reference (Elfel.jl v0.4.0), file:line in that project:
   solve!                  test/test_heat.jl:73-76 (scipy SuperLU stands in
                           for SuiteSparse's factorisation behind ``\\``)
   error norms             test/test_stokes.jl:438-496, 716-760
+  Gauss / tetrahedron     src/RefShapes.jl:85-112, 248-281, 325-361
+  Q4, T4, T3 bubble, L2   src/FElements.jl:290-470 (numpy; the heat weak
+                          form of test/test_heat.jl:151-171 and
+                          examples/heat/poisson/t4.jl:32-52 over them)
 
 Parity is pinned by the golden vectors in tests/golden (extracted from the
 reference's own tests by tests/golden/make_golden.py).
@@ -85,6 +89,92 @@ def quadrature_triangle(npts=1):
     else:
         raise ValueError(f"Unknown number of integration points {npts}")
     return np.array(pc, dtype=np.float64), np.array(w, dtype=np.float64)
+
+
+def gauss_1d(order):
+    """Gauss rule on [-1, 1] (src/RefShapes.jl:85-112): the reference's
+    tabulated decimals up to order 5, Golub-Welsch above."""
+    tab = {1: ([0.0], [2.0]),
+           2: ([-0.577350269189626, 0.577350269189626], [1.0, 1.0]),
+           3: ([-0.774596669241483, 0.0, 0.774596669241483], [0.5555555555555556, 0.8888888888888889,
+                                                              0.5555555555555556]),
+           4: ([-0.86113631159405, -0.33998104358486, 0.33998104358486, 0.86113631159405],
+               [0.34785484513745, 0.65214515486255, 0.65214515486255, 0.34785484513745]),
+           5: ([-0.906179845938664, -0.538469310105683, 0.0, 0.538469310105683, 0.906179845938664],
+               [0.236926885056189, 0.478628670499367, 0.568888888888889, 0.478628670499367, 0.236926885056189])}
+    if order in tab:
+        x, w = tab[order]
+        return np.array(x), np.array(w)
+    k = np.arange(1, order, dtype=np.float64)
+    b = k / np.sqrt(4 * k * k - 1)
+    lam, V = np.linalg.eigh(np.diag(b, 1) + np.diag(b, -1))
+    return lam, 2 * V[0] ** 2
+
+
+def quadrature_square(order=1):
+    """Tensor-product Gauss rule, first coordinate outer (src/RefShapes.jl:325-361)."""
+    x, w = gauss_1d(order)
+    pc = np.array([[x[i], x[j]] for i in range(order) for j in range(order)])
+    return pc, np.array([w[i] * w[j] for i in range(order) for j in range(order)])
+
+
+def quadrature_tetrahedron(npts=1):
+    """src/RefShapes.jl:248-281 (npts = 1, 4, 5)."""
+    if npts == 1:
+        return np.array([[0.25, 0.25, 0.25]]), np.array([1.0 / 6.0])
+    if npts == 4:
+        a, b = 0.13819660, 0.58541020
+        return np.array([[a, a, a], [b, a, a], [a, b, a], [a, a, b]]), np.full(4, 1.0 / 24.0)
+    if npts == 5:
+        a = 1.0 / 6.0
+        pc = [[0.25, 0.25, 0.25], [0.5, a, a], [a, 0.5, a], [a, a, 0.5], [a, a, a]]
+        return np.array(pc), np.array([-0.8, 0.45, 0.45, 0.45, 0.45]) / 6
+    raise ValueError(f"Unknown number of integration points {npts}")
+
+
+def basis(kind, pc):
+    """(N, gradNpar) of one scalar element at one parametric point
+    (src/FElements.jl:199-470): kind in Q4, T4, T3B (T3 with bubble), L2."""
+    if kind == "Q4":
+        x, y = pc
+        N = 0.25 * np.array([(1 - x) * (1 - y), (1 + x) * (1 - y), (1 + x) * (1 + y), (1 - x) * (1 + y)])
+        G = 0.25 * np.array([[-(1 - y), -(1 - x)], [1 - y, -(1 + x)], [1 + y, 1 + x], [-(1 + y), 1 - x]])
+        return N, G
+    if kind == "T4":
+        r, s, t = pc
+        return np.array([1 - r - s - t, r, s, t]), np.array([[-1.0, -1, -1], [1, 0, 0], [0, 1, 0], [0, 0, 1]])
+    if kind == "T3B":
+        r, s = pc
+        N = np.array([1 - r - s, r, s, (1 - r - s) * r * s])
+        G = np.array([[-1.0, -1], [1, 0], [0, 1], [-r * s + (1 - r - s) * s, -r * s + (1 - r - s) * r]])
+        return N, G
+    if kind == "L2":
+        x = pc[0]
+        return np.array([(1 - x) / 2, (1 + x) / 2]), np.array([[-0.5], [0.5]])
+    raise ValueError(kind)
+
+
+def heat_element_matrices_iso(kind, pc, w, conn0, X, kappa, Q, nodes_geom=None):
+    """Heat element matrices (test/test_heat.jl:151-171) of an isoparametric
+    element over all elements at once, one quadrature point at a time:
+    J = X^T gradNpar (geometry from the first nodes_geom basis functions),
+    gradN = gradNpar J^-1, ke += gradN gradN^T kappa J w, fe += N Q J w."""
+    E, nn = conn0.shape
+    ng = nn if nodes_geom is None else nodes_geom
+    kappa = np.broadcast_to(np.asarray(kappa, dtype=np.float64), (E,))
+    Xe = X[conn0[:, :ng]]  # E x ng x sdim
+    nb = basis(kind, pc[0])[0].size
+    ke = np.zeros((E, nb, nb))
+    fe = np.zeros((E, nb))
+    for q in range(pc.shape[0]):
+        N, G = basis(kind, pc[q])
+        J = np.einsum("eka,kb->eab", Xe, G[:ng])  # E x sdim x mdim
+        det = np.linalg.det(J)
+        g = np.einsum("ib,eba->eia", G, np.linalg.inv(J))  # gradN = G J^-1
+        JxW = det * w[q]
+        ke += np.einsum("eia,eja->eij", g, g) * (kappa * JxW)[:, None, None]
+        fe += N[None, :] * (Q * JxW)[:, None]
+    return ke.transpose(0, 2, 1).reshape(E, nb * nb), fe  # column-major per element, as local_coo wants
 
 
 def bfun_tables(nn, pc):

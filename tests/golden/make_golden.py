@@ -22,6 +22,10 @@ Sources (file:line in the reference project):
   test/test_qpiterators.jl:22-61    basis values, gradients and weights
   test/test_refshapes.jl:26-29      3-point triangle rule
   test/test_fefields.jl:13-52       numbering counts on mt3gen3
+  test/test_refshapes.jl:1-146      interval, square, triangle, tetrahedron rules
+  test/test_felements.jl:1-158      L2, T4, FEL2_Q4, FEL2_T4, FEL2_T3 elements
+  test/test_fespaces.jl:85-172      T3 with a bubble: features, DOF layout
+  test/test_heat.jl:120-220         Q4 heat: N, quadrature, unknowns, nodal error
   test/qmesh*.dat, test/mt3gen3*.dat  mesh fixtures (data files)
 """
 import json
@@ -178,6 +182,98 @@ def fefields():
     }
 
 
+def _module(text, name):
+    start = text.index("module " + name + "\n")
+    end = text.find("\nmodule ", start + 8)
+    return text[start:end if end >= 0 else len(text)]
+
+
+def _after(text, anchor):
+    """Body of the first bracketed literal after anchor."""
+    body, _ = block_after(text, text.index(anchor) + len(anchor))
+    return body
+
+
+def terms(s):
+    """Comma/space separated literal terms, each a number or a product or
+    quotient of numbers (e.g. '2*0.3333', '1/4')."""
+    out = []
+    for t in re.split(r"[,\s;]+", s.strip()):
+        if not t:
+            continue
+        if not re.fullmatch(r"[-+0-9.eE*/]+", t):
+            raise ValueError(t)
+        v = None
+        for k, part in enumerate(re.split(r"([*/])", t)):
+            if k == 0:
+                v = float(part)
+            elif k % 2 == 1:
+                op = part
+            else:
+                v = v * float(part) if op == "*" else v / float(part)
+        out.append(v)
+    return out
+
+
+def elements():
+    rs = read("test/test_refshapes.jl")
+    m1, m3, m5 = _module(rs, "mrs1"), _module(rs, "mrs3"), _module(rs, "mrs5")
+    m6, m7 = _module(rs, "mrs6"), _module(rs, "mrs7")
+    tet = []
+    pos = 0
+    for _ in range(3):
+        n = int(re.search(r"@test npts\(qr\) == (\d+)", m6[pos:]).group(1))
+        pc, pos = block_after(m6, m6.index("param_coords(qr),", pos) + len("param_coords(qr),"))
+        wt, pos = block_after(m6, m6.index("weights(qr),", pos) + len("weights(qr),"))
+        tet.append({"npts": n, "param_coords": julia_matrix(pc), "weights": terms(wt)})
+    fe = read("test/test_felements.jl")
+    f1 = _module(fe, "mfes1")
+    l2 = f1[f1.index("fe = FEH1_L2()"):]
+    f2 = _module(fe, "mfes2")
+    counts = {}
+    for mod in ("mfes2", "mfes3", "mfes4"):
+        parts = re.split(r"fe = (FE\w+)\(\)", _module(fe, mod))[1:]
+        for k in range(0, len(parts), 2):
+            body = parts[k + 1]
+            counts[parts[k]] = {
+                "nfeatofdim": [int(x) for x in re.findall(r"nfeatofdim\(fe, \d\) == (\d+)", body)],
+                "ndofperfeat": [int(x) for x in re.findall(r"ndofperfeat\(fe, \d\) == (\d+)", body)],
+                "bfun": terms(_after(body, "isapprox(bfun(fe, [" + body.split("isapprox(bfun(fe, [")[1].split("]")[0]
+                                     + "]),")),
+            }
+    fs = read("test/test_fespaces.jl")
+    fb = fs[fs.index("FESpace(Float64, mesh, FEH1_T3_BUBBLE(), 1)"):]
+    fb = fb[:fb.index("FESpace(Float64, mesh, FEH1_T3_BUBBLE(), 2)")]
+    ht = read("test/test_heat.jl")
+    hq = ht[ht.index("module m_heat_poisson_q4"):]
+    return {
+        "source": "test/test_refshapes.jl, test/test_felements.jl, test/test_fespaces.jl:85-172, "
+                  "test/test_heat.jl:120-220",
+        "interval_default_npts": int(re.search(r"@test npts\(qr\) == (\d+)", m1).group(1)),
+        "interval_order3": {"param_coords": terms(_after(m1, "param_coords(qr),")),
+                            "weights": terms(_after(m1, "weights(qr),"))},
+        "square_order2_point3": terms(_after(m3, "param_coords(qr)[3, :]),")),
+        "square_orders": [int(x) for x in re.search(r"for o in (\d+):(\d+)", _module(rs, "mrs4")).groups()],
+        "triangle_npts": [int(x) for x in re.search(r"for n in \[([^\]]*)\]", m5).group(1).split(",")],
+        "tetrahedron": tet,
+        "interval_exp_integrals": terms(_after(m7, "reference_results =")),
+        "L2": {"bfun_at_one_third": terms(_after(l2, "bfun(fe, [1/3]),")),
+               "gradpar": [terms(_after(l2, "g[1],")), terms(_after(l2, "g[2],"))]},
+        "T4_gradpar": [terms(b) for b in re.findall(r"isapprox\(g\[\d\], \[([^\]]*)\]", f2)],
+        "counts": counts,
+        "bubble": {"nfeatofdim": [int(x) for x in re.findall(r"nfeatofdim\(fesp.fe, \d\) == (\d+)", fb)],
+                   "ndofperfeat": [int(x) for x in re.findall(r"ndofperfeat\(fesp.fe, \d\) == (\d+)", fb)],
+                   "ndofsperel": int(re.search(r"ndofsperel\(fesp.fe\) == (\d+)", fb).group(1)),
+                   "bfun_at_one_third": terms(_after(fb, "bfun(fesp.fe, [1/3, 1/3]),"))},
+        "heat_q4": {"N": int(re.search(r"\nN = (\d+);", hq).group(1)),
+                    "order": int(re.search(r"kind = :Gauss, order = (\d+)", hq).group(1)),
+                    "nunknowns": int(re.search(r"nunknowns\(fesp\) == (\d+)", hq).group(1)),
+                    "kappa": float(re.search(r"kappa =\s*(" + NUM + ")", hq).group(1)),
+                    "Q": float(re.search(r"Q = (" + NUM + ")", hq).group(1)),
+                    "mean_nodal_error_max": float(re.search(r"<= (" + NUM + ")", hq).group(1))},
+    }
+
+
 def datfile(rel):
     return [numbers(line) for line in read(rel).splitlines() if line.strip()]
 
@@ -192,6 +288,7 @@ def main():
         "stokes.json": stokes(),
         "qpiterators.json": qpiterators(),
         "fefields.json": fefields(),
+        "elements.json": elements(),
         "meshes.json": {
             "source": "test/qmesh-xyz.dat, test/qmesh-conn.dat, test/mt3gen3-xyz.dat, test/mt3gen3-conn.dat",
             "qmesh_xyz": datfile("test/qmesh-xyz.dat"),
