@@ -165,14 +165,49 @@ def build_cavity(E, N):
     return vmesh, pmesh, ufesp, pfesp
 
 
+def build_shape_problem(E, kind, N, seed=20261203, jit=0.2):
+    """Heat on a Q4 block (N x N cells of the unit square) or a T4 block (N^3
+    cubes of the unit cube, 6 tetrahedra each): vertices jittered +-jit*h,
+    kappa log-uniform [0.5, 2] per element, T = 1 + x^2 + 2 y^2 on the boundary."""
+    mesh = E.Q4block(1.0, 1.0, N, N) if kind == "Q4" else E.T4block(1.0, 1.0, 1.0, N, N, N)
+    mesh = E.jitter(mesh, jit / N, seed=seed)
+    fesp = E.FESpace(float, mesh, E.FEH1_Q4() if kind == "Q4" else E.FEH1_T4())
+    bn = E.boundary_nodes(mesh)
+    x, y = mesh.xy[bn - 1, 0], mesh.xy[bn - 1, 1]
+    E.setebc(fesp, 0, bn, 1, 1.0 + x ** 2 + 2.0 * y ** 2)
+    E.numberdofs(fesp)
+    rng = np.random.default_rng(seed + 1)
+    kappa = np.exp(rng.uniform(np.log(0.5), np.log(2.0), mesh.nel))
+    return mesh, fesp, kappa
+
+
 def problem_bench(E, ctx, args):
-    """Elasticity (plane strain T6) or Stokes (Taylor-Hood cavity) at scale:
-    fused assembly rate, and the FP64 vs FP32-refinement solves."""
+    """Elasticity (plane strain T6), Stokes (Taylor-Hood cavity) or heat on
+    Q4 / T4 meshes at scale: fused assembly rate, and the FP64 vs
+    FP32-refinement solves."""
     import torch
 
     stream = torch.cuda.ExternalStream(ctx.stream())
     t0 = time.perf_counter()
-    if args.problem == "elasticity":
+    alg = None
+    if args.problem in ("heat-q4", "heat-t4"):
+        kind = "Q4" if args.problem == "heat-q4" else "T4"
+        N = args.n or (1414 if kind == "Q4" else 70)
+        mesh, fesp, kappa = build_shape_problem(E, kind, N)
+        n, nu = E.ndofs(fesp), E.nunknowns(fesp)
+        qs = {"kind": "Gauss", "order": 2} if kind == "Q4" else {"npts": 1}
+        elit, qpit = E.FEIterator(fesp), E.QPIterator(fesp, qs)
+        am = E.start(E.SysmatAssemblerGPU(ctx), n, n)
+        E.assemble_heat(am, elit, qpit, kappa, -6.0)  # set-up and coefficient upload
+        step = lambda: am.heat(None, -6.0)
+        methods, rtol = ("pcg64", "pcg32_ir"), 1e-10
+        sd = mesh.sdim
+        # compulsory bytes of one integration launch: conn 16 + coordinates + kappa 8 + records 14 x 8
+        alg = {"integrate_heat": mesh.nel * (16 + 8 + 14 * 8) + mesh.nnodes * 8 * sd}
+        work = (f"heat {kind} {'x'.join([str(N)] * (2 if kind == 'Q4' else 3))} ({mesh.nel} elements, {n} DOFs), "
+                f"{'2x2 Gauss' if kind == 'Q4' else '1-point rule'}, fused K+F assembly, pattern reused")
+        spaces = fesp
+    elif args.problem == "elasticity":
         nx = args.n or 1000
         mesh, fesp, bforce, right = build_elasticity(E, nx, nx // 2)
         n, nu = E.ndofs(fesp), E.nunknowns(fesp)
@@ -197,30 +232,47 @@ def problem_bench(E, ctx, args):
     host_s = time.perf_counter() - t0
     step()  # set-up (tables, pattern) and a first assembly
     ctx.synchronize()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
+            flush.zero_()
             step()
         torch.cuda.synchronize()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
+        ctx.profile(True)
+        evs = []
         for _ in range(args.steps):
+            flush.zero_()  # L2 (129 MB) flushed between timed steps
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
             step()
-        b.record(stream)
+            b.record(stream)
+            evs.append((a, b))
         torch.cuda.synchronize()
-    t_asm = a.elapsed_time(b) / 1e3 / args.steps
-    U0 = np.zeros(n)
-    E.gathersysvec(U0, spaces)
-    sols = {}
-    for m in methods:
-        U = U0.copy()
-        st = am.solve(U, nu, None, method=m, rtol=rtol, maxit=500000)
-        sols[m] = (st, U)
-    (s64, U64), (s32, U32) = sols[methods[0]], sols[methods[1]]
+        phases = ctx.phases()
+        ctx.profile(False)
+    t_asm = sum(a.elapsed_time(b) for a, b in evs) / 1e3 / args.steps
+    per = {k: (ms / cnt if cnt else 0.0) for k, (ms, cnt) in phases.items()}
+    kernels = {k: {"ms_per_launch": v, "share": v / sum(per.values())} for k, v in per.items()}
+    if alg:
+        hbm, peak_kind = read_peaks()
+        for k, b in alg.items():
+            if per.get(k):
+                kernels[k].update({"alg_bytes": b, "gbs": b / (per[k] * 1e-3) / 1e9,
+                                   "frac": b / (per[k] * 1e-3) / 1e9 / hbm, "peak": hbm, "peak_kind": peak_kind})
     out = {"problem": args.problem, "workload": work, "elements": mesh.nel, "ndofs": n, "nunknowns": nu,
            "assembly_elements_per_s": mesh.nel / t_asm, "assembly_ms": t_asm * 1e3, "host_setup_s": host_s,
-           "rtol": rtol, methods[0]: s64, methods[1]: s32, "speedup": s64["seconds"] / s32["seconds"],
-           "fp32_vs_fp64_rel_err_max": float(np.abs(U32[:nu] - U64[:nu]).max() / np.abs(U64[:nu]).max()),
-           "data": "synthetic (seeded)"}
+           "kernels": kernels, "l2": "256 MB buffer written between timed steps", "data": "synthetic (seeded)"}
+    if not args.no_pcg:
+        U0 = np.zeros(n)
+        E.gathersysvec(U0, spaces)
+        sols = {}
+        for m in methods:
+            U = U0.copy()
+            st = am.solve(U, nu, None, method=m, rtol=rtol, maxit=500000)
+            sols[m] = (st, U)
+        (s64, U64), (s32, U32) = sols[methods[0]], sols[methods[1]]
+        out.update({"rtol": rtol, methods[0]: s64, methods[1]: s32, "speedup": s64["seconds"] / s32["seconds"],
+                    "fp32_vs_fp64_rel_err_max": float(np.abs(U32[:nu] - U64[:nu]).max() / np.abs(U64[:nu]).max())})
     print(json.dumps(out), flush=True)
     del am
     return 0
@@ -385,8 +437,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=None, help="cells per side (heat, elasticity: 1000; Stokes: 600)")
-    ap.add_argument("--problem", default="heat", choices=["heat", "elasticity", "stokes"],
-                    help="heat: the contract line; elasticity / stokes: assembly rate and solves at scale")
+    ap.add_argument("--problem", default="heat", choices=["heat", "elasticity", "stokes", "heat-q4", "heat-t4"],
+                    help="heat: the contract line; elasticity / stokes / heat-q4 / heat-t4: assembly rate and "
+                         "solves at scale")
     ap.add_argument("--no-pcg", action="store_true")
     ap.add_argument("--pcg-methods", default="pcg64,pcg32_ir", help="solves to run, in order")
     ap.add_argument("--no-cpu", action="store_true")
@@ -503,9 +556,9 @@ def main():
     asm_bytes = nel * 6 * 4 + mesh.nnodes * 16 + nel * 8 + nnz_est * 8 + n * 8
     ach = alg[dom] / (per[dom] * 1e-3) / 1e9
     # DRAM traffic of one heat_k<6> launch (dram__bytes_read.sum + dram__bytes_write.sum) measured
-    # with ncu on the 700 x 700 case of this workload (980,000 elements: 63.04 + 152.40 MB), scaled
+    # with ncu on the 700 x 700 case of this workload (980,000 elements: 63.98 + 152.87 MB), scaled
     # by the element count; writes still dirty in L2 when the kernel ends are not counted
-    HEAT_K_TRAFFIC_PER_ELEMENT = (63.04128e6 + 152.398592e6) / 980000
+    HEAT_K_TRAFFIC_PER_ELEMENT = (63.97568e6 + 152.874496e6) / 980000
     traffic = HEAT_K_TRAFFIC_PER_ELEMENT * nel if dom == "integrate_heat" else None
     roofline = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
                 "traffic": traffic, "kernel": dom, "peak_kind": peak_kind,

@@ -26,6 +26,10 @@ ELFEL_HEAT = 1
 ELFEL_ELASTICITY = 2
 ELFEL_STOKES = 3
 
+ELFEL_SHAPE_TRIANGLE = 0
+ELFEL_SHAPE_Q4 = 1
+ELFEL_SHAPE_T4 = 2
+
 ELFEL_PCG64 = 0
 ELFEL_PCG32_IR = 1
 ELFEL_MINRES64 = 2
@@ -64,7 +68,8 @@ class Space(ctypes.Structure):
 
 class FusedDesc(ctypes.Structure):
     _fields_ = [("physics", ctypes.c_int32), ("npts", ctypes.c_int32), ("qp_coords", _dp), ("qp_weights", _dp),
-                ("ndofs", ctypes.c_int64), ("u", Space), ("p", Space)]
+                ("ndofs", ctypes.c_int64), ("u", Space), ("p", Space), ("shape", ctypes.c_int32),
+                ("sdim", ctypes.c_int32)]
 
 
 class SolveStats(ctypes.Structure):

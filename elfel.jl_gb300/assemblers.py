@@ -174,6 +174,21 @@ _SOLVERS = {"pcg64": N.ELFEL_PCG64, "pcg32_ir": N.ELFEL_PCG32_IR, "minres64": N.
             "minres32_ir": N.ELFEL_MINRES32_IR}
 
 
+def _shape_of(fesp):
+    """(enum elfel_shape, coordinates per node) of a space the fused kernels take."""
+    from . import felements as fel
+
+    fe = fesp.fe
+    if type(fe) in (fel.FEH1_T3, fel.FEH1_T6):
+        return N.ELFEL_SHAPE_TRIANGLE, 2
+    if type(fe) is fel.FEH1_Q4:
+        return N.ELFEL_SHAPE_Q4, 2
+    if type(fe) is fel.FEH1_T4:
+        return N.ELFEL_SHAPE_T4, 3
+    raise N.ElfelError(N.ELFEL_ERR_UNSUPPORTED, f"fused device assembly takes FEH1_T3, FEH1_T6, FEH1_Q4 and FEH1_T4 "
+                                                f"spaces, not {fe}: assemble it with SysmatAssemblerSparse")
+
+
 def _space_struct(elit: FEIterator, keep):
     fesp = elit.fesp
     mesh = fesp.mesh
@@ -217,7 +232,8 @@ class SysmatAssemblerGPU:
         w = N.f64(qr.weights)
         keep.extend([pc, w])
         n = int(ndofs if ndofs is not None else self.nrow)
-        d = N.FusedDesc(physics, qr.npts, N.ptr(pc), N.ptr(w), n, u, p)
+        shape, sdim = _shape_of(elit.fesp)
+        d = N.FusedDesc(physics, qr.npts, N.ptr(pc), N.ptr(w), n, u, p, shape, sdim)
         self._hd.check(self._hd.lib.elfel_fused_setup(self._hd.h, ctypes.byref(d)))
         self._keep = keep
         self.physics = physics
@@ -225,6 +241,7 @@ class SysmatAssemblerGPU:
         self.nel = elit.fesp.mesh.nel
         self._nn = elit.fesp.mesh.nodes_per_elem
         self._nedof = self._nn * elit.fesp.nfecopies
+        self._sdim = sdim
         self._setup_key = (id(elit.fesp), id(pelit.fesp) if pelit is not None else None, qr.npts, physics, n)
         return self
 
@@ -245,6 +262,7 @@ class SysmatAssemblerGPU:
         self.nrow = self.ncol = n.value
         self.nel = 2 * int(nx) * int(ny)
         self._nn = self._nedof = 3 if etype == "T3" else 6
+        self._sdim = 2
         self._setup_key = ("block", etype, nx, ny, lx, ly, orientation, npts)
         return n.value, nu.value
 
@@ -262,7 +280,7 @@ class SysmatAssemblerGPU:
                                                      ctypes.byref(nd)))
         conn = np.empty((nel.value, self._nn), dtype=np.int64)
         dofs = np.empty((nel.value, self._nedof), dtype=np.int64)
-        xy = np.empty((nnodes.value, 2))
+        xy = np.empty((nnodes.value, self._sdim))
         self._hd.check(self._hd.lib.elfel_fused_tables(self._hd.h, N.ptr(conn, N._i64p), N.ptr(xy),
                                                        N.ptr(dofs, N._i64p)))
         return conn, xy, dofs

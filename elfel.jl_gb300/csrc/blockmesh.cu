@@ -185,7 +185,8 @@ int tables_to_host(Ctx* c, const Fused& F, int64_t* conn, double* xy, int64_t* e
     ELFEL_CUDA(c, cudaMemcpyAsync(eldofs, tmp.p, sizeof(int64_t) * nd, cudaMemcpyDeviceToHost, c->stream));
   }
   if (xy && F.nnodes_u)
-    ELFEL_CUDA(c, cudaMemcpyAsync(xy, F.xy_u.p, sizeof(double) * 2 * F.nnodes_u, cudaMemcpyDeviceToHost, c->stream));
+    ELFEL_CUDA(c, cudaMemcpyAsync(xy, F.xy_u.p, sizeof(double) * F.sdim * F.nnodes_u, cudaMemcpyDeviceToHost,
+                                  c->stream));
   ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
   tmp.release(c);
   return ELFEL_OK;

@@ -324,8 +324,8 @@ extern "C" int elfel_sysvec_assemble(elfel_ctx* h, int64_t nrow, const int64_t* 
 }
 
 // ------------------------------------------------------------------ fused
-static int upload_space(Ctx* c, const elfel_space& s, int64_t ndofs, DBuf<int32_t>* conn, DBuf<double>* xy,
-                        DBuf<int32_t>* dofs, const char* name) {
+static int upload_space(Ctx* c, const elfel_space& s, int64_t ndofs, int sdim, DBuf<int32_t>* conn,
+                        DBuf<double>* xy, DBuf<int32_t>* dofs, const char* name) {
   if (s.nel < 0 || s.nnodes < 0 || !s.conn || !s.eldofs || (s.nnodes > 0 && !s.xy))
     return fail(c, ELFEL_ERR_ARG, "%s space: missing arrays", name);
   const int nedof = s.nodes_per_elem * s.ncomp;
@@ -334,9 +334,10 @@ static int upload_space(Ctx* c, const elfel_space& s, int64_t ndofs, DBuf<int32_
   ELFEL_TRY(to_index32(c, s.conn, s.nel * s.nodes_per_elem, s.nnodes, conn, w1.c_str()));
   ELFEL_TRY(to_index32(c, s.eldofs, s.nel * nedof, ndofs, dofs, w2.c_str()));
   if (xy) {
-    ELFEL_TRY(xy->alloc(c, (size_t)(s.nnodes > 0 ? 2 * s.nnodes : 1)));
+    ELFEL_TRY(xy->alloc(c, (size_t)(s.nnodes > 0 ? sdim * s.nnodes : 1)));
     if (s.nnodes)
-      ELFEL_CUDA(c, cudaMemcpyAsync(xy->p, s.xy, sizeof(double) * 2 * s.nnodes, cudaMemcpyHostToDevice, c->stream));
+      ELFEL_CUDA(c, cudaMemcpyAsync(xy->p, s.xy, sizeof(double) * sdim * s.nnodes, cudaMemcpyHostToDevice,
+                                    c->stream));
   }
   return ELFEL_OK;
 }
@@ -348,9 +349,22 @@ extern "C" int elfel_fused_setup(elfel_sysmat* m, const elfel_fused_desc* d) {
   cudaSetDevice(c->device);
   if (d->ndofs < 0) return fail(c, ELFEL_ERR_ARG, "fused_setup: negative ndofs");
   const elfel_space& u = d->u;
-  if (u.nodes_per_elem != 3 && u.nodes_per_elem != 6)
-    return fail(c, ELFEL_ERR_UNSUPPORTED, "fused_setup: elements with %d nodes are not provided (T3, T6 only)",
-                u.nodes_per_elem);
+  const int sdim = d->sdim ? d->sdim : 2;
+  if (d->shape == ELFEL_SHAPE_TRIANGLE) {
+    if (u.nodes_per_elem != 3 && u.nodes_per_elem != 6)
+      return fail(c, ELFEL_ERR_UNSUPPORTED, "fused_setup: triangles with %d nodes are not provided (T3, T6 only)",
+                  u.nodes_per_elem);
+  } else if (d->shape == ELFEL_SHAPE_Q4 || d->shape == ELFEL_SHAPE_T4) {
+    if (u.nodes_per_elem != 4)
+      return fail(c, ELFEL_ERR_ARG, "fused_setup: %s elements have 4 nodes (got %d)",
+                  d->shape == ELFEL_SHAPE_Q4 ? "Q4" : "T4", u.nodes_per_elem);
+    if (d->physics != ELFEL_HEAT)
+      return fail(c, ELFEL_ERR_UNSUPPORTED, "fused_setup: Q4 and T4 elements take the heat weak form only");
+  } else {
+    return fail(c, ELFEL_ERR_ARG, "fused_setup: unknown element shape %d", d->shape);
+  }
+  if (sdim != (d->shape == ELFEL_SHAPE_T4 ? 3 : 2))
+    return fail(c, ELFEL_ERR_ARG, "fused_setup: %d coordinates per node for this element shape", sdim);
   if (d->npts < 1 || d->npts > kMaxQP || !d->qp_coords || !d->qp_weights)
     return fail(c, ELFEL_ERR_ARG, "fused_setup: quadrature with %d points (1..%d)", d->npts, kMaxQP);
   if (d->physics == ELFEL_HEAT && u.ncomp != 1)
@@ -367,16 +381,21 @@ extern "C" int elfel_fused_setup(elfel_sysmat* m, const elfel_fused_desc* d) {
   Fused& F = m->F;
   F.physics = d->physics;
   F.npts = d->npts;
+  F.shape = d->shape;
+  F.sdim = sdim;
   F.nn_u = u.nodes_per_elem;
   F.ncomp_u = u.ncomp;
   F.nel = u.nel;
   F.nnodes_u = u.nnodes;
-  ELFEL_TRY(make_tables(u.nodes_per_elem, d->npts, d->qp_coords, d->qp_weights, &F.tab));
-  ELFEL_TRY(upload_space(c, u, d->ndofs, &F.conn_u, &F.xy_u, &F.dofs_u, "primary"));
+  if (F.shape == ELFEL_SHAPE_TRIANGLE)
+    ELFEL_TRY(make_tables(u.nodes_per_elem, d->npts, d->qp_coords, d->qp_weights, &F.tab));
+  else
+    ELFEL_TRY(make_shape_tables(F.shape, d->npts, d->qp_coords, d->qp_weights, &F.stab));
+  ELFEL_TRY(upload_space(c, u, d->ndofs, sdim, &F.conn_u, &F.xy_u, &F.dofs_u, "primary"));
   if (d->physics == ELFEL_STOKES) {
     F.nn_p = 3;
     F.nnodes_p = d->p.nnodes;
-    ELFEL_TRY(upload_space(c, d->p, d->ndofs, &F.conn_p, nullptr, &F.dofs_p, "pressure"));
+    ELFEL_TRY(upload_space(c, d->p, d->ndofs, 2, &F.conn_p, nullptr, &F.dofs_p, "pressure"));
   }
   return fused_build(m, d->ndofs);
 }
@@ -445,7 +464,8 @@ int fused_build(elfel_sysmat* m, int64_t ndofs) {
     ELFEL_TRY(F.pmass_diag.alloc(c, (size_t)(ndofs > 0 ? ndofs : 1)));
   }
   ELFEL_TRY(F.straight.alloc(c, (size_t)(F.nel > 0 ? F.nel : 1)));
-  ELFEL_TRY(launch_straight(c, F.nn_u, F.nel, F.conn_u.p, F.xy_u.p, F.straight.p));
+  if (F.shape == ELFEL_SHAPE_TRIANGLE)
+    ELFEL_TRY(launch_straight(c, F.nn_u, F.nel, F.conn_u.p, F.xy_u.p, F.straight.p, &F.ncurved));
   ELFEL_TRY(F.kstore.alloc(c, (size_t)(F.nel * g.store_per_elem > 0 ? F.nel * g.store_per_elem : 1)));
   ELFEL_TRY(F.fstore.alloc(c, (size_t)(F.nel * nedof > 0 ? F.nel * nedof : 1)));
   ELFEL_TRY(m->vals.alloc(c, (size_t)(m->P.nnz > 0 ? m->P.nnz : 1)));
@@ -526,9 +546,10 @@ extern "C" int elfel_fused_set_geometry(elfel_sysmat* m, const double* xy) {
   if (!xy) return fail(c, ELFEL_ERR_ARG, "set_geometry: NULL coordinates");
   cudaSetDevice(c->device);
   if (m->F.nnodes_u)
-    ELFEL_CUDA(c, cudaMemcpyAsync(m->F.xy_u.p, xy, sizeof(double) * 2 * m->F.nnodes_u, cudaMemcpyHostToDevice,
-                                  c->stream));
-  return launch_straight(c, m->F.nn_u, m->F.nel, m->F.conn_u.p, m->F.xy_u.p, m->F.straight.p);
+    ELFEL_CUDA(c, cudaMemcpyAsync(m->F.xy_u.p, xy, sizeof(double) * m->F.sdim * m->F.nnodes_u,
+                                  cudaMemcpyHostToDevice, c->stream));
+  if (m->F.shape != ELFEL_SHAPE_TRIANGLE) return ELFEL_OK;
+  return launch_straight(c, m->F.nn_u, m->F.nel, m->F.conn_u.p, m->F.xy_u.p, m->F.straight.p, &m->F.ncurved);
 }
 
 static int finish_values(elfel_sysmat* m) {
@@ -557,8 +578,11 @@ extern "C" int elfel_fused_heat(elfel_sysmat* m, const double* kappa, double Q) 
     ELFEL_CUDA(c, cudaMemcpyAsync(F.coef.p, kappa, sizeof(double) * F.nel, cudaMemcpyHostToDevice, c->stream));
   {
     Phase ph(c, "integrate_heat");
-    ELFEL_TRY(launch_heat(c, F.nn_u, F.nel, F.conn_u.p, F.xy_u.p, F.coef.p, Q, F.straight.p, F.tab, F.kstore.p,
-                          F.fstore.p));
+    if (F.shape == ELFEL_SHAPE_TRIANGLE)
+      ELFEL_TRY(launch_heat(c, F.nn_u, F.nel, F.conn_u.p, F.xy_u.p, F.coef.p, Q, F.straight.p, F.ncurved, F.tab,
+                            F.kstore.p, F.fstore.p));
+    else
+      ELFEL_TRY(launch_heat_shape(c, F.stab, F.nel, F.conn_u.p, F.xy_u.p, F.coef.p, Q, F.kstore.p, F.fstore.p));
   }
   return finish_values(m);
 }

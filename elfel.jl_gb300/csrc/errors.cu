@@ -116,6 +116,8 @@ extern "C" int elfel_error_l2(elfel_sysmat* m, const double* U, int32_t space, c
   if (!U || !poly || !err || !qp_coords || !qp_weights) return fail(c, ELFEL_ERR_ARG, "error_l2: NULL argument");
   if (npts < 1 || npts > kMaxQP) return fail(c, ELFEL_ERR_ARG, "error_l2: quadrature with %d points", npts);
   const Fused& F = m->F;
+  if (F.shape != ELFEL_SHAPE_TRIANGLE)
+    return fail(c, ELFEL_ERR_UNSUPPORTED, "error_l2: triangle (T3/T6) spaces only");
   if (space != 0 && !(space == 1 && F.physics == ELFEL_STOKES))
     return fail(c, ELFEL_ERR_ARG, "error_l2: space 0, or 1 (pressure) of a Stokes system");
   cudaSetDevice(c->device);

@@ -165,7 +165,8 @@ constexpr int kPatGeneric = 0, kPatT6 = 1;
 // geometry, not per assembly.
 template <int NN>
 __global__ void straight_k(int64_t nel, const int32_t* __restrict__ conn, const double2* __restrict__ xy,
-                           uint8_t* __restrict__ flag) {
+                           uint8_t* __restrict__ flag, unsigned long long* __restrict__ ncurved) {
+  unsigned long long curved = 0;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nel; e += (int64_t)gridDim.x * blockDim.x) {
     Geo<NN> g;
 #pragma unroll
@@ -174,16 +175,31 @@ __global__ void straight_k(int64_t nel, const int32_t* __restrict__ conn, const 
       g.x[j] = p.x;
       g.y[j] = p.y;
     }
-    flag[e] = straight_sided<NN>(g) ? 1 : 0;
+    const bool s = straight_sided<NN>(g);
+    flag[e] = s ? 1 : 0;
+    curved += s ? 0 : 1;
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) curved += __shfl_down_sync(0xffffffffu, curved, o);
+  if ((threadIdx.x & 31) == 0 && curved) atomicAdd(ncurved, curved);
 }
 
-int launch_straight(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* xy, uint8_t* flag) {
+int launch_straight(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* xy, uint8_t* flag,
+                    int64_t* ncurved) {
+  *ncurved = 0;
   if (nel == 0) return ELFEL_OK;
+  DBuf<unsigned long long> cnt;
+  ELFEL_TRY(cnt.alloc(c, 1));
+  ELFEL_CUDA(c, cudaMemsetAsync(cnt.p, 0, sizeof(unsigned long long), c->stream));
   const unsigned grid = grid_for(nel, 256, (int64_t)c->sm_count * 16);
-  if (nn == 3) straight_k<3><<<grid, 256, 0, c->stream>>>(nel, conn, (const double2*)xy, flag);
-  else straight_k<6><<<grid, 256, 0, c->stream>>>(nel, conn, (const double2*)xy, flag);
+  if (nn == 3) straight_k<3><<<grid, 256, 0, c->stream>>>(nel, conn, (const double2*)xy, flag, cnt.p);
+  else straight_k<6><<<grid, 256, 0, c->stream>>>(nel, conn, (const double2*)xy, flag, cnt.p);
   ELFEL_LAUNCH_CHECK(c);
+  unsigned long long h = 0;
+  ELFEL_CUDA(c, cudaMemcpyAsync(&h, cnt.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+  cnt.release(c);
+  *ncurved = (int64_t)h;
   return ELFEL_OK;
 }
 
@@ -212,6 +228,54 @@ int heat_pattern(int nn, const QPTab& t) {
   return (m11 == kT6S11 && m22 == kT6S22 && m12 == kT6S12 && mp == kT6P) ? kPatT6 : kPatGeneric;
 }
 
+// Records of one straight-sided element from its three vertices (reference-
+// tensor form): ke = c11 S11 + c22 S22 + c12 (S12 + S21), fe = Q det P.
+template <int NN, int LD, int PAT>
+__device__ __forceinline__ void straight_record(double x0, double y0, double x1, double y1, double x2, double y2,
+                                                double kap, double Q, const double (*sS)[NN * (NN + 1) / 2],
+                                                const QPTab& tab, double* acc, double* fa, int t) {
+  constexpr int NS = NN * (NN + 1) / 2;
+  const double J11 = x1 - x0, J12 = x2 - x0;
+  const double J21 = y1 - y0, J22 = y2 - y0;
+  const double det = J11 * J22 - J21 * J12;
+  const double s = kap / det;
+  const double c11 = (J22 * J22 + J12 * J12) * s;
+  const double c22 = (J21 * J21 + J11 * J11) * s;
+  const double c12 = -(J22 * J21 + J12 * J11) * s;
+  const double qd = Q * det;
+  if (PAT == kPatT6) {
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      double a = 0.0;
+      if ((kT6S12 >> k) & 1u) a = c12 * sS[2][k];
+      if ((kT6S22 >> k) & 1u) a = fma(c22, sS[1][k], a);
+      if ((kT6S11 >> k) & 1u) a = fma(c11, sS[0][k], a);
+      acc[k * LD + t] = a;
+    }
+#pragma unroll
+    for (int j = 0; j < NN; ++j) fa[j * LD + t] = ((kT6P >> j) & 1u) ? qd * tab.P[j] : 0.0;
+  } else {
+#pragma unroll
+    for (int k = 0; k < NS; ++k) acc[k * LD + t] = c11 * sS[0][k] + c22 * sS[1][k] + c12 * sS[2][k];
+#pragma unroll
+    for (int j = 0; j < NN; ++j) fa[j * LD + t] = qd * tab.P[j];
+  }
+}
+
+// The reference tensors' stored entries (column-packed upper triangle) of a CTA.
+template <int NN, int NT>
+__device__ __forceinline__ void stage_tensors(const QPTab& tab, double (*sS)[NN * (NN + 1) / 2]) {
+  constexpr int NS = NN * (NN + 1) / 2;
+  for (int k = threadIdx.x; k < NS; k += NT) {
+    int j = 0;
+    while ((j + 1) * (j + 2) / 2 <= k) ++j;
+    int i = k - j * (j + 1) / 2;
+    sS[0][k] = tab.S[0][0][i * 6 + j];
+    sS[1][k] = tab.S[1][1][i * 6 + j];
+    sS[2][k] = tab.S[0][1][i * 6 + j] + tab.S[1][0][i * 6 + j];
+  }
+}
+
 // The NT elements e0 .. e0 + NT - 1 of one mesh, one per thread.  straight:
 // per-element flags (straight_k); PAT: the tensors' zero pattern.
 template <int NN, int NT, int PAT>
@@ -226,14 +290,7 @@ __device__ __forceinline__ void heat_elems(int64_t e0, int64_t nel, const int32_
   __shared__ int32_t sconn[NT * NN];
   __shared__ double sS[3][NS];
   stage_tables(tab, &st);
-  for (int k = threadIdx.x; k < NS; k += NT) {
-    int j = 0;
-    while ((j + 1) * (j + 2) / 2 <= k) ++j;
-    int i = k - j * (j + 1) / 2;
-    sS[0][k] = tab.S[0][0][i * 6 + j];
-    sS[1][k] = tab.S[1][1][i * 6 + j];
-    sS[2][k] = tab.S[0][1][i * 6 + j] + tab.S[1][0][i * 6 + j];
-  }
+  stage_tensors<NN, NT>(tab, sS);
   Geo<NN> g;
   load_geo<NN, NT>(conn, xy, e0, nel, sconn, g, nullptr);  // contains __syncthreads
   const int t = threadIdx.x;
@@ -242,31 +299,7 @@ __device__ __forceinline__ void heat_elems(int64_t e0, int64_t nel, const int32_
   if (e < nel) {
     const double kap = kappa[e];
     if (NN == 3 || straight[e]) {
-      const double J11 = g.x[1] - g.x[0], J12 = g.x[2] - g.x[0];
-      const double J21 = g.y[1] - g.y[0], J22 = g.y[2] - g.y[0];
-      const double det = J11 * J22 - J21 * J12;
-      const double s = kap / det;
-      const double c11 = (J22 * J22 + J12 * J12) * s;
-      const double c22 = (J21 * J21 + J11 * J11) * s;
-      const double c12 = -(J22 * J21 + J12 * J11) * s;
-      const double qd = Q * det;
-      if (PAT == kPatT6) {
-#pragma unroll
-        for (int k = 0; k < NS; ++k) {
-          double a = 0.0;
-          if ((kT6S12 >> k) & 1u) a = c12 * sS[2][k];
-          if ((kT6S22 >> k) & 1u) a = fma(c22, sS[1][k], a);
-          if ((kT6S11 >> k) & 1u) a = fma(c11, sS[0][k], a);
-          acc[k * LD + t] = a;
-        }
-#pragma unroll
-        for (int j = 0; j < NN; ++j) fa[j * LD + t] = ((kT6P >> j) & 1u) ? qd * tab.P[j] : 0.0;
-      } else {
-#pragma unroll
-        for (int k = 0; k < NS; ++k) acc[k * LD + t] = c11 * sS[0][k] + c22 * sS[1][k] + c12 * sS[2][k];
-#pragma unroll
-        for (int j = 0; j < NN; ++j) fa[j * LD + t] = qd * tab.P[j];
-      }
+      straight_record<NN, LD, PAT>(g.x[0], g.y[0], g.x[1], g.y[1], g.x[2], g.y[2], kap, Q, sS, tab, acc, fa, t);
     } else {
       double ke[NS], fe[NN];
 #pragma unroll
@@ -311,6 +344,41 @@ __device__ __forceinline__ void heat_elems(int64_t e0, int64_t nel, const int32_
   write_records<NT>(fa, NN, e0, nel, fstore);
 }
 
+// T6 meshes whose elements are all straight-sided (no curved element in the
+// geometry): only the three vertices are gathered and the per-point branch is
+// absent, which keeps the register count, and with it the occupancy, of the
+// triangle kernel.  Same records, bit for bit, as heat_k's straight branch.
+template <int PAT>
+__global__ void __launch_bounds__(kIntThreads) heat_t6s_k(int64_t nel, const int32_t* __restrict__ conn,
+                                                         const double2* __restrict__ xy,
+                                                         const double* __restrict__ kappa, double Q,
+                                                         const __grid_constant__ QPTab tab,
+                                                         double* __restrict__ kstore, double* __restrict__ fstore) {
+  constexpr int NN = 6, NS = 21, NT = kIntThreads, LD = NT + 1;
+  extern __shared__ double acc[];  // (NS + NN) * LD
+  __shared__ int32_t sconn[NT * NN];
+  __shared__ double sS[3][NS];
+  stage_tensors<NN, NT>(tab, sS);
+  const int64_t e0 = (int64_t)blockIdx.x * NT;
+  const int64_t base = e0 * NN, lim = nel * NN;
+  for (int k = threadIdx.x; k < NT * NN; k += NT) {
+    const int64_t gi = base + k;
+    sconn[k] = gi < lim ? __ldg(conn + gi) : 0;
+  }
+  __syncthreads();
+  const int t = threadIdx.x;
+  const int64_t e = e0 + t;
+  double* fa = acc + NS * LD;
+  if (e < nel) {
+    const double2 p0 = __ldg(xy + sconn[t * NN]), p1 = __ldg(xy + sconn[t * NN + 1]),
+                  p2 = __ldg(xy + sconn[t * NN + 2]);
+    straight_record<NN, LD, PAT>(p0.x, p0.y, p1.x, p1.y, p2.x, p2.y, kappa[e], Q, sS, tab, acc, fa, t);
+  }
+  write_records<NT>(acc, NS, e0, nel, kstore);
+  __syncthreads();
+  write_records<NT>(fa, NN, e0, nel, fstore);
+}
+
 template <int NN, int PAT>
 __global__ void __launch_bounds__(kIntThreads) heat_k(int64_t nel, const int32_t* __restrict__ conn,
                                                      const double2* __restrict__ xy, const double* __restrict__ kappa,
@@ -339,17 +407,211 @@ __global__ void __launch_bounds__(NT) heat_batch_k(const HeatJob* __restrict__ j
 static size_t heat_smem(int nn, int nt) { return (size_t)(nn == 3 ? 6 + 3 : 21 + 6) * (nt + 1) * sizeof(double); }
 
 int launch_heat(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* xy, const double* kappa, double Q,
-                const uint8_t* straight, const QPTab& tab, double* kstore, double* fstore) {
+                const uint8_t* straight, int64_t ncurved, const QPTab& tab, double* kstore, double* fstore) {
   if (nel == 0) return ELFEL_OK;
   const unsigned grid = grid_for(nel, kIntThreads);
   const double2* p = (const double2*)xy;
   const size_t sm = heat_smem(nn, kIntThreads);
   if (nn == 3)
     heat_k<3, kPatGeneric><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, p, kappa, Q, straight, tab, kstore, fstore);
+  else if (ncurved == 0 && heat_pattern(6, tab) == kPatT6)
+    heat_t6s_k<kPatT6><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, p, kappa, Q, tab, kstore, fstore);
+  else if (ncurved == 0)
+    heat_t6s_k<kPatGeneric><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, p, kappa, Q, tab, kstore, fstore);
   else if (heat_pattern(6, tab) == kPatT6)
     heat_k<6, kPatT6><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, p, kappa, Q, straight, tab, kstore, fstore);
   else
     heat_k<6, kPatGeneric><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, p, kappa, Q, straight, tab, kstore, fstore);
+  ELFEL_LAUNCH_CHECK(c);
+  return ELFEL_OK;
+}
+
+// ------------------------------------------------------------------ Q4 / T4 heat
+// The reference's integrate! loop (test/test_heat.jl:151-171,
+// examples/heat/poisson/t4.jl:32-52) with the quadrature sum kept per point:
+//   ke_ij += gradN_i . gradN_j * kappa * det J * w_q,  fe_j += N_j * Q * det J * w_q.
+// gradN = gradNpar J^-1 is written as adj(J)-rows / det J, so that
+//   ke_ij += (a_i . a_j) * kappa * w_q / det J   (a_i = gradNpar_i adj(J)).
+// Q4: J varies over the element; 2-D coordinates.  T4: J is constant, so the
+// sum over the points collapses to W = sum_q w_q; 3-D coordinates.
+int make_shape_tables(int shape, int npts, const double* pc, const double* w, ShapeTab* t) {
+  if (npts < 1 || npts > kMaxQP || (shape != ELFEL_SHAPE_Q4 && shape != ELFEL_SHAPE_T4)) return ELFEL_ERR_ARG;
+  memset(t, 0, sizeof(*t));
+  t->shape = shape;
+  t->npts = npts;
+  for (int q = 0; q < npts; ++q) {
+    t->w[q] = w[q];
+    t->W += w[q];
+    if (shape == ELFEL_SHAPE_Q4) {
+      const double x = pc[2 * q], y = pc[2 * q + 1];
+      const double N[4] = {0.25 * (1.0 - x) * (1.0 - y), 0.25 * (1.0 + x) * (1.0 - y), 0.25 * (1.0 + x) * (1.0 + y),
+                           0.25 * (1.0 - x) * (1.0 + y)};
+      const double G[4][2] = {{-(1.0 - y) * 0.25, -(1.0 - x) * 0.25},
+                              {(1.0 - y) * 0.25, -(1.0 + x) * 0.25},
+                              {(1.0 + y) * 0.25, (1.0 + x) * 0.25},
+                              {-(1.0 + y) * 0.25, (1.0 - x) * 0.25}};
+      for (int j = 0; j < 4; ++j) {
+        t->N[q][j] = N[j];
+        t->G[q][j][0] = G[j][0];
+        t->G[q][j][1] = G[j][1];
+      }
+    } else {
+      const double r = pc[3 * q], s = pc[3 * q + 1], u = pc[3 * q + 2];
+      t->N[q][0] = 1.0 - r - s - u;
+      t->N[q][1] = r;
+      t->N[q][2] = s;
+      t->N[q][3] = u;
+    }
+  }
+  for (int j = 0; j < 4; ++j) {
+    double P = 0.0;
+    for (int q = 0; q < npts; ++q) P += t->w[q] * t->N[q][j];
+    t->P[j] = P;
+  }
+  return ELFEL_OK;
+}
+
+constexpr int kShapeNS = 10;  // stored entries of a symmetric 4 x 4 element matrix
+
+template <int NT>
+__device__ __forceinline__ void load_conn4(const int32_t* __restrict__ conn, int64_t e0, int64_t nel, int32_t* sconn) {
+  const int64_t base = e0 * 4, lim = nel * 4;
+  for (int k = threadIdx.x; k < NT * 4; k += NT) {
+    const int64_t gi = base + k;
+    sconn[k] = gi < lim ? __ldg(conn + gi) : 0;
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kIntThreads) heat_q4_k(int64_t nel, const int32_t* __restrict__ conn,
+                                                        const double2* __restrict__ xy,
+                                                        const double* __restrict__ kappa, double Q,
+                                                        const __grid_constant__ ShapeTab tab,
+                                                        double* __restrict__ kstore, double* __restrict__ fstore) {
+  constexpr int NT = kIntThreads, LD = NT + 1;
+  __shared__ double acc[(kShapeNS + 4) * LD];
+  __shared__ int32_t sconn[NT * 4];
+  const int64_t e0 = (int64_t)blockIdx.x * NT;
+  load_conn4<NT>(conn, e0, nel, sconn);
+  const int t = threadIdx.x;
+  const int64_t e = e0 + t;
+  double* fa = acc + kShapeNS * LD;
+  if (e < nel) {
+    double x[4], y[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const double2 p = __ldg(xy + sconn[t * 4 + j]);
+      x[j] = p.x;
+      y[j] = p.y;
+    }
+    const double kap = kappa[e];
+    double ke[kShapeNS], fe[4];
+#pragma unroll
+    for (int k = 0; k < kShapeNS; ++k) ke[k] = 0.0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) fe[j] = 0.0;
+    for (int q = 0; q < tab.npts; ++q) {
+      double J11 = 0.0, J12 = 0.0, J21 = 0.0, J22 = 0.0;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        J11 = fma(x[j], tab.G[q][j][0], J11);
+        J12 = fma(x[j], tab.G[q][j][1], J12);
+        J21 = fma(y[j], tab.G[q][j][0], J21);
+        J22 = fma(y[j], tab.G[q][j][1], J22);
+      }
+      const double det = J11 * J22 - J21 * J12;
+      double u[4], v[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const double a = tab.G[q][j][0], b = tab.G[q][j][1];
+        u[j] = a * J22 - b * J21;
+        v[j] = b * J11 - a * J12;
+      }
+      const double cq = kap * tab.w[q] / det;
+      const double fq = Q * det * tab.w[q];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+#pragma unroll
+        for (int i = 0; i <= j; ++i) ke[j * (j + 1) / 2 + i] = fma(fma(u[i], u[j], v[i] * v[j]), cq, ke[j * (j + 1) / 2 + i]);
+        fe[j] = fma(tab.N[q][j], fq, fe[j]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kShapeNS; ++k) acc[k * LD + t] = ke[k];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) fa[j * LD + t] = fe[j];
+  }
+  write_records<NT>(acc, kShapeNS, e0, nel, kstore);
+  __syncthreads();
+  write_records<NT>(fa, 4, e0, nel, fstore);
+}
+
+__global__ void __launch_bounds__(kIntThreads) heat_t4_k(int64_t nel, const int32_t* __restrict__ conn,
+                                                        const double* __restrict__ xyz,
+                                                        const double* __restrict__ kappa, double Q,
+                                                        const __grid_constant__ ShapeTab tab,
+                                                        double* __restrict__ kstore, double* __restrict__ fstore) {
+  constexpr int NT = kIntThreads, LD = NT + 1;
+  __shared__ double acc[(kShapeNS + 4) * LD];
+  __shared__ int32_t sconn[NT * 4];
+  const int64_t e0 = (int64_t)blockIdx.x * NT;
+  load_conn4<NT>(conn, e0, nel, sconn);
+  const int t = threadIdx.x;
+  const int64_t e = e0 + t;
+  double* fa = acc + kShapeNS * LD;
+  if (e < nel) {
+    double X[4][3];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const double* p = xyz + 3 * (int64_t)sconn[t * 4 + j];
+      X[j][0] = __ldg(p);
+      X[j][1] = __ldg(p + 1);
+      X[j][2] = __ldg(p + 2);
+    }
+    // columns of J: d_a = x_a - x_0 (gradNpar of FEH1_T4 is [-1 -1 -1; I])
+    double d[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) d[a][k] = X[a + 1][k] - X[0][k];
+    // rows of adj(J): a_1 = d_2 x d_3, a_2 = d_3 x d_1, a_3 = d_1 x d_2; a_0 = -(a_1 + a_2 + a_3)
+    double A[4][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const double* p = d[(a + 1) % 3];
+      const double* r = d[(a + 2) % 3];
+      A[a + 1][0] = p[1] * r[2] - p[2] * r[1];
+      A[a + 1][1] = p[2] * r[0] - p[0] * r[2];
+      A[a + 1][2] = p[0] * r[1] - p[1] * r[0];
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) A[0][k] = -(A[1][k] + A[2][k] + A[3][k]);
+    const double det = d[0][0] * A[1][0] + d[0][1] * A[1][1] + d[0][2] * A[1][2];
+    const double c = kappa[e] * tab.W / det;
+    const double qd = Q * det;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+#pragma unroll
+      for (int i = 0; i <= j; ++i)
+        acc[(j * (j + 1) / 2 + i) * LD + t] = (A[i][0] * A[j][0] + A[i][1] * A[j][1] + A[i][2] * A[j][2]) * c;
+      fa[j * LD + t] = qd * tab.P[j];
+    }
+  }
+  write_records<NT>(acc, kShapeNS, e0, nel, kstore);
+  __syncthreads();
+  write_records<NT>(fa, 4, e0, nel, fstore);
+}
+
+int launch_heat_shape(Ctx* c, const ShapeTab& tab, int64_t nel, const int32_t* conn, const double* xy,
+                      const double* kappa, double Q, double* kstore, double* fstore) {
+  if (nel == 0) return ELFEL_OK;
+  const unsigned grid = grid_for(nel, kIntThreads);
+  if (tab.shape == ELFEL_SHAPE_Q4)
+    heat_q4_k<<<grid, kIntThreads, 0, c->stream>>>(nel, conn, (const double2*)xy, kappa, Q, tab, kstore, fstore);
+  else if (tab.shape == ELFEL_SHAPE_T4)
+    heat_t4_k<<<grid, kIntThreads, 0, c->stream>>>(nel, conn, xy, kappa, Q, tab, kstore, fstore);
+  else
+    return fail(c, ELFEL_ERR_ARG, "heat: unknown element shape %d", tab.shape);
   ELFEL_LAUNCH_CHECK(c);
   return ELFEL_OK;
 }

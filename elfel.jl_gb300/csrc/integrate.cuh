@@ -32,12 +32,15 @@ struct Mat3 {
 int make_tables(int nn, int npts, const double* pc, const double* w, QPTab* t);
 
 // straight: per-element straight-sided flags of the geometry (launch_straight;
-// unused for T3, whose elements always are).
+// unused for T3, whose elements always are); ncurved: the number of elements
+// without the flag (0 selects the straight-only T6 kernel).
 int launch_heat(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* xy, const double* kappa, double Q,
-                const uint8_t* straight, const QPTab& tab, double* kstore, double* fstore);
+                const uint8_t* straight, int64_t ncurved, const QPTab& tab, double* kstore, double* fstore);
 // Per-element straight-sided flags (1: every midside node is the exact
-// midpoint of its edge) of a mesh; recomputed whenever the coordinates change.
-int launch_straight(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* xy, uint8_t* flag);
+// midpoint of its edge) of a mesh and the count of curved elements;
+// recomputed whenever the coordinates change.  Synchronises the stream.
+int launch_straight(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* xy, uint8_t* flag,
+                    int64_t* ncurved);
 
 // One mesh of a batched heat integration (device array, ordered by blk0).
 struct HeatJob {
@@ -54,6 +57,24 @@ struct HeatJob {
 // All meshes of jobs_dev (same element type nn and tables) in one launch of
 // `blocks` CTAs of nt threads (64, 128 or 256; one element per thread).
 int launch_heat_batch(Ctx* c, int nn, int nt, const HeatJob* jobs_dev, int njobs, int64_t blocks, const QPTab& tab);
+// Quadrilateral and tetrahedron heat (FEH1_Q4, FEH1_T4).  Basis values and
+// parametric gradients at the rule's points (src/FElements.jl:290-320,
+// 357-386); P[j] = sum_q w_q N_j(q), W = sum_q w_q.
+struct ShapeTab {
+  int shape;  // ELFEL_SHAPE_Q4 or ELFEL_SHAPE_T4
+  int npts;
+  double w[kMaxQP];
+  double N[kMaxQP][4];
+  double G[kMaxQP][4][2];  // Q4 only (T4 gradients are constant)
+  double P[4];
+  double W;
+};
+int make_shape_tables(int shape, int npts, const double* pc, const double* w, ShapeTab* t);
+// Element records of the heat weak form on Q4 (xy: nnodes x 2) or T4 (xy:
+// nnodes x 3) meshes: kstore nel x 10 (upper triangle, column-packed), fstore nel x 4.
+int launch_heat_shape(Ctx* c, const ShapeTab& tab, int64_t nel, const int32_t* conn, const double* xy,
+                      const double* kappa, double Q, double* kstore, double* fstore);
+
 int launch_elasticity(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* xy, const Mat3& D,
                       const double* bforce, const QPTab& tab, double* kstore, double* fstore);
 int launch_traction(Ctx* c, int64_t ntrac, const int32_t* edges, const int32_t* conn, int nn, const double* xy,

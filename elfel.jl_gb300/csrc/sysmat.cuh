@@ -121,11 +121,14 @@ int to_index32(Ctx* c, const int64_t* src_host, int64_t n, int64_t limit, DBuf<i
 struct Fused {
   int physics = 0;
   int npts = 0;
-  QPTab tab;
+  int shape = ELFEL_SHAPE_TRIANGLE;  // enum elfel_shape of the primary space
+  int sdim = 2;                      // coordinates per node of the primary space
+  QPTab tab;                         // triangles
+  ShapeTab stab;                     // Q4 / T4
   int nn_u = 0, ncomp_u = 0, nn_p = 0;
   int64_t nel = 0, nnodes_u = 0, nnodes_p = 0;
   DBuf<int32_t> conn_u, conn_p;      // nel x nn, 0-based node ids
-  DBuf<double> xy_u;                 // nnodes x 2
+  DBuf<double> xy_u;                 // nnodes x sdim
   DBuf<int32_t> dofs_u, dofs_p;      // nel x nedof, 0-based DOFs
   DBuf<int32_t> zero_rows;           // nel x nedof zeros (row table of the rhs "matrix")
   DBuf<double> coef;                 // per-element coefficients
@@ -139,8 +142,12 @@ struct Fused {
   int is_block = 0;                  // tables generated on the device from `block`
   elfel_block_desc block;
   DBuf<uint8_t> straight;            // nel: 1 = straight-sided element (of the current coordinates)
+  int64_t ncurved = -1;              // elements without the flag (-1: not computed)
   void release(Ctx* c) {
     is_block = 0;
+    shape = ELFEL_SHAPE_TRIANGLE;
+    sdim = 2;
+    ncurved = -1;
     straight.release(c);
     conn_u.release(c); conn_p.release(c); xy_u.release(c); dofs_u.release(c); dofs_p.release(c);
     zero_rows.release(c); coef.release(c); kstore.release(c); fstore.release(c);

@@ -195,19 +195,30 @@ def _facets(mesh):
     return np.sort(nodes[:, :nv], axis=1), nodes
 
 
+def _single(key):
+    """Mask of the rows of key that occur once (lexicographic sort of the rows)."""
+    if key.shape[0] == 0:
+        return np.zeros(0, dtype=bool)
+    order = np.lexsort(key.T[::-1])
+    ks = key[order]
+    start = np.concatenate([[True], np.any(ks[1:] != ks[:-1], axis=1)])
+    grp = np.cumsum(start) - 1
+    cnt = np.bincount(grp)
+    once = np.empty(key.shape[0], dtype=bool)
+    once[order] = cnt[grp] == 1
+    return once
+
+
 def boundary_nodes(mesh):
     """Nodes on facets used by exactly one cell (connectedv(boundary(mesh))), 1-based, ascending."""
     key, nodes = _facets(mesh)
-    _, inv, cnt = np.unique(key, axis=0, return_inverse=True, return_counts=True)
-    on = cnt[inv.ravel()] == 1
-    return np.unique(nodes[on].ravel())
+    return np.unique(nodes[_single(key)].ravel())
 
 
 def boundary_edges(mesh):
     """(element, local facet) pairs, 1-based, of the facets used by one element only."""
     key, _ = _facets(mesh)
-    _, inv, cnt = np.unique(key, axis=0, return_inverse=True, return_counts=True)
-    on = np.nonzero(cnt[inv.ravel()] == 1)[0]
+    on = np.nonzero(_single(key))[0]
     nel = mesh.nel
     return np.stack([on % nel + 1, on // nel + 1], axis=1).astype(np.int64)
 

@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define ELFEL_ABI_VERSION 1
+#define ELFEL_ABI_VERSION 2
 
 #if defined(__GNUC__)
 #define ELFEL_API __attribute__((visibility("default")))
@@ -137,28 +137,37 @@ enum elfel_physics {
   ELFEL_STOKES = 3      /* test/test_stokes.jl:629-657, vector T6 velocity + T3 pressure */
 };
 
-/* One finite element space on a triangle mesh, flattened from the Julia
- * objects: the mesh connectivity and geometry (MeshCore incidence relation and
- * "geom" attribute) and the FEIterator DOF table (eldofs, src/FEIterators.jl:119,
+/* Cell shape of the primary space's elements. */
+enum elfel_shape {
+  ELFEL_SHAPE_TRIANGLE = 0, /* FEH1_T3 / FEH1_T6 by nodes_per_elem (src/FElements.jl:225-288) */
+  ELFEL_SHAPE_Q4 = 1,       /* FEH1_Q4, 4-node quadrilateral (src/FElements.jl:290-320) */
+  ELFEL_SHAPE_T4 = 2        /* FEH1_T4, 4-node tetrahedron, 3-D coordinates (src/FElements.jl:357-386) */
+};
+
+/* One finite element space, flattened from the Julia objects: the mesh
+ * connectivity and geometry (MeshCore incidence relation and "geom"
+ * attribute) and the FEIterator DOF table (eldofs, src/FEIterators.jl:119,
  * gathered by _storedofs!, src/FEIterators.jl:161-171). */
 typedef struct {
-  int32_t nodes_per_elem; /* 3 = FEH1_T3, 6 = FEH1_T6 (src/FElements.jl:225-288) */
+  int32_t nodes_per_elem; /* 3 = FEH1_T3, 6 = FEH1_T6, 4 = FEH1_Q4 or FEH1_T4 */
   int32_t ncomp;          /* nfecopies of the FESpace (src/FESpaces.jl:25-40) */
   int64_t nel;
   int64_t nnodes;
   const int64_t* conn;   /* nel x nodes_per_elem, 1-based node numbers, element-major */
-  const double* xy;      /* nnodes x 2 coordinates */
+  const double* xy;      /* nnodes x sdim coordinates (sdim of elfel_fused_desc; 2 for every space but T4) */
   const int64_t* eldofs; /* nel x (nodes_per_elem*ncomp) 1-based DOFs, node-major/component-minor */
 } elfel_space;
 
 typedef struct {
   int32_t physics;           /* enum elfel_physics */
-  int32_t npts;              /* quadrature points of the triangle rule */
-  const double* qp_coords;   /* npts x 2 parametric coordinates (src/RefShapes.jl:113-160) */
+  int32_t npts;              /* quadrature points of the rule */
+  const double* qp_coords;   /* npts x manifold-dimension parametric coordinates (src/RefShapes.jl:85-361) */
   const double* qp_weights;  /* npts weights */
   int64_t ndofs;             /* size of K (all spaces) */
   elfel_space u;             /* heat/elasticity space, or the Stokes velocity space */
   elfel_space p;             /* Stokes pressure space (nodes_per_elem = 3); else zeroed */
+  int32_t shape;             /* enum elfel_shape of u; Q4 and T4 take ELFEL_HEAT only */
+  int32_t sdim;              /* coordinates per node of u: 2, or 3 for T4 (0 means 2) */
 } elfel_fused_desc;
 
 /* Upload the mesh and DOF tables and build the CSC pattern and the

@@ -200,3 +200,33 @@ def test_fused_stokes_parity(E, O, gpu):
     assert close(K.data, K0.data)
     # explicit zeros of the cross-component couplings are in the pattern
     assert (K.data == 0.0).sum() > 0 and (K0.data == 0.0).sum() > 0
+
+
+def test_t6_straight_kernel_matches_general(E, gpu):
+    """A straight-sided T6 mesh takes the straight-only kernel; the same mesh
+    with one curved element takes the general kernel.  Entries away from the
+    curved element must agree bit for bit (both kernels share the
+    straight-sided arithmetic)."""
+    mesh = E.jitter(E.T6block(1.0, 1.0, 12, 10), 0.02, seed=5)
+    fesp = heat_space(E, mesh, E.FEH1_T6())
+    n = E.ndofs(fesp)
+    kappa = np.linspace(0.5, 2.0, mesh.nel)
+    am = E.start(E.SysmatAssemblerGPU(), n, n)
+    E.assemble_heat(am, E.FEIterator(fesp), E.QPIterator(fesp, {"npts": 3}), kappa, -6.0)
+    K0, F0 = E.finish(am).tocoo(), am.rhs()
+    xy = mesh.xy.copy()
+    e = mesh.nel // 2
+    mid = mesh.conn[e, 3] - 1  # a midside node of one interior element
+    xy[mid] += [1e-3, -1e-3]
+    am.set_geometry(xy)
+    am.heat(None, -6.0)
+    K1, F1 = E.finish(am).tocoo(), am.rhs()
+    touched = np.nonzero((mesh.conn - 1 == mid).any(axis=1))[0]
+    dofs = E.FEIterator(fesp).eldofs_table() - 1
+    near = np.zeros(n, dtype=bool)
+    near[dofs[touched].ravel()] = True
+    far = ~(near[K0.row] | near[K0.col])
+    assert far.sum() > 0.8 * K0.nnz
+    assert (K0.row == K1.row).all() and (K0.col == K1.col).all()
+    assert (K0.data[far] == K1.data[far]).all()
+    assert not (K0.data[~far] == K1.data[~far]).all()

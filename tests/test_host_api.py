@@ -156,7 +156,7 @@ def test_library_exports_header_symbols(E):
     assert not missing, missing
     assert set(syms) == set(E._native.SIGNATURES)
     lib.elfel_abi_version.restype = ctypes.c_int
-    assert lib.elfel_abi_version() == 1
+    assert lib.elfel_abi_version() == 2
 
 
 def test_no_cpu_fallback_without_library(E, tmp_path):
