@@ -158,7 +158,25 @@ __device__ __forceinline__ void write_records(const double* acc, int rec, int64_
 // integrate to zero).  With pattern kPatT6 the straight-sided branch skips
 // the zero terms: 34 of 63 FP64 multiply-adds remain.
 constexpr uint32_t kT6S11 = 0x1842c7u, kT6S22 = 0x12e229u, kT6S12 = 0x1efadbu, kT6P = 0x38u;
-constexpr int kPatGeneric = 0, kPatT6 = 1;
+constexpr int kPatGeneric = 0, kPatT6 = 1, kPatT6R = 2;
+
+// Rules that integrate the products of the parametric gradients exactly give
+// the exact T6 tensors, whose stored entries (S11, S22, S12 + S21) are
+// rational multiples of seven directions: with c11 = q11 s, c22 = q22 s,
+// c12 = -q12 s (q11 = J22^2 + J12^2, q22 = J21^2 + J11^2, q12 = J22 J21 +
+// J12 J11, s = kappa / det J) and u = q11 - q12, v = q22 - q12,
+//   k0 = (u + v) s/2   k1 = u s/6   k2 = q11 s/2   k3 = v s/6   k4 = q12 s/6
+//   k5 = q22 s/2       k6 = k7 = -u 2s/3   k19 = 2 k6   k15 = k17 = -v 2s/3
+//   k13 = 2 k15        k11 = k12 = -q12 2s/3   k18 = 2 k11
+//   k9 = k14 = k20 = 2 (u + q22) 2s/3        k8 = k10 = k16 = 0,
+// and the element load is Q det / 6 at the midside nodes, 0 at the vertices.
+// kPatT6R evaluates that form: 45 instead of 63 FP64 operations per element.
+constexpr double kT6Exact[21][3] = {
+    {0.5, 0.5, 1.0},      {1. / 6, 0, 1. / 6},  {0.5, 0, 0},          {0, 1. / 6, 1. / 6},   {0, 0, -1. / 6},
+    {0, 0.5, 0},          {-2. / 3, 0, -2. / 3}, {-2. / 3, 0, -2. / 3}, {0, 0, 0},             {4. / 3, 4. / 3, 4. / 3},
+    {0, 0, 0},            {0, 0, 2. / 3},        {0, 0, 2. / 3},        {0, -4. / 3, -4. / 3}, {4. / 3, 4. / 3, 4. / 3},
+    {0, -2. / 3, -2. / 3}, {0, 0, 0},            {0, -2. / 3, -2. / 3}, {0, 0, 4. / 3},        {-4. / 3, 0, -4. / 3},
+    {4. / 3, 4. / 3, 4. / 3}};
 
 // Per-element flag: 1 when the element is straight-sided (the Jacobian is
 // constant and the reference-tensor form applies).  Computed once per
@@ -225,7 +243,17 @@ int heat_pattern(int nn, const QPTab& t) {
   for (int j = 0; j < 6; ++j) pmax = fmax(pmax, fabs(t.P[j]));
   for (int j = 0; j < 6; ++j)
     if (fabs(t.P[j]) > 1e-13 * pmax) mp |= 1u << j;
-  return (m11 == kT6S11 && m22 == kT6S22 && m12 == kT6S12 && mp == kT6P) ? kPatT6 : kPatGeneric;
+  if (!(m11 == kT6S11 && m22 == kT6S22 && m12 == kT6S12 && mp == kT6P)) return kPatGeneric;
+  for (int j = 0; j < 6; ++j)
+    for (int i = 0; i <= j; ++i) {
+      const double* x = kT6Exact[j * (j + 1) / 2 + i];
+      if (fabs(t.S[0][0][i * 6 + j] - x[0]) > 1e-14 || fabs(t.S[1][1][i * 6 + j] - x[1]) > 1e-14 ||
+          fabs(t.S[0][1][i * 6 + j] + t.S[1][0][i * 6 + j] - x[2]) > 1e-14)
+        return kPatT6;
+    }
+  for (int j = 3; j < 6; ++j)
+    if (fabs(t.P[j] - 1.0 / 6.0) > 1e-15) return kPatT6;
+  return kPatT6R;
 }
 
 // Records of one straight-sided element from its three vertices (reference-
@@ -234,31 +262,71 @@ template <int NN, int LD, int PAT>
 __device__ __forceinline__ void straight_record(double x0, double y0, double x1, double y1, double x2, double y2,
                                                 double kap, double Q, const double (*sS)[NN * (NN + 1) / 2],
                                                 const QPTab& tab, double* acc, double* fa, int t) {
+  // Every operation is spelled out (no contraction left to the compiler), so
+  // all kernels that inline this produce the same bits.
   constexpr int NS = NN * (NN + 1) / 2;
-  const double J11 = x1 - x0, J12 = x2 - x0;
-  const double J21 = y1 - y0, J22 = y2 - y0;
-  const double det = J11 * J22 - J21 * J12;
-  const double s = kap / det;
-  const double c11 = (J22 * J22 + J12 * J12) * s;
-  const double c22 = (J21 * J21 + J11 * J11) * s;
-  const double c12 = -(J22 * J21 + J12 * J11) * s;
-  const double qd = Q * det;
-  if (PAT == kPatT6) {
+  const double J11 = __dsub_rn(x1, x0), J12 = __dsub_rn(x2, x0);
+  const double J21 = __dsub_rn(y1, y0), J22 = __dsub_rn(y2, y0);
+  const double det = __fma_rn(J11, J22, -__dmul_rn(J21, J12));
+  const double s = __ddiv_rn(kap, det);
+  const double c11 = __dmul_rn(__fma_rn(J22, J22, __dmul_rn(J12, J12)), s);
+  const double c22 = __dmul_rn(__fma_rn(J21, J21, __dmul_rn(J11, J11)), s);
+  const double c12 = -__dmul_rn(__fma_rn(J22, J21, __dmul_rn(J12, J11)), s);
+  const double qd = __dmul_rn(Q, det);
+  if (PAT == kPatT6R) {
+    const double q11 = __fma_rn(J22, J22, __dmul_rn(J12, J12));
+    const double q22 = __fma_rn(J21, J21, __dmul_rn(J11, J11));
+    const double q12 = __fma_rn(J22, J21, __dmul_rn(J12, J11));
+    const double u = __dsub_rn(q11, q12), v = __dsub_rn(q22, q12);
+    const double s2 = __dmul_rn(s, 0.5), s6 = __dmul_rn(s, 1.0 / 6.0), s23 = __dmul_rn(s, 2.0 / 3.0);
+    const double k6 = -__dmul_rn(u, s23), k15 = -__dmul_rn(v, s23), k11 = -__dmul_rn(q12, s23);
+    const double k9 = __dmul_rn(__dmul_rn(__dadd_rn(u, q22), s23), 2.0);
+    double* a = acc + t;
+    a[0 * LD] = __dmul_rn(__dadd_rn(u, v), s2);
+    a[1 * LD] = __dmul_rn(u, s6);
+    a[2 * LD] = __dmul_rn(q11, s2);
+    a[3 * LD] = __dmul_rn(v, s6);
+    a[4 * LD] = __dmul_rn(q12, s6);
+    a[5 * LD] = __dmul_rn(q22, s2);
+    a[6 * LD] = k6;
+    a[7 * LD] = k6;
+    a[8 * LD] = 0.0;
+    a[9 * LD] = k9;
+    a[10 * LD] = 0.0;
+    a[11 * LD] = k11;
+    a[12 * LD] = k11;
+    a[13 * LD] = __dadd_rn(k15, k15);
+    a[14 * LD] = k9;
+    a[15 * LD] = k15;
+    a[16 * LD] = 0.0;
+    a[17 * LD] = k15;
+    a[18 * LD] = __dadd_rn(k11, k11);
+    a[19 * LD] = __dadd_rn(k6, k6);
+    a[20 * LD] = k9;
+    const double fm = __dmul_rn(qd, tab.P[3]);
+    fa[0 * LD + t] = 0.0;
+    fa[1 * LD + t] = 0.0;
+    fa[2 * LD + t] = 0.0;
+    fa[3 * LD + t] = fm;
+    fa[4 * LD + t] = fm;
+    fa[5 * LD + t] = fm;
+  } else if (PAT == kPatT6) {
 #pragma unroll
     for (int k = 0; k < NS; ++k) {
       double a = 0.0;
-      if ((kT6S12 >> k) & 1u) a = c12 * sS[2][k];
-      if ((kT6S22 >> k) & 1u) a = fma(c22, sS[1][k], a);
-      if ((kT6S11 >> k) & 1u) a = fma(c11, sS[0][k], a);
+      if ((kT6S12 >> k) & 1u) a = __dmul_rn(c12, sS[2][k]);
+      if ((kT6S22 >> k) & 1u) a = __fma_rn(c22, sS[1][k], a);
+      if ((kT6S11 >> k) & 1u) a = __fma_rn(c11, sS[0][k], a);
       acc[k * LD + t] = a;
     }
 #pragma unroll
-    for (int j = 0; j < NN; ++j) fa[j * LD + t] = ((kT6P >> j) & 1u) ? qd * tab.P[j] : 0.0;
+    for (int j = 0; j < NN; ++j) fa[j * LD + t] = ((kT6P >> j) & 1u) ? __dmul_rn(qd, tab.P[j]) : 0.0;
   } else {
 #pragma unroll
-    for (int k = 0; k < NS; ++k) acc[k * LD + t] = c11 * sS[0][k] + c22 * sS[1][k] + c12 * sS[2][k];
+    for (int k = 0; k < NS; ++k)
+      acc[k * LD + t] = __fma_rn(c11, sS[0][k], __fma_rn(c22, sS[1][k], __dmul_rn(c12, sS[2][k])));
 #pragma unroll
-    for (int j = 0; j < NN; ++j) fa[j * LD + t] = qd * tab.P[j];
+    for (int j = 0; j < NN; ++j) fa[j * LD + t] = __dmul_rn(qd, tab.P[j]);
   }
 }
 
@@ -412,13 +480,18 @@ int launch_heat(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* 
   const unsigned grid = grid_for(nel, kIntThreads);
   const double2* p = (const double2*)xy;
   const size_t sm = heat_smem(nn, kIntThreads);
+  const int pat = nn == 6 ? heat_pattern(6, tab) : kPatGeneric;
   if (nn == 3)
     heat_k<3, kPatGeneric><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, p, kappa, Q, straight, tab, kstore, fstore);
-  else if (ncurved == 0 && heat_pattern(6, tab) == kPatT6)
+  else if (ncurved == 0 && pat == kPatT6R)
+    heat_t6s_k<kPatT6R><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, p, kappa, Q, tab, kstore, fstore);
+  else if (ncurved == 0 && pat == kPatT6)
     heat_t6s_k<kPatT6><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, p, kappa, Q, tab, kstore, fstore);
   else if (ncurved == 0)
     heat_t6s_k<kPatGeneric><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, p, kappa, Q, tab, kstore, fstore);
-  else if (heat_pattern(6, tab) == kPatT6)
+  else if (pat == kPatT6R)
+    heat_k<6, kPatT6R><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, p, kappa, Q, straight, tab, kstore, fstore);
+  else if (pat == kPatT6)
     heat_k<6, kPatT6><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, p, kappa, Q, straight, tab, kstore, fstore);
   else
     heat_k<6, kPatGeneric><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, p, kappa, Q, straight, tab, kstore, fstore);
@@ -625,8 +698,10 @@ static void heat_batch_launch(Ctx* c, const HeatJob* jobs, int njobs, int64_t bl
 
 template <int NT>
 static void heat_batch_launch_nn(Ctx* c, int nn, const HeatJob* jobs, int njobs, int64_t blocks, const QPTab& tab) {
+  const int pat = nn == 6 ? heat_pattern(6, tab) : kPatGeneric;
   if (nn == 3) heat_batch_launch<3, NT, kPatGeneric>(c, jobs, njobs, blocks, tab);
-  else if (heat_pattern(6, tab) == kPatT6) heat_batch_launch<6, NT, kPatT6>(c, jobs, njobs, blocks, tab);
+  else if (pat == kPatT6R) heat_batch_launch<6, NT, kPatT6R>(c, jobs, njobs, blocks, tab);
+  else if (pat == kPatT6) heat_batch_launch<6, NT, kPatT6>(c, jobs, njobs, blocks, tab);
   else heat_batch_launch<6, NT, kPatGeneric>(c, jobs, njobs, blocks, tab);
 }
 

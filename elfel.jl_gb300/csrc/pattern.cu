@@ -146,6 +146,33 @@ __global__ void emit_k(SlotGen g, const int64_t* colstart, const int64_t* colptr
 
 __global__ void set_last_k(int32_t* cptr, int64_t nnz, int64_t total) { cptr[nnz] = (int32_t)total; }
 
+// For every window of kReduceWindow nonzeros (one warp each): the window's
+// nonzeros ordered by contributor count, ties by position (a stable order);
+// perm[w * kReduceWindow + rank] = position in the window.  Positions past
+// the last nonzero sort last.
+__global__ void window_order_k(const int32_t* __restrict__ cptr, int64_t nnz, uint8_t* __restrict__ perm) {
+  __shared__ int32_t cnt[8][kReduceWindow];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t nwin = (nnz + kReduceWindow - 1) / kReduceWindow;
+  for (int64_t w = (int64_t)blockIdx.x * 8 + wid; w < nwin; w += (int64_t)gridDim.x * 8) {
+    const int64_t base = w * kReduceWindow;
+    const int n = (int)min((int64_t)kReduceWindow, nnz - base);
+    for (int j = lane; j < kReduceWindow; j += 32)
+      cnt[wid][j] = j < n ? cptr[base + j + 1] - cptr[base + j] : 0x7fffffff;
+    __syncwarp();
+    for (int j = lane; j < kReduceWindow; j += 32) {
+      const int cj = cnt[wid][j];
+      int rank = 0;
+      for (int i = 0; i < kReduceWindow; ++i) {
+        const int ci = cnt[wid][i];
+        rank += (ci < cj) || (ci == cj && i < j);
+      }
+      perm[base + rank] = (uint8_t)j;
+    }
+    __syncwarp();
+  }
+}
+
 int build_pattern(Ctx* c, const SlotGen& g, int64_t nrow, int64_t ncol, Pattern* P) {
   P->release(c);
   const int64_t M = g.total();
@@ -207,6 +234,12 @@ int build_pattern(Ctx* c, const SlotGen& g, int64_t nrow, int64_t ncol, Pattern*
   }
   set_last_k<<<1, 1, 0, st>>>(P->cptr.p, nnz, M);
   ELFEL_LAUNCH_CHECK(c);
+  if (nnz > 0) {
+    const int64_t nwin = (nnz + kReduceWindow - 1) / kReduceWindow;
+    ELFEL_TRY(P->perm.alloc(c, (size_t)(nwin * kReduceWindow)));
+    window_order_k<<<grid_for(nwin, 8, (int64_t)c->sm_count * 16), 256, 0, st>>>(P->cptr.p, nnz, P->perm.p);
+    ELFEL_LAUNCH_CHECK(c);
+  }
   keys.release(c);
   colcnt.release(c);
   colstart.release(c);
@@ -216,13 +249,88 @@ int build_pattern(Ctx* c, const SlotGen& g, int64_t nrow, int64_t ncol, Pattern*
 
 // One thread per nonzero; its contributions are summed left to right, in the
 // order the reference's sparse() adds duplicates.
+// Each thread reduces kReduceItems nonzeros (k, k + stride, ...) with their
+// loads interleaved, so that several independent load chains (cptr ->
+// contrib -> record) are in flight per thread; every nonzero still adds its
+// contributions in slot order.
+constexpr int kReduceItems = 4;
+
 __global__ void reduce_k(const int32_t* __restrict__ cptr, const int32_t* __restrict__ contrib,
                          const double* __restrict__ store, int64_t nnz, double* __restrict__ out) {
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nnz; k += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t b = cptr[k], e = cptr[k + 1];
-    double s = store[contrib[b]];
-    for (int32_t t = b + 1; t < e; ++t) s += store[contrib[t]];
-    out[k] = s;
+  constexpr int R = kReduceItems;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t k0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k0 < nnz; k0 += R * stride) {
+    int32_t b[R], e[R];
+    double s[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int64_t k = k0 + i * stride;
+      b[i] = 0;
+      e[i] = 0;
+      if (k < nnz) {
+        b[i] = cptr[k];
+        e[i] = cptr[k + 1];
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < R; ++i) s[i] = b[i] < e[i] ? store[contrib[b[i]]] : 0.0;
+#pragma unroll
+    for (int i = 0; i < R; ++i)
+      if (b[i] + 1 < e[i]) s[i] += store[contrib[b[i] + 1]];
+#pragma unroll
+    for (int i = 0; i < R; ++i)
+      for (int32_t t = b[i] + 2; t < e[i]; ++t) s[i] += store[contrib[t]];
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int64_t k = k0 + i * stride;
+      if (k < nnz) out[k] = s[i];
+    }
+  }
+}
+
+// One warp per window of kReduceWindow nonzeros, four rounds of 32 lanes in
+// the window's contributor-count order: the lanes of a round have similar
+// counts, so a round issues about as many FP64 adds as its nonzeros need
+// (every warp-level FP64 instruction costs the SM's FP64 pipe the same time
+// however few of its lanes are active).  Each nonzero still adds its
+// contributions in slot order, and the window's values are written inside
+// its own 1 KB of the output.
+__global__ void __launch_bounds__(256) reduce_win_k(const int32_t* __restrict__ cptr,
+                                                   const int32_t* __restrict__ contrib,
+                                                   const uint8_t* __restrict__ perm,
+                                                   const double* __restrict__ store, int64_t nnz,
+                                                   double* __restrict__ out) {
+  constexpr int R = kReduceWindow / 32;
+  const int lane = threadIdx.x & 31;
+  const int64_t nwin = (nnz + kReduceWindow - 1) / kReduceWindow;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x / 32);
+  for (int64_t w = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); w < nwin; w += warps) {
+    const int64_t base = w * kReduceWindow;
+    const int n = (int)min((int64_t)kReduceWindow, nnz - base);
+    int j[R];
+    int32_t b[R], e[R];
+    double s[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      j[r] = perm[base + r * 32 + lane];
+      b[r] = 0;
+      e[r] = 0;
+      if (j[r] < n) {
+        b[r] = cptr[base + j[r]];
+        e[r] = cptr[base + j[r] + 1];
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) s[r] = b[r] < e[r] ? store[contrib[b[r]]] : 0.0;
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+      if (b[r] + 1 < e[r]) s[r] += store[contrib[b[r] + 1]];
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+      for (int32_t t = b[r] + 2; t < e[r]; ++t) s[r] += store[contrib[t]];
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+      if (j[r] < n) out[base + j[r]] = s[r];
   }
 }
 
@@ -264,8 +372,14 @@ int reduce_batch(Ctx* c, const RedJob* jobs_dev, int njobs, int64_t blocks) {
 
 int reduce_values(Ctx* c, const Pattern& P, const double* store, double* vals_out) {
   if (P.nnz == 0) return ELFEL_OK;
-  reduce_k<<<grid_for(P.nnz, 256, (int64_t)c->sm_count * 16), 256, 0, c->stream>>>(P.cptr.p, P.contrib.p, store,
-                                                                                   P.nnz, vals_out);
+  if (P.perm.p) {
+    const int64_t nwin = (P.nnz + kReduceWindow - 1) / kReduceWindow;
+    reduce_win_k<<<grid_for(nwin, 8, (int64_t)c->sm_count * 16), 256, 0, c->stream>>>(
+        P.cptr.p, P.contrib.p, P.perm.p, store, P.nnz, vals_out);
+  } else {
+    reduce_k<<<grid_for(P.nnz, 256, (int64_t)c->sm_count * 16), 256, 0, c->stream>>>(P.cptr.p, P.contrib.p, store,
+                                                                                     P.nnz, vals_out);
+  }
   ELFEL_LAUNCH_CHECK(c);
   return ELFEL_OK;
 }

@@ -76,6 +76,10 @@ __device__ __forceinline__ void slot_rc(const SlotGen& g, int64_t s, int32_t& r,
   store = e * (int64_t)g.store_per_elem + B.store_off + loc;
 }
 
+// Nonzeros per reduction window: a warp reduces one window in four rounds of
+// 32 lanes, the window's nonzeros taken in order of their contributor count.
+constexpr int kReduceWindow = 128;
+
 // CSC pattern with the contributor lists of each nonzero.
 struct Pattern {
   int64_t nrow = 0, ncol = 0, nnz = 0, nslots = 0;
@@ -83,11 +87,13 @@ struct Pattern {
   DBuf<int32_t> rowval;   // nnz, 0-based
   DBuf<int32_t> cptr;     // nnz+1: contributors of nonzero k are contrib[cptr[k] .. cptr[k+1])
   DBuf<int32_t> contrib;  // nslots: storage index of each contribution, ascending slot order
+  DBuf<uint8_t> perm;     // per window of kReduceWindow nonzeros: their order by contributor count
   void release(Ctx* c) {
     colptr.release(c);
     rowval.release(c);
     cptr.release(c);
     contrib.release(c);
+    perm.release(c);
     nrow = ncol = nnz = nslots = 0;
   }
 };

@@ -124,6 +124,8 @@ HEAT_CASES = [
     ("T6", 9, 7, "a", 0.01, True, 3),
     ("T6", 8, 8, "a", 0.01, True, 6),
     ("T3", 100, 100, "alternate", 0.0, False, 3),
+    ("T6", 7, 6, "a", 0.01, False, 1),  # inexact rule: the general tensor form
+    ("T6", 10, 9, "alternate", 0.02, False, 7),
 ]
 
 
