@@ -24,6 +24,7 @@
 // (the tensor representation of Kirby & Logg's FFC).  Curved T6 elements take
 // the per-quadrature-point path, which mirrors the reference loop.
 #include "integrate.cuh"
+#include "floatpair.cuh"
 
 namespace elfel {
 
@@ -256,24 +257,15 @@ int heat_pattern(int nn, const QPTab& t) {
   return kPatT6R;
 }
 
-// Records of one straight-sided element from its three vertices (reference-
-// tensor form): ke = c11 S11 + c22 S22 + c12 (S12 + S21), fe = Q det P.
-template <int NN, int LD, int PAT>
-__device__ __forceinline__ void straight_record(double x0, double y0, double x1, double y1, double x2, double y2,
-                                                double kap, double Q, const double (*sS)[NN * (NN + 1) / 2],
-                                                const QPTab& tab, double* acc, double* fa, int t) {
-  // Every operation is spelled out (no contraction left to the compiler), so
-  // all kernels that inline this produce the same bits.
-  constexpr int NS = NN * (NN + 1) / 2;
-  const double J11 = __dsub_rn(x1, x0), J12 = __dsub_rn(x2, x0);
-  const double J21 = __dsub_rn(y1, y0), J22 = __dsub_rn(y2, y0);
+// The exact-rational T6 record (kPatT6R) in FP64: the fallback of
+// t6r_record_pair for elements outside its accuracy range.
+template <int LD>
+__device__ __forceinline__ void t6r_record_fp64(double J11, double J12, double J21, double J22, double kap, double Q,
+                                                double P6, double* a, double* fa) {
   const double det = __fma_rn(J11, J22, -__dmul_rn(J21, J12));
   const double s = __ddiv_rn(kap, det);
-  const double c11 = __dmul_rn(__fma_rn(J22, J22, __dmul_rn(J12, J12)), s);
-  const double c22 = __dmul_rn(__fma_rn(J21, J21, __dmul_rn(J11, J11)), s);
-  const double c12 = -__dmul_rn(__fma_rn(J22, J21, __dmul_rn(J12, J11)), s);
   const double qd = __dmul_rn(Q, det);
-  if (PAT == kPatT6R) {
+  {
     const double q11 = __fma_rn(J22, J22, __dmul_rn(J12, J12));
     const double q22 = __fma_rn(J21, J21, __dmul_rn(J11, J11));
     const double q12 = __fma_rn(J22, J21, __dmul_rn(J12, J11));
@@ -281,7 +273,6 @@ __device__ __forceinline__ void straight_record(double x0, double y0, double x1,
     const double s2 = __dmul_rn(s, 0.5), s6 = __dmul_rn(s, 1.0 / 6.0), s23 = __dmul_rn(s, 2.0 / 3.0);
     const double k6 = -__dmul_rn(u, s23), k15 = -__dmul_rn(v, s23), k11 = -__dmul_rn(q12, s23);
     const double k9 = __dmul_rn(__dmul_rn(__dadd_rn(u, q22), s23), 2.0);
-    double* a = acc + t;
     a[0 * LD] = __dmul_rn(__dadd_rn(u, v), s2);
     a[1 * LD] = __dmul_rn(u, s6);
     a[2 * LD] = __dmul_rn(q11, s2);
@@ -303,14 +294,103 @@ __device__ __forceinline__ void straight_record(double x0, double y0, double x1,
     a[18 * LD] = __dadd_rn(k11, k11);
     a[19 * LD] = __dadd_rn(k6, k6);
     a[20 * LD] = k9;
-    const double fm = __dmul_rn(qd, tab.P[3]);
-    fa[0 * LD + t] = 0.0;
-    fa[1 * LD + t] = 0.0;
-    fa[2 * LD + t] = 0.0;
-    fa[3 * LD + t] = fm;
-    fa[4 * LD + t] = fm;
-    fa[5 * LD + t] = fm;
-  } else if (PAT == kPatT6) {
+    const double fm = __dmul_rn(qd, P6);
+    fa[0 * LD] = 0.0;
+    fa[1 * LD] = 0.0;
+    fa[2 * LD] = 0.0;
+    fa[3 * LD] = fm;
+    fa[4 * LD] = fm;
+    fa[5 * LD] = fm;
+  }
+}
+
+// The exact-rational T6 record in float pairs (48-bit significands; see
+// floatpair.cuh): J is scaled by 2^-k so that max |J'| is in [1, 2), kappa and
+// Q to [1, 2) by their own powers of two, and the powers come back in the
+// exponents of the results.  Only the 4 coordinate differences and 8 joins
+// to double are FP64 instructions (45 in t6r_record_fp64); the entries that
+// are power-of-two multiples of others are exponent adds.  Elements with
+// det J' < 1/4 (strongly distorted: the pair subtraction in det J' would cost
+// more than 2^-42 relative accuracy) return false and take the FP64 form.
+template <int LD>
+__device__ __forceinline__ bool t6r_record_pair(double J11, double J12, double J21, double J22, double kap, double Q,
+                                                double P6, double* a, double* fa) {
+  const int em = max(max(dexp(J11), dexp(J12)), max(dexp(J21), dexp(J22)));
+  const int k = em - 1023;
+  const int kk = dexp(kap) - 1023, kq = dexp(Q) - 1023;
+  if (em == 0 || k < -400 || k > 400 || kk < -900 || kk > 900 || kq + 2 * k < -900 || kq + 2 * k > 900) return false;
+  f2 A, B, C, D, kp, qp, p6, sixth;
+  bool ok = split_scaled(J11, k, &A) & split_scaled(J12, k, &B) & split_scaled(J21, k, &C) &
+            split_scaled(J22, k, &D) & split_scaled(kap, kk, &kp) & split_scaled(Q, kq, &qp) &
+            split_scaled(P6, 0, &p6) & split_scaled(1.0 / 6.0, 0, &sixth);
+  if (!ok) return false;
+  const f2 det = f2_sub(f2_mul(A, D), f2_mul(C, B));
+  if (!(fabsf(det.hi) >= 0.25f)) return false;
+  const f2 q11 = f2_add(f2_mul(D, D), f2_mul(B, B));
+  const f2 q22 = f2_add(f2_mul(C, C), f2_mul(A, A));
+  const f2 q12 = f2_add(f2_mul(D, C), f2_mul(B, A));
+  const f2 u = f2_sub(q11, q12), v = f2_sub(q22, q12);
+  const f2 s = f2_div(kp, det);
+  const f2 s6 = f2_mul(s, sixth);
+  const double a1 = join_scaled(f2_mul(u, s6), kk);
+  const double a3 = join_scaled(f2_mul(v, s6), kk);
+  const double a4 = join_scaled(f2_mul(q12, s6), kk);
+  const double g8 = join_scaled(f2_mul(f2_add(u, q22), s6), kk + 3);
+  a[0 * LD] = join_scaled(f2_mul(f2_add(u, v), s), kk - 1);
+  a[1 * LD] = a1;
+  a[2 * LD] = join_scaled(f2_mul(q11, s), kk - 1);
+  a[3 * LD] = a3;
+  a[4 * LD] = a4;
+  a[5 * LD] = join_scaled(f2_mul(q22, s), kk - 1);
+  const double k6 = pow2_scale(-a1, 2), k15 = pow2_scale(-a3, 2), k11 = pow2_scale(-a4, 2);
+  a[6 * LD] = k6;
+  a[7 * LD] = k6;
+  a[8 * LD] = 0.0;
+  a[9 * LD] = g8;
+  a[10 * LD] = 0.0;
+  a[11 * LD] = k11;
+  a[12 * LD] = k11;
+  a[13 * LD] = pow2_scale(-a3, 3);
+  a[14 * LD] = g8;
+  a[15 * LD] = k15;
+  a[16 * LD] = 0.0;
+  a[17 * LD] = k15;
+  a[18 * LD] = pow2_scale(-a4, 3);
+  a[19 * LD] = pow2_scale(-a1, 3);
+  a[20 * LD] = g8;
+  const double fm = join_scaled(f2_mul(f2_mul(qp, det), p6), kq + 2 * k);
+  fa[0 * LD] = 0.0;
+  fa[1 * LD] = 0.0;
+  fa[2 * LD] = 0.0;
+  fa[3 * LD] = fm;
+  fa[4 * LD] = fm;
+  fa[5 * LD] = fm;
+  return true;
+}
+
+// Records of one straight-sided element from its three vertices (reference-
+// tensor form): ke = c11 S11 + c22 S22 + c12 (S12 + S21), fe = Q det P.
+template <int NN, int LD, int PAT>
+__device__ __forceinline__ void straight_record(double x0, double y0, double x1, double y1, double x2, double y2,
+                                                double kap, double Q, const double (*sS)[NN * (NN + 1) / 2],
+                                                const QPTab& tab, double* acc, double* fa, int t) {
+  // Every operation is spelled out (no contraction left to the compiler), so
+  // all kernels that inline this produce the same bits.
+  constexpr int NS = NN * (NN + 1) / 2;
+  const double J11 = __dsub_rn(x1, x0), J12 = __dsub_rn(x2, x0);
+  const double J21 = __dsub_rn(y1, y0), J22 = __dsub_rn(y2, y0);
+  if (PAT == kPatT6R) {
+    if (!t6r_record_pair<LD>(J11, J12, J21, J22, kap, Q, tab.P[3], acc + t, fa + t))
+      t6r_record_fp64<LD>(J11, J12, J21, J22, kap, Q, tab.P[3], acc + t, fa + t);
+    return;
+  }
+  const double det = __fma_rn(J11, J22, -__dmul_rn(J21, J12));
+  const double s = __ddiv_rn(kap, det);
+  const double c11 = __dmul_rn(__fma_rn(J22, J22, __dmul_rn(J12, J12)), s);
+  const double c22 = __dmul_rn(__fma_rn(J21, J21, __dmul_rn(J11, J11)), s);
+  const double c12 = -__dmul_rn(__fma_rn(J22, J21, __dmul_rn(J12, J11)), s);
+  const double qd = __dmul_rn(Q, det);
+  if (PAT == kPatT6) {
 #pragma unroll
     for (int k = 0; k < NS; ++k) {
       double a = 0.0;
