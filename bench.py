@@ -555,14 +555,19 @@ def main():
     # whole-assembly algorithmic bytes (conn + coords + coefficient + K values + F)
     asm_bytes = nel * 6 * 4 + mesh.nnodes * 16 + nel * 8 + nnz_est * 8 + n * 8
     ach = alg[dom] / (per[dom] * 1e-3) / 1e9
-    # DRAM traffic of one heat_k<6> launch (dram__bytes_read.sum + dram__bytes_write.sum) measured
-    # with ncu on the 700 x 700 case of this workload (980,000 elements: 63.98 + 152.87 MB), scaled
-    # by the element count; writes still dirty in L2 when the kernel ends are not counted
-    HEAT_K_TRAFFIC_PER_ELEMENT = (63.97568e6 + 152.874496e6) / 980000
-    traffic = HEAT_K_TRAFFIC_PER_ELEMENT * nel if dom == "integrate_heat" else None
+    # DRAM traffic of one launch of each kernel (dram__bytes_read.sum + dram__bytes_write.sum)
+    # measured with ncu on the 700 x 700 case of this workload (980,000 elements; heat_t6s_k<2>
+    # 47.20 + 151.46 MB, reduce_win_k 426.97 + 155.31 MB, reduce_row0_dense_k 94.17 + 8.09 MB),
+    # scaled by the element count; writes still dirty in L2 when a kernel ends are not counted
+    TRAFFIC_PER_ELEMENT = {"integrate_heat": (47.202304e6 + 151.463424e6) / 980000,
+                           "reduce_K": (426.966016e6 + 155.309568e6) / 980000,
+                           "reduce_F": (94.168832e6 + 8.086528e6) / 980000}
+    traffic = TRAFFIC_PER_ELEMENT[dom] * nel if dom in TRAFFIC_PER_ELEMENT else None
+    for k, row in kernel_rows.items():
+        row["traffic"] = TRAFFIC_PER_ELEMENT[k] * nel if k in TRAFFIC_PER_ELEMENT else None
     roofline = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
                 "traffic": traffic, "kernel": dom, "peak_kind": peak_kind,
-                "traffic_source": "ncu DRAM bytes of heat_k<6> at 980,000 elements, scaled per element",
+                "traffic_source": "ncu DRAM bytes of the kernel at 980,000 elements, scaled per element",
                 "assembly": {"alg_bytes": asm_bytes, "achieved": asm_bytes / t_step / 1e9,
                              "frac": asm_bytes / t_step / 1e9 / hbm},
                 "kernels": kernel_rows}
