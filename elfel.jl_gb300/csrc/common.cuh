@@ -26,6 +26,7 @@ struct Ctx {
   int device = 0;
   cudaStream_t stream = nullptr;      // stream all work is issued on
   cudaStream_t own_stream = nullptr;  // the context's own stream
+  cudaMemPool_t pool = nullptr;  // the context's stream-ordered pool (keeps freed memory for reuse)
   int64_t budget = 0;       // bytes the context may hold on the device (0 = unlimited)
   int64_t in_use = 0;       // bytes currently held
   int64_t peak = 0;

@@ -24,10 +24,10 @@ int dalloc(Ctx* c, void** p, size_t bytes) {
   if (c->budget > 0 && c->in_use + (int64_t)bytes > c->budget)
     return fail(c, ELFEL_ERR_BUDGET, "device memory budget exceeded: in use %lld + request %zu > budget %lld",
                 (long long)c->in_use, bytes, (long long)c->budget);
-  cudaError_t e = cudaMallocAsync(p, bytes, c->stream);
+  cudaError_t e = c->pool ? cudaMallocFromPoolAsync(p, bytes, c->pool, c->stream) : cudaMallocAsync(p, bytes, c->stream);
   if (e != cudaSuccess) {
     cudaGetLastError();
-    return fail(c, ELFEL_ERR_BUDGET, "cudaMallocAsync(%zu bytes): %s", bytes, cudaGetErrorString(e));
+    return fail(c, ELFEL_ERR_BUDGET, "device allocation of %zu bytes: %s", bytes, cudaGetErrorString(e));
   }
   c->in_use += (int64_t)bytes;
   if (c->in_use > c->peak) c->peak = c->in_use;
@@ -199,6 +199,24 @@ extern "C" int elfel_ctx_create(int device, int64_t mem_budget_bytes, elfel_ctx*
     return ELFEL_ERR_CUDA;
   }
   h->c.own_stream = h->c.stream;
+  // A pool of the context's own: memory freed by one assembly (the pattern
+  // builder's sort keys, a replaced system's buffers) stays mapped for the
+  // next one instead of going back to the driver at every synchronisation.
+  // It keeps up to the memory budget (everything without one).
+  {
+    cudaMemPoolProps props;
+    memset(&props, 0, sizeof(props));
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    if (cudaMemPoolCreate(&h->c.pool, &props) == cudaSuccess) {
+      uint64_t keep = mem_budget_bytes > 0 ? (uint64_t)mem_budget_bytes : UINT64_MAX;
+      cudaMemPoolSetAttribute(h->c.pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    } else {
+      cudaGetLastError();
+      h->c.pool = nullptr;  // the device's default pool then
+    }
+  }
   const char* tr = getenv("ELFEL_TRACE");
   h->c.trace = (tr && tr[0] == '1') ? 1 : 0;
   const char* tu = getenv("ELFEL_TUNE");
@@ -301,6 +319,8 @@ extern "C" int elfel_ctx_destroy(elfel_ctx* h) {
   cudaStreamSynchronize(h->c.stream);
   clear_phases(&h->c);
   if (h->c.own_stream) cudaStreamDestroy(h->c.own_stream);
+  // memory still held by live systems is released once they free it
+  if (h->c.pool) cudaMemPoolDestroy(h->c.pool);
   delete h;
   return ELFEL_OK;
 }

@@ -55,27 +55,32 @@ __device__ __forceinline__ void cmpswap(uint64_t* a, int64_t i, int64_t j) {
 
 // Bitonic network in its "flip" form: every comparator puts the smaller key at
 // the lower index, so any length n sorts correctly when comparators that reach
-// past n are skipped (those positions behave as +infinity).  One warp.
-__device__ void warp_sort(uint64_t* a, int64_t n, int lane) {
+// past n are skipped (those positions behave as +infinity).  One warp.  The
+// sizes are powers of two below 2^31 (a column holds fewer than 2^31 slots),
+// so block and offset come from 32-bit shifts and masks.
+__device__ void warp_sort(uint64_t* a, int n, int lane) {
   if (n < 2) return;
-  int64_t npow = 1;
-  while (npow < n) npow <<= 1;
-  const int64_t half_pairs = npow >> 1;
-  for (int64_t size = 2; size <= npow; size <<= 1) {
-    const int64_t h = size >> 1;
-    for (int64_t p = lane; p < half_pairs; p += 32) {
-      int64_t blk = p / h, off = p - blk * h;
-      int64_t i = blk * size + off;
-      int64_t j = blk * size + size - 1 - off;
-      if (j < n) cmpswap(a, i, j);
+  const unsigned un = (unsigned)n;
+  int lg = 0;
+  while ((1u << lg) < un) ++lg;
+  const unsigned half_pairs = 1u << (lg - 1);
+  for (int ls = 1; ls <= lg; ++ls) {  // size = 2^ls, h = 2^(ls - 1)
+    const int lh = ls - 1;
+    const unsigned size = 1u << ls, h = 1u << lh;
+    for (unsigned p = lane; p < half_pairs; p += 32) {
+      const unsigned blk = p >> lh, off = p & (h - 1);
+      const unsigned i = blk * size + off;
+      const unsigned j = blk * size + size - 1 - off;
+      if (j < un) cmpswap(a, i, j);
     }
     __syncwarp();
-    for (int64_t stride = h >> 1; stride > 0; stride >>= 1) {
-      for (int64_t p = lane; p < half_pairs; p += 32) {
-        int64_t blk = p / stride, off = p - blk * stride;
-        int64_t i = blk * 2 * stride + off;
-        int64_t j = i + stride;
-        if (j < n) cmpswap(a, i, j);
+    for (int lst = lh - 1; lst >= 0; --lst) {  // stride = 2^lst
+      const unsigned stride = 1u << lst;
+      for (unsigned p = lane; p < half_pairs; p += 32) {
+        const unsigned blk = p >> lst, off = p & (stride - 1);
+        const unsigned i = (blk << (lst + 1)) + off;
+        const unsigned j = i + stride;
+        if (j < un) cmpswap(a, i, j);
       }
       __syncwarp();
     }
@@ -89,10 +94,11 @@ __global__ void __launch_bounds__(kSortThreads) sort_cols_k(const int64_t* colst
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int64_t warps = (int64_t)gridDim.x * (kSortThreads / 32);
   for (int64_t col = (int64_t)blockIdx.x * (kSortThreads / 32) + wid; col < ncol; col += warps) {
-    const int64_t b = colstart[col], n = colstart[col + 1] - b;
+    const int64_t b = colstart[col];
+    const int n = (int)(colstart[col + 1] - b);
     uint64_t* a;
     if (n <= kSortCap) {
-      for (int64_t t = lane; t < n; t += 32) sh[wid][t] = keys[b + t];
+      for (int t = lane; t < n; t += 32) sh[wid][t] = keys[b + t];
       __syncwarp();
       a = sh[wid];
     } else {
@@ -101,14 +107,14 @@ __global__ void __launch_bounds__(kSortThreads) sort_cols_k(const int64_t* colst
     warp_sort(a, n, lane);
     // distinct rows
     int32_t cnt = 0;
-    for (int64_t t0 = 0; t0 < n; t0 += 32) {
-      int64_t t = t0 + lane;
+    for (int t0 = 0; t0 < n; t0 += 32) {
+      const int t = t0 + lane;
       bool first = false;
       if (t < n) first = (t == 0) || ((a[t] >> 32) != (a[t - 1] >> 32));
       cnt += __popc(__ballot_sync(0xffffffffu, first));
     }
     if (n <= kSortCap)
-      for (int64_t t = lane; t < n; t += 32) keys[b + t] = a[t];
+      for (int t = lane; t < n; t += 32) keys[b + t] = a[t];
     if (lane == 0) nnzcnt[col] = cnt;
     __syncwarp();
   }

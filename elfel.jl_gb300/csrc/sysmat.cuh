@@ -52,8 +52,10 @@ __device__ __forceinline__ void slot_rc(const SlotGen& g, int64_t s, int32_t& r,
     store = s;
     return;
   }
-  const int64_t e = s / g.slots_per_elem;
-  const int l = (int)(s - e * g.slots_per_elem);
+  // slot numbers stay below 2^31 (build_pattern checks), so 32-bit division
+  const uint32_t su = (uint32_t)s, spe = (uint32_t)g.slots_per_elem;
+  const int64_t e = (int64_t)(su / spe);
+  const int l = (int)(su - (uint32_t)e * spe);
   int bi = 0;
 #pragma unroll
   for (int k = 1; k < kMaxBlocks; ++k)
