@@ -87,7 +87,25 @@ __device__ void warp_sort(uint64_t* a, int n, int lane) {
   }
 }
 
+// Register-resident bitonic sort of 32 keys, one per lane, ascending by lane;
+// shuffles exchange the partners.  Unused lanes hold ~0.
+__device__ __forceinline__ uint64_t reg_sort32(uint64_t v, int lane) {
+#pragma unroll
+  for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      const uint64_t o = __shfl_xor_sync(0xffffffffu, v, j);
+      const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
+      v = keep_min ? (v < o ? v : o) : (v < o ? o : v);
+    }
+  }
+  return v;
+}
+
 // Sort every column's keys by (row, slot) and count its distinct rows.
+// Columns of up to 32 keys (most of a finite element pattern) are sorted in
+// registers; longer ones with the bitonic network in shared memory (up to
+// kSortCap keys) or in place in global memory.
 __global__ void __launch_bounds__(kSortThreads) sort_cols_k(const int64_t* colstart, int64_t ncol, uint64_t* keys,
                                                            int32_t* nnzcnt) {
   __shared__ uint64_t sh[kSortThreads / 32][kSortCap];
@@ -96,6 +114,17 @@ __global__ void __launch_bounds__(kSortThreads) sort_cols_k(const int64_t* colst
   for (int64_t col = (int64_t)blockIdx.x * (kSortThreads / 32) + wid; col < ncol; col += warps) {
     const int64_t b = colstart[col];
     const int n = (int)(colstart[col + 1] - b);
+    if (n <= 32) {
+      uint64_t v = lane < n ? keys[b + lane] : ~0ull;
+      if (n > 1) v = reg_sort32(v, lane);
+      // distinct rows: a key starts a row when its predecessor has another row
+      const uint64_t pv = __shfl_up_sync(0xffffffffu, v, 1);
+      const bool first = lane < n && (lane == 0 || (v >> 32) != (pv >> 32));
+      const int cnt = __popc(__ballot_sync(0xffffffffu, first));
+      if (lane < n) keys[b + lane] = v;
+      if (lane == 0) nnzcnt[col] = cnt;
+      continue;
+    }
     uint64_t* a;
     if (n <= kSortCap) {
       for (int t = lane; t < n; t += 32) sh[wid][t] = keys[b + t];
@@ -153,29 +182,47 @@ __global__ void emit_k(SlotGen g, const int64_t* colstart, const int64_t* colptr
 __global__ void set_last_k(int32_t* cptr, int64_t nnz, int64_t total) { cptr[nnz] = (int32_t)total; }
 
 // For every window of kReduceWindow nonzeros (one warp each): the window's
-// nonzeros ordered by contributor count, ties by position (a stable order);
-// perm[w * kReduceWindow + rank] = position in the window.  Positions past
-// the last nonzero sort last.
+// nonzeros ordered by contributor count (counts of 8 and more together), ties
+// by position -- a stable bucket order; perm[w * kReduceWindow + rank] =
+// position in the window.  Positions past the last nonzero sort last.  The
+// ranks come from one ballot per bucket and round: rank = items in smaller
+// buckets + items of the same bucket in earlier rounds or lower lanes.
+constexpr int kOrderBuckets = 8;
+
 __global__ void window_order_k(const int32_t* __restrict__ cptr, int64_t nnz, uint8_t* __restrict__ perm) {
-  __shared__ int32_t cnt[8][kReduceWindow];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  constexpr int R = kReduceWindow / 32;
+  const int lane = threadIdx.x & 31;
+  const unsigned lower = (1u << lane) - 1u;
   const int64_t nwin = (nnz + kReduceWindow - 1) / kReduceWindow;
-  for (int64_t w = (int64_t)blockIdx.x * 8 + wid; w < nwin; w += (int64_t)gridDim.x * 8) {
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x / 32);
+  for (int64_t w = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); w < nwin; w += warps) {
     const int64_t base = w * kReduceWindow;
     const int n = (int)min((int64_t)kReduceWindow, nnz - base);
-    for (int j = lane; j < kReduceWindow; j += 32)
-      cnt[wid][j] = j < n ? cptr[base + j + 1] - cptr[base + j] : 0x7fffffff;
-    __syncwarp();
-    for (int j = lane; j < kReduceWindow; j += 32) {
-      const int cj = cnt[wid][j];
-      int rank = 0;
-      for (int i = 0; i < kReduceWindow; ++i) {
-        const int ci = cnt[wid][i];
-        rank += (ci < cj) || (ci == cj && i < j);
+    int v[R], rank[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int j = r * 32 + lane;
+      v[r] = kOrderBuckets;  // padding: after every bucket
+      if (j < n) {
+        const int c = cptr[base + j + 1] - cptr[base + j];
+        v[r] = (c < 1 ? 1 : (c > kOrderBuckets ? kOrderBuckets : c)) - 1;
       }
-      perm[base + rank] = (uint8_t)j;
+      rank[r] = 0;
     }
-    __syncwarp();
+    int start = 0;
+#pragma unroll
+    for (int bkt = 0; bkt <= kOrderBuckets; ++bkt) {
+      int before = start;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const unsigned m = __ballot_sync(0xffffffffu, v[r] == bkt);
+        if (v[r] == bkt) rank[r] = before + __popc(m & lower);
+        before += __popc(m);
+      }
+      start = before;
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) perm[base + rank[r]] = (uint8_t)(r * 32 + lane);
   }
 }
 
