@@ -87,11 +87,13 @@ __device__ void warp_sort(uint64_t* a, int n, int lane) {
   }
 }
 
-// Register-resident bitonic sort of 32 keys, one per lane, ascending by lane;
-// shuffles exchange the partners.  Unused lanes hold ~0.
-__device__ __forceinline__ uint64_t reg_sort32(uint64_t v, int lane) {
+// Register-resident bitonic sort of P <= 32 keys, one per lane: lanes 0..P-1
+// end ascending (every group of P lanes is sorted, in alternating
+// directions); shuffles exchange the partners.  Unused lanes hold ~0.
+template <int P>
+__device__ __forceinline__ uint64_t reg_sort(uint64_t v, int lane) {
 #pragma unroll
-  for (int k = 2; k <= 32; k <<= 1) {
+  for (int k = 2; k <= P; k <<= 1) {
 #pragma unroll
     for (int j = k >> 1; j > 0; j >>= 1) {
       const uint64_t o = __shfl_xor_sync(0xffffffffu, v, j);
@@ -102,79 +104,193 @@ __device__ __forceinline__ uint64_t reg_sort32(uint64_t v, int lane) {
   return v;
 }
 
-// Sort every column's keys by (row, slot) and count its distinct rows.
-// Columns of up to 32 keys (most of a finite element pattern) are sorted in
-// registers; longer ones with the bitonic network in shared memory (up to
-// kSortCap keys) or in place in global memory.
+// Register-resident bitonic sort of 64 keys held two per lane (index lane in
+// v0, lane + 32 in v1), ascending; shuffles exchange keys between lanes, the
+// j = 32 stages compare a lane's own pair.  Unused positions hold ~0.
+__device__ __forceinline__ void reg_sort64(uint64_t& v0, uint64_t& v1, int lane) {
+#pragma unroll
+  for (int k = 2; k <= 64; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      if (j == 32) {  // partner of index i is i + 32: the same lane's other key
+        const bool up = ((lane & k) == 0);
+        const uint64_t lo = v0 < v1 ? v0 : v1, hi = v0 < v1 ? v1 : v0;
+        v0 = up ? lo : hi;
+        v1 = up ? hi : lo;
+      } else {
+        const uint64_t o0 = __shfl_xor_sync(0xffffffffu, v0, j);
+        const uint64_t o1 = __shfl_xor_sync(0xffffffffu, v1, j);
+        const bool lower = (lane & j) == 0;
+        const bool up0 = ((lane & k) == 0), up1 = (((lane + 32) & k) == 0);
+        v0 = (lower == up0) ? (v0 < o0 ? v0 : o0) : (v0 < o0 ? o0 : v0);
+        v1 = (lower == up1) ? (v1 < o1 ? v1 : o1) : (v1 < o1 ? o1 : v1);
+      }
+    }
+  }
+}
+
+// Sort one column's keys by (row, slot) and count its distinct rows (one
+// warp).  Columns of up to 64 keys are sorted in registers (one key per lane
+// up to 32, two up to 64); longer ones with the bitonic network in shared
+// memory (up to kSortCap keys, in sh) or in place in global memory.
+__device__ void sort_column(int64_t b, int n, uint64_t* keys, int32_t* cnt_out, uint64_t* sh, int lane) {
+  if (n <= 32) {
+    uint64_t v = lane < n ? keys[b + lane] : ~0ull;
+    if (n > 16) v = reg_sort<32>(v, lane);
+    else if (n > 8) v = reg_sort<16>(v, lane);
+    else if (n > 4) v = reg_sort<8>(v, lane);
+    else if (n > 1) v = reg_sort<4>(v, lane);
+    // distinct rows: a key starts a row when its predecessor has another row
+    const uint64_t pv = __shfl_up_sync(0xffffffffu, v, 1);
+    const bool first = lane < n && (lane == 0 || (v >> 32) != (pv >> 32));
+    const int cnt = __popc(__ballot_sync(0xffffffffu, first));
+    if (lane < n) keys[b + lane] = v;
+    if (lane == 0) *cnt_out = cnt;
+    return;
+  }
+  if (n <= 64) {
+    uint64_t v0 = keys[b + lane];
+    uint64_t v1 = lane + 32 < n ? keys[b + lane + 32] : ~0ull;
+    reg_sort64(v0, v1, lane);
+    const uint64_t p0 = __shfl_up_sync(0xffffffffu, v0, 1);
+    const uint64_t last0 = __shfl_sync(0xffffffffu, v0, 31);
+    uint64_t p1 = __shfl_up_sync(0xffffffffu, v1, 1);
+    if (lane == 0) p1 = last0;
+    const bool f0 = lane == 0 || (v0 >> 32) != (p0 >> 32);
+    const bool f1 = lane + 32 < n && (v1 >> 32) != (p1 >> 32);
+    const int cnt = __popc(__ballot_sync(0xffffffffu, f0)) + __popc(__ballot_sync(0xffffffffu, f1));
+    keys[b + lane] = v0;
+    if (lane + 32 < n) keys[b + lane + 32] = v1;
+    if (lane == 0) *cnt_out = cnt;
+    return;
+  }
+  uint64_t* a;
+  if (n <= kSortCap) {
+    for (int t = lane; t < n; t += 32) sh[t] = keys[b + t];
+    __syncwarp();
+    a = sh;
+  } else {
+    a = keys + b;  // long column: sort in place in global memory
+  }
+  warp_sort(a, n, lane);
+  int32_t cnt = 0;
+  for (int t0 = 0; t0 < n; t0 += 32) {
+    const int t = t0 + lane;
+    bool first = false;
+    if (t < n) first = (t == 0) || ((a[t] >> 32) != (a[t - 1] >> 32));
+    cnt += __popc(__ballot_sync(0xffffffffu, first));
+  }
+  if (n <= kSortCap)
+    for (int t = lane; t < n; t += 32) keys[b + t] = a[t];
+  if (lane == 0) *cnt_out = cnt;
+  __syncwarp();
+}
+
+// A warp takes four consecutive columns.  When each has at most 8 keys (the
+// rhs pattern, where a column holds a node's element contributions), the
+// four are sorted at once, one per group of 8 lanes; otherwise one after the
+// other by the whole warp.
+constexpr int kColsPerWarp = 4;
+
 __global__ void __launch_bounds__(kSortThreads) sort_cols_k(const int64_t* colstart, int64_t ncol, uint64_t* keys,
                                                            int32_t* nnzcnt) {
   __shared__ uint64_t sh[kSortThreads / 32][kSortCap];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int grp = lane >> 3, gl = lane & 7;
   const int64_t warps = (int64_t)gridDim.x * (kSortThreads / 32);
-  for (int64_t col = (int64_t)blockIdx.x * (kSortThreads / 32) + wid; col < ncol; col += warps) {
-    const int64_t b = colstart[col];
-    const int n = (int)(colstart[col + 1] - b);
-    if (n <= 32) {
-      uint64_t v = lane < n ? keys[b + lane] : ~0ull;
-      if (n > 1) v = reg_sort32(v, lane);
-      // distinct rows: a key starts a row when its predecessor has another row
-      const uint64_t pv = __shfl_up_sync(0xffffffffu, v, 1);
-      const bool first = lane < n && (lane == 0 || (v >> 32) != (pv >> 32));
-      const int cnt = __popc(__ballot_sync(0xffffffffu, first));
-      if (lane < n) keys[b + lane] = v;
-      if (lane == 0) nnzcnt[col] = cnt;
+  for (int64_t c0 = ((int64_t)blockIdx.x * (kSortThreads / 32) + wid) * kColsPerWarp; c0 < ncol;
+       c0 += warps * kColsPerWarp) {
+    const int64_t cg = c0 + grp;
+    int64_t bg = 0;
+    int ng = 0;
+    if (cg < ncol) {
+      bg = colstart[cg];
+      ng = (int)(colstart[cg + 1] - bg);
+    }
+    if (__all_sync(0xffffffffu, ng <= 8)) {
+      uint64_t v = gl < ng ? keys[bg + gl] : ~0ull;
+      v = reg_sort<8>(v, gl);  // partners lane ^ j (j < 8) stay inside the group
+      const uint64_t pv = __shfl_up_sync(0xffffffffu, v, 1, 8);
+      const bool first = gl < ng && (gl == 0 || (v >> 32) != (pv >> 32));
+      const unsigned m = __ballot_sync(0xffffffffu, first);
+      if (gl < ng) keys[bg + gl] = v;
+      if (gl == 0 && cg < ncol) nnzcnt[cg] = __popc(m & (0xffu << (grp * 8)));
       continue;
     }
-    uint64_t* a;
-    if (n <= kSortCap) {
-      for (int t = lane; t < n; t += 32) sh[wid][t] = keys[b + t];
-      __syncwarp();
-      a = sh[wid];
-    } else {
-      a = keys + b;  // long column: sort in place in global memory
+    for (int q = 0; q < kColsPerWarp; ++q) {
+      const int64_t col = c0 + q;
+      if (col >= ncol) break;
+      const int64_t b = colstart[col];
+      sort_column(b, (int)(colstart[col + 1] - b), keys, nnzcnt + col, sh[wid], lane);
     }
-    warp_sort(a, n, lane);
-    // distinct rows
-    int32_t cnt = 0;
-    for (int t0 = 0; t0 < n; t0 += 32) {
-      const int t = t0 + lane;
-      bool first = false;
-      if (t < n) first = (t == 0) || ((a[t] >> 32) != (a[t - 1] >> 32));
-      cnt += __popc(__ballot_sync(0xffffffffu, first));
+  }
+}
+
+// Emit one column's nonzeros (rows, first contributions) and the storage
+// index of each contribution (one warp).
+__device__ void emit_column(const SlotGen& g, int64_t b, int64_t n, int64_t k, const uint64_t* keys,
+                            int32_t* rowval, int32_t* cptr, int32_t* contrib, int lane) {
+  for (int64_t t0 = 0; t0 < n; t0 += 32) {
+    int64_t t = t0 + lane;
+    bool first = false;
+    uint64_t key = 0;
+    if (t < n) {
+      key = keys[b + t];
+      first = (t == 0) || ((key >> 32) != (keys[b + t - 1] >> 32));
+      int32_t r, c;
+      int64_t st;
+      slot_rc(g, (int64_t)(key & 0xffffffffull), r, c, st);
+      contrib[b + t] = (int32_t)st;
     }
-    if (n <= kSortCap)
-      for (int t = lane; t < n; t += 32) keys[b + t] = a[t];
-    if (lane == 0) nnzcnt[col] = cnt;
-    __syncwarp();
+    unsigned m = __ballot_sync(0xffffffffu, first);
+    if (first) {
+      int64_t kk = k + __popc(m & ((1u << lane) - 1u));
+      rowval[kk] = (int32_t)(key >> 32);
+      cptr[kk] = (int32_t)(b + t);
+    }
+    k += __popc(m);
   }
 }
 
 __global__ void emit_k(SlotGen g, const int64_t* colstart, const int64_t* colptr, int64_t ncol, const uint64_t* keys,
                        int32_t* rowval, int32_t* cptr, int32_t* contrib) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int grp = lane >> 3, gl = lane & 7;
+  const unsigned below = (1u << lane) - 1u, group = 0xffu << (grp * 8);
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x / 32);
-  for (int64_t col = (int64_t)blockIdx.x * (blockDim.x / 32) + wid; col < ncol; col += warps) {
-    const int64_t b = colstart[col], n = colstart[col + 1] - b;
-    int64_t k = colptr[col];
-    for (int64_t t0 = 0; t0 < n; t0 += 32) {
-      int64_t t = t0 + lane;
+  for (int64_t c0 = ((int64_t)blockIdx.x * (blockDim.x / 32) + wid) * kColsPerWarp; c0 < ncol;
+       c0 += warps * kColsPerWarp) {
+    const int64_t cg = c0 + grp;
+    int64_t bg = 0;
+    int ng = 0;
+    if (cg < ncol) {
+      bg = colstart[cg];
+      ng = (int)(colstart[cg + 1] - bg);
+    }
+    if (__all_sync(0xffffffffu, ng <= 8)) {
       bool first = false;
       uint64_t key = 0;
-      if (t < n) {
-        key = keys[b + t];
-        first = (t == 0) || ((key >> 32) != (keys[b + t - 1] >> 32));
+      if (gl < ng) {
+        key = keys[bg + gl];
+        first = (gl == 0) || ((key >> 32) != (keys[bg + gl - 1] >> 32));
         int32_t r, c;
         int64_t st;
         slot_rc(g, (int64_t)(key & 0xffffffffull), r, c, st);
-        contrib[b + t] = (int32_t)st;
+        contrib[bg + gl] = (int32_t)st;
       }
-      unsigned m = __ballot_sync(0xffffffffu, first);
+      const unsigned m = __ballot_sync(0xffffffffu, first);
       if (first) {
-        int64_t kk = k + __popc(m & ((1u << lane) - 1u));
+        const int64_t kk = colptr[cg] + __popc(m & group & below);
         rowval[kk] = (int32_t)(key >> 32);
-        cptr[kk] = (int32_t)(b + t);
+        cptr[kk] = (int32_t)(bg + gl);
       }
-      k += __popc(m);
+      continue;
+    }
+    for (int q = 0; q < kColsPerWarp; ++q) {
+      const int64_t col = c0 + q;
+      if (col >= ncol) break;
+      const int64_t b = colstart[col];
+      emit_column(g, b, colstart[col + 1] - b, colptr[col], keys, rowval, cptr, contrib, lane);
     }
   }
 }
@@ -266,7 +382,8 @@ int build_pattern(Ctx* c, const SlotGen& g, int64_t nrow, int64_t ncol, Pattern*
   }
   cursor.release(c);
   // sort + distinct counts (reuse colcnt as per-column nonzero counts)
-  const unsigned gsort = grid_for(ncol, kSortThreads / 32, (int64_t)c->sm_count * 32);
+  const unsigned gsort = grid_for((ncol + kColsPerWarp - 1) / kColsPerWarp, kSortThreads / 32,
+                                  (int64_t)c->sm_count * 32);
   if (ncol > 0) {
     sort_cols_k<<<gsort, kSortThreads, 0, st>>>(colstart.p, ncol, keys.p, colcnt.p);
     ELFEL_LAUNCH_CHECK(c);
