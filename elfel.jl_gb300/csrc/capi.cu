@@ -617,7 +617,8 @@ extern "C" int elfel_fused_elasticity(elfel_sysmat* m, double E, double nu, int3
   }
   {
     Phase ph(c, "integrate_elasticity");
-    ELFEL_TRY(launch_elasticity(c, F.nn_u, F.nel, F.conn_u.p, F.xy_u.p, D, bf, F.tab, F.kstore.p, F.fstore.p));
+    ELFEL_TRY(launch_elasticity(c, F.nn_u, F.nel, F.conn_u.p, F.xy_u.p, D, bf, F.ncurved, F.tab, F.kstore.p,
+                                F.fstore.p));
   }
   ELFEL_TRY(finish_values(m));
   if (ntrac > 0) {

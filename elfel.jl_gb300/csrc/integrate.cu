@@ -879,10 +879,122 @@ __global__ void __launch_bounds__(kIntThreads) elast_k(int64_t nel, const int32_
   write_records(fa, ND, e0, nel, fstore);
 }
 
+// Straight-sided elements (constant Jacobian J, A = J^-1): with the
+// parametric gradients G_a(q) the physical ones are G_a(q) A, and
+//   ke_(a,c),(b,d) = det J sum_q w_q B_(a,c)^T D B_(b,d)
+//                  = sum_(alpha,beta) S^(alpha beta)_ab Phi^cd_(alpha beta),
+//   Phi^cd = adj(J) E^cd adj(J)^T / det J,   E^cd = P_c^T D P_d,
+// where S are the heat kernel's reference tensors (sum_q w_q G_a,alpha
+// G_b,beta) and P_0 g = (g0, 0, g1), P_1 g = (0, g1, g0) build the strain
+// vectors: E^00 = [D00 D02; D20 D22], E^01 = [D02 D01; D22 D21],
+// E^11 = [D22 D21; D12 D11], E^10 = (E^01)^T.  Four multiply-adds per stored
+// entry instead of the per-point loop.  The load vector is det J b P_a.
+template <int NN>
+__global__ void __launch_bounds__(kIntThreads) elast_straight_k(int64_t nel, const int32_t* __restrict__ conn,
+                                                               const double2* __restrict__ xy, const Mat3 D,
+                                                               const double* __restrict__ bforce,
+                                                               const __grid_constant__ QPTab tab,
+                                                               double* __restrict__ kstore,
+                                                               double* __restrict__ fstore) {
+  constexpr int ND = 2 * NN, NS = ND * (ND + 1) / 2, NP = NN * (NN + 1) / 2;
+  constexpr int NT = kIntThreads, LD = NT + 1;
+  extern __shared__ double acc[];  // (NS + ND) * LD
+  __shared__ int32_t sconn[NT * NN];
+  __shared__ double sS[4][NP];  // S^00, S^11, S^01, S^10 of node pairs a <= b, index b(b+1)/2 + a
+  for (int k = threadIdx.x; k < NP; k += NT) {
+    int b = 0;
+    while ((b + 1) * (b + 2) / 2 <= k) ++b;
+    const int a = k - b * (b + 1) / 2;
+    sS[0][k] = tab.S[0][0][a * 6 + b];
+    sS[1][k] = tab.S[1][1][a * 6 + b];
+    sS[2][k] = tab.S[0][1][a * 6 + b];
+    sS[3][k] = tab.S[1][0][a * 6 + b];
+  }
+  const int64_t e0 = (int64_t)blockIdx.x * NT;
+  const int64_t base = e0 * NN, lim = nel * NN;
+  for (int k = threadIdx.x; k < NT * NN; k += NT) {
+    const int64_t gi = base + k;
+    sconn[k] = gi < lim ? __ldg(conn + gi) : 0;
+  }
+  __syncthreads();
+  const int t = threadIdx.x;
+  const int64_t e = e0 + t;
+  double* fa = acc + NS * LD;
+  if (e < nel) {
+    const double2 p0 = __ldg(xy + sconn[t * NN]), p1 = __ldg(xy + sconn[t * NN + 1]),
+                  p2 = __ldg(xy + sconn[t * NN + 2]);
+    const double J11 = p1.x - p0.x, J12 = p2.x - p0.x, J21 = p1.y - p0.y, J22 = p2.y - p0.y;
+    const double det = J11 * J22 - J21 * J12;
+    const double rd = 1.0 / det;
+    // adj(J) = [J22 -J12; -J21 J11];  Phi = adj E adj^T / det
+    const double m00 = J22, m01 = -J12, m10 = -J21, m11 = J11;
+    double phi[4][4];  // (00, 11, 01, 10) x (alpha beta = 00, 11, 01, 10)
+    const double E[3][4] = {{D.a[0][0], D.a[0][2], D.a[2][0], D.a[2][2]},   // E^00 rows
+                            {D.a[2][2], D.a[2][1], D.a[1][2], D.a[1][1]},   // E^11
+                            {D.a[0][2], D.a[0][1], D.a[2][2], D.a[2][1]}};  // E^01
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      const double e00 = E[m][0], e01 = E[m][1], e10 = E[m][2], e11 = E[m][3];
+      // T = E adj^T: T_ij = sum_k E_ik adj_jk
+      const double t00 = e00 * m00 + e01 * m01, t01 = e00 * m10 + e01 * m11;
+      const double t10 = e10 * m00 + e11 * m01, t11 = e10 * m10 + e11 * m11;
+      // adj T
+      phi[m][0] = (m00 * t00 + m01 * t10) * rd;  // alpha beta = 00
+      phi[m][1] = (m10 * t01 + m11 * t11) * rd;  // 11
+      phi[m][2] = (m00 * t01 + m01 * t11) * rd;  // 01
+      phi[m][3] = (m10 * t00 + m11 * t10) * rd;  // 10
+    }
+    // Phi^10 = (Phi^01)^T
+    phi[3][0] = phi[2][0];
+    phi[3][1] = phi[2][1];
+    phi[3][2] = phi[2][3];
+    phi[3][3] = phi[2][2];
+#pragma unroll
+    for (int j = 0; j < ND; ++j) {
+      const int b = j >> 1, dj = j & 1;
+#pragma unroll
+      for (int i = 0; i <= j; ++i) {
+        const int a = i >> 1, ci = i & 1;
+        const int cd = ci == dj ? (ci == 0 ? 0 : 1) : (ci == 0 ? 2 : 3);
+        // node pair (a, b), a <= b here because i <= j
+        const int k = b * (b + 1) / 2 + a;
+        acc[(j * (j + 1) / 2 + i) * LD + t] = sS[0][k] * phi[cd][0] + sS[1][k] * phi[cd][1] +
+                                             sS[2][k] * phi[cd][2] + sS[3][k] * phi[cd][3];
+      }
+    }
+    double b0 = 0.0, b1 = 0.0;
+    if (bforce) {
+      b0 = bforce[2 * e];
+      b1 = bforce[2 * e + 1];
+    }
+#pragma unroll
+    for (int a = 0; a < NN; ++a) {
+      fa[(2 * a) * LD + t] = tab.P[a] * b0 * det;
+      fa[(2 * a + 1) * LD + t] = tab.P[a] * b1 * det;
+    }
+  }
+  write_records<NT>(acc, NS, e0, nel, kstore);
+  __syncthreads();
+  write_records<NT>(fa, ND, e0, nel, fstore);
+}
+
 int launch_elasticity(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* xy, const Mat3& D,
-                      const double* bforce, const QPTab& tab, double* kstore, double* fstore) {
+                      const double* bforce, int64_t ncurved, const QPTab& tab, double* kstore, double* fstore) {
   if (nel == 0) return ELFEL_OK;
   const unsigned grid = grid_for(nel, kIntThreads);
+  if (ncurved == 0) {
+    const size_t sm = (size_t)(nn == 3 ? 21 + 6 : 78 + 12) * (kIntThreads + 1) * sizeof(double);
+    if (nn == 3) {
+      elast_straight_k<3><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, (const double2*)xy, D, bforce, tab,
+                                                                 kstore, fstore);
+    } else {
+      ELFEL_CUDA(c, cudaFuncSetAttribute(elast_straight_k<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      elast_straight_k<6><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, (const double2*)xy, D, bforce, tab,
+                                                                 kstore, fstore);
+    }
+    ELFEL_LAUNCH_CHECK(c);
+    return ELFEL_OK;
+  }
   if (nn == 3) {
     const size_t sm = (size_t)(21 + 6) * (kIntThreads + 1) * sizeof(double);
     elast_k<3><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, (const double2*)xy, D, bforce, tab, kstore, fstore);

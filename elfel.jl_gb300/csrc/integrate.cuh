@@ -75,8 +75,9 @@ int make_shape_tables(int shape, int npts, const double* pc, const double* w, Sh
 int launch_heat_shape(Ctx* c, const ShapeTab& tab, int64_t nel, const int32_t* conn, const double* xy,
                       const double* kappa, double Q, double* kstore, double* fstore);
 
+// ncurved: curved elements of the geometry (0: the straight-sided tensor form).
 int launch_elasticity(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* xy, const Mat3& D,
-                      const double* bforce, const QPTab& tab, double* kstore, double* fstore);
+                      const double* bforce, int64_t ncurved, const QPTab& tab, double* kstore, double* fstore);
 int launch_traction(Ctx* c, int64_t ntrac, const int32_t* edges, const int32_t* conn, int nn, const double* xy,
                     double t0, double t1, double* out);
 int launch_stokes(Ctx* c, int64_t nel, const int32_t* conn, const double* xy, double mu, const QPTab& tab,

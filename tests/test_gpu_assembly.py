@@ -232,3 +232,33 @@ def test_t6_straight_kernel_matches_general(E, gpu):
     assert (K0.row == K1.row).all() and (K0.col == K1.col).all()
     assert (K0.data[far] == K1.data[far]).all()
     assert not (K0.data[~far] == K1.data[~far]).all()
+
+
+@pytest.mark.parametrize("case", ["flat", "kappa_range"])
+def test_t6_pair_and_fp64_paths(E, O, gpu, case):
+    """The straight-sided T6 record is evaluated in float pairs unless an
+    element is strongly distorted (det J' < 1/4 after scaling) or kappa / Q
+    fall outside the pair range; those take the FP64 form.  Flat elements
+    (aspect ratio 40) and coefficients over 580 decades exercise the
+    fallback; every entry matches the oracle to 1e-11 of its column's largest."""
+    if case == "flat":
+        mesh = E.jitter(E.T6block(1.0, 0.025, 8, 8), 0.0003, seed=3)
+        kappa = np.linspace(0.5, 2.0, mesh.nel)
+        Q = -6.0
+    else:
+        mesh = E.jitter(E.T6block(1.0, 1.0, 9, 7), 0.02, seed=4)
+        rng = np.random.default_rng(8)
+        kappa = 10.0 ** rng.uniform(-290, 290, mesh.nel)  # beyond 2^+-900 some take the FP64 form
+        Q = 1e-250
+    fesp = heat_space(E, mesh, E.FEH1_T6())
+    n = E.ndofs(fesp)
+    am = E.start(E.SysmatAssemblerGPU(), n, n)
+    E.assemble_heat(am, E.FEIterator(fesp), E.QPIterator(fesp, {"npts": 3}), kappa, Q)
+    K, F = E.finish(am), am.rhs()
+    K0, F0 = heat_oracle(E, O, mesh, fesp, 3, kappa, Q)
+    assert same_pattern(K, K0)
+    # each entry against its own size (the contributions of one entry share an element scale here)
+    rowmax = np.maximum.reduceat(np.abs(K0.data), K0.indptr[:-1]) if K0.nnz else np.zeros(0)
+    scale = np.repeat(rowmax, np.diff(K0.indptr))
+    assert (np.abs(K.data - K0.data) <= 1e-11 * scale).all()
+    assert np.abs(F - F0).max() <= 1e-11 * np.abs(F0).max()
