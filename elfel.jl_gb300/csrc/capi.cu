@@ -673,7 +673,7 @@ extern "C" int elfel_fused_stokes(elfel_sysmat* m, double mu) {
   Fused& F = m->F;
   {
     Phase ph(c, "integrate_stokes");
-    ELFEL_TRY(launch_stokes(c, F.nel, F.conn_u.p, F.xy_u.p, mu, F.tab, F.kstore.p, F.pmass_store.p));
+    ELFEL_TRY(launch_stokes(c, F.nel, F.conn_u.p, F.xy_u.p, mu, F.ncurved, F.tab, F.kstore.p, F.pmass_store.p));
   }
   {
     Phase ph(c, "reduce_K");

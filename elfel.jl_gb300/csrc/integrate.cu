@@ -317,7 +317,7 @@ __device__ __forceinline__ bool t6r_record_pair(double J11, double J12, double J
                                                 double P6, double* a, double* fa) {
   const int em = max(max(dexp(J11), dexp(J12)), max(dexp(J21), dexp(J22)));
   const int k = em - 1023;
-  const int kk = dexp(kap) - 1023, kq = dexp(Q) - 1023;
+  const int kk = dexp(kap) - 1023, kq = dexp(Q) == 0 ? 0 : dexp(Q) - 1023;  // Q = 0: no scaling needed
   if (em == 0 || k < -400 || k > 400 || kk < -900 || kk > 900 || kq + 2 * k < -900 || kq + 2 * k > 900) return false;
   f2 A, B, C, D, kp, qp, p6, sixth;
   bool ok = split_scaled(J11, k, &A) & split_scaled(J12, k, &B) & split_scaled(J21, k, &C) &
@@ -1150,9 +1150,90 @@ __global__ void __launch_bounds__(kIntThreads) stokes_k(int64_t nel, const int32
   write_records(pa, 3, e0, nel, pmass);
 }
 
-int launch_stokes(Ctx* c, int64_t nel, const int32_t* conn, const double* xy, double mu, const QPTab& tab,
-                  double* kstore, double* pmass) {
+// Straight-sided elements: the scalar Laplacian block is the heat record with
+// kappa = mu (straight_record), the velocity-pressure block
+//   kup_(a,c),j = -sum_q w_q det Np_j g_a,c = -sum_alpha T^alpha_aj adj(J)_alpha,c
+// (T the tabulated sum_q w_q Np_j G_a,alpha, det J g = G adj(J)), and the
+// pressure mass det J Mp_j.
+template <int PAT>
+__global__ void __launch_bounds__(kIntThreads) stokes_straight_k(int64_t nel, const int32_t* __restrict__ conn,
+                                                                const double2* __restrict__ xy, double mu,
+                                                                const __grid_constant__ QPTab tab,
+                                                                double* __restrict__ kstore,
+                                                                double* __restrict__ pmass) {
+  constexpr int NN = 6, NS = 78, NR = NS + 36, NT = kIntThreads, LD = NT + 1;
+  extern __shared__ double acc[];  // (NR + 3 + 21 + 6) * LD
+  __shared__ int32_t sconn[NT * NN];
+  __shared__ double sS[3][21];
+  stage_tensors<NN, NT>(tab, sS);
+  const int64_t e0 = (int64_t)blockIdx.x * NT;
+  const int64_t base = e0 * NN, lim = nel * NN;
+  for (int k = threadIdx.x; k < NT * NN; k += NT) {
+    const int64_t gi = base + k;
+    sconn[k] = gi < lim ? __ldg(conn + gi) : 0;
+  }
+  __syncthreads();
+  const int t = threadIdx.x;
+  const int64_t e = e0 + t;
+  double* pa = acc + NR * LD;
+  double* kb = pa + 3 * LD;  // the scalar block (21 entries) and an unused load vector (6)
+  double* fb = kb + 21 * LD;
+  if (e < nel) {
+    const double2 p0 = __ldg(xy + sconn[t * NN]), p1 = __ldg(xy + sconn[t * NN + 1]),
+                  p2 = __ldg(xy + sconn[t * NN + 2]);
+    straight_record<NN, LD, PAT>(p0.x, p0.y, p1.x, p1.y, p2.x, p2.y, mu, 0.0, sS, tab, kb, fb, t);
+#pragma unroll
+    for (int J = 0; J < 12; ++J)
+#pragma unroll
+      for (int I = 0; I <= J; ++I) {
+        double v = 0.0;
+        if ((I & 1) == (J & 1)) v = kb[((J >> 1) * ((J >> 1) + 1) / 2 + (I >> 1)) * LD + t];
+        acc[(J * (J + 1) / 2 + I) * LD + t] = v;
+      }
+    const double J11 = p1.x - p0.x, J12 = p2.x - p0.x, J21 = p1.y - p0.y, J22 = p2.y - p0.y;
+    const double det = J11 * J22 - J21 * J12;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+#pragma unroll
+      for (int a = 0; a < NN; ++a) {
+        const double t0 = tab.T[0][a * 3 + j], t1 = tab.T[1][a * 3 + j];
+        acc[(NS + 2 * a + 12 * j) * LD + t] = -(t0 * J22 - t1 * J21);
+        acc[(NS + 2 * a + 1 + 12 * j) * LD + t] = -(t1 * J11 - t0 * J12);
+      }
+      pa[j * LD + t] = det * tab.Mp[j];
+    }
+  }
+  write_records<NT>(acc, NR, e0, nel, kstore);
+  __syncthreads();
+  write_records<NT>(pa, 3, e0, nel, pmass);
+}
+
+int launch_stokes(Ctx* c, int64_t nel, const int32_t* conn, const double* xy, double mu, int64_t ncurved,
+                  const QPTab& tab, double* kstore, double* pmass) {
   if (nel == 0) return ELFEL_OK;
+  if (ncurved == 0) {
+    const size_t sm = (size_t)(78 + 36 + 3 + 21 + 6) * (kIntThreads + 1) * sizeof(double);
+    const int pat = heat_pattern(6, tab);
+    const unsigned grid = grid_for(nel, kIntThreads);
+    if (pat == kPatT6R) {
+      ELFEL_CUDA(c, cudaFuncSetAttribute(stokes_straight_k<kPatT6R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)sm));
+      stokes_straight_k<kPatT6R><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, (const double2*)xy, mu, tab,
+                                                                         kstore, pmass);
+    } else if (pat == kPatT6) {
+      ELFEL_CUDA(c, cudaFuncSetAttribute(stokes_straight_k<kPatT6>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)sm));
+      stokes_straight_k<kPatT6><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, (const double2*)xy, mu, tab,
+                                                                        kstore, pmass);
+    } else {
+      ELFEL_CUDA(c, cudaFuncSetAttribute(stokes_straight_k<kPatGeneric>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      stokes_straight_k<kPatGeneric><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, (const double2*)xy, mu, tab,
+                                                                             kstore, pmass);
+    }
+    ELFEL_LAUNCH_CHECK(c);
+    return ELFEL_OK;
+  }
   const size_t sm = (size_t)(78 + 36 + 3) * (kIntThreads + 1) * sizeof(double);
   ELFEL_CUDA(c, cudaFuncSetAttribute(stokes_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   stokes_k<<<grid_for(nel, kIntThreads), kIntThreads, sm, c->stream>>>(nel, conn, (const double2*)xy, mu, tab,

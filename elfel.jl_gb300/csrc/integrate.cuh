@@ -80,7 +80,7 @@ int launch_elasticity(Ctx* c, int nn, int64_t nel, const int32_t* conn, const do
                       const double* bforce, int64_t ncurved, const QPTab& tab, double* kstore, double* fstore);
 int launch_traction(Ctx* c, int64_t ntrac, const int32_t* edges, const int32_t* conn, int nn, const double* xy,
                     double t0, double t1, double* out);
-int launch_stokes(Ctx* c, int64_t nel, const int32_t* conn, const double* xy, double mu, const QPTab& tab,
-                  double* kstore, double* pmass);
+int launch_stokes(Ctx* c, int64_t nel, const int32_t* conn, const double* xy, double mu, int64_t ncurved,
+                  const QPTab& tab, double* kstore, double* pmass);
 
 }  // namespace elfel
