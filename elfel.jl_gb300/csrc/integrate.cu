@@ -257,64 +257,57 @@ int heat_pattern(int nn, const QPTab& t) {
   return kPatT6R;
 }
 
-// The exact-rational T6 record (kPatT6R) in FP64: the fallback of
-// t6r_record_pair for elements outside its accuracy range.
-template <int LD>
-__device__ __forceinline__ void t6r_record_fp64(double J11, double J12, double J21, double J22, double kap, double Q,
-                                                double P6, double* a, double* fa) {
-  const double det = __fma_rn(J11, J22, -__dmul_rn(J21, J12));
-  const double s = __ddiv_rn(kap, det);
-  const double qd = __dmul_rn(Q, det);
-  {
-    const double q11 = __fma_rn(J22, J22, __dmul_rn(J12, J12));
-    const double q22 = __fma_rn(J21, J21, __dmul_rn(J11, J11));
-    const double q12 = __fma_rn(J22, J21, __dmul_rn(J12, J11));
-    const double u = __dsub_rn(q11, q12), v = __dsub_rn(q22, q12);
-    const double s2 = __dmul_rn(s, 0.5), s6 = __dmul_rn(s, 1.0 / 6.0), s23 = __dmul_rn(s, 2.0 / 3.0);
-    const double k6 = -__dmul_rn(u, s23), k15 = -__dmul_rn(v, s23), k11 = -__dmul_rn(q12, s23);
-    const double k9 = __dmul_rn(__dmul_rn(__dadd_rn(u, q22), s23), 2.0);
-    a[0 * LD] = __dmul_rn(__dadd_rn(u, v), s2);
-    a[1 * LD] = __dmul_rn(u, s6);
-    a[2 * LD] = __dmul_rn(q11, s2);
-    a[3 * LD] = __dmul_rn(v, s6);
-    a[4 * LD] = __dmul_rn(q12, s6);
-    a[5 * LD] = __dmul_rn(q22, s2);
-    a[6 * LD] = k6;
-    a[7 * LD] = k6;
-    a[8 * LD] = 0.0;
-    a[9 * LD] = k9;
-    a[10 * LD] = 0.0;
-    a[11 * LD] = k11;
-    a[12 * LD] = k11;
-    a[13 * LD] = __dadd_rn(k15, k15);
-    a[14 * LD] = k9;
-    a[15 * LD] = k15;
-    a[16 * LD] = 0.0;
-    a[17 * LD] = k15;
-    a[18 * LD] = __dadd_rn(k11, k11);
-    a[19 * LD] = __dadd_rn(k6, k6);
-    a[20 * LD] = k9;
-    const double fm = __dmul_rn(qd, P6);
-    fa[0 * LD] = 0.0;
-    fa[1 * LD] = 0.0;
-    fa[2 * LD] = 0.0;
-    fa[3 * LD] = fm;
-    fa[4 * LD] = fm;
-    fa[5 * LD] = fm;
-  }
+// The exact-rational T6 record is determined by 8 base values: the stored K
+// entries k0..k5, k9 (= k14 = k20) and the load at the midside nodes; every
+// other entry is one of them times -4 or -8, or zero (t6r_expand).
+// t6r_scale: code 0: b; 1: -4 b; 2: -8 b; 3: +0, by integer operations only:
+// normal values are scaled exactly by an exponent add; a result above the
+// double range is the infinity of its sign, infinities and NaNs keep their
+// exponent, and subnormal values (below 2^-1022, negligible next to any entry
+// of an element record) become zero of their sign.
+__device__ __forceinline__ double t6r_scale(double b, int code) {
+  const long long bits = __double_as_longlong(b) ^ (long long)(1ull << 63);  // -b
+  const long long sign = bits & (long long)(1ull << 63);
+  const int ex = (int)((bits >> 52) & 0x7ff);
+  const int m = code == 1 ? 2 : 3;
+  long long r = bits + ((long long)m << 52);
+  r = ex == 0 ? sign : r;                                                        // zero or subnormal
+  r = ex == 0x7ff ? bits : r;                                                    // inf, NaN
+  r = (ex != 0 && ex != 0x7ff && ex + m > 2046) ? (sign | 0x7ff0000000000000LL) : r;  // overflow
+  const double scaled = __longlong_as_double(r);
+  return code == 0 ? b : (code == 3 ? 0.0 : scaled);
 }
 
-// The exact-rational T6 record in float pairs (48-bit significands; see
-// floatpair.cuh): J is scaled by 2^-k so that max |J'| is in [1, 2), kappa and
-// Q to [1, 2) by their own powers of two, and the powers come back in the
-// exponents of the results.  Only the 4 coordinate differences and 8 joins
-// to double are FP64 instructions (45 in t6r_record_fp64); the entries that
-// are power-of-two multiples of others are exponent adds.  Elements with
+// The 8 bases in FP64: the fallback of t6r_bases_pair for elements outside
+// its accuracy range.
+__device__ __forceinline__ void t6r_bases_fp64(double J11, double J12, double J21, double J22, double kap, double Q,
+                                               double P6, double* b) {
+  const double det = __fma_rn(J11, J22, -__dmul_rn(J21, J12));
+  const double s = __ddiv_rn(kap, det);
+  const double q11 = __fma_rn(J22, J22, __dmul_rn(J12, J12));
+  const double q22 = __fma_rn(J21, J21, __dmul_rn(J11, J11));
+  const double q12 = __fma_rn(J22, J21, __dmul_rn(J12, J11));
+  const double u = __dsub_rn(q11, q12), v = __dsub_rn(q22, q12);
+  const double s2 = __dmul_rn(s, 0.5), s6 = __dmul_rn(s, 1.0 / 6.0);
+  b[0] = __dmul_rn(__dadd_rn(u, v), s2);
+  b[1] = __dmul_rn(u, s6);
+  b[2] = __dmul_rn(q11, s2);
+  b[3] = __dmul_rn(v, s6);
+  b[4] = __dmul_rn(q12, s6);
+  b[5] = __dmul_rn(q22, s2);
+  b[6] = __dmul_rn(__dmul_rn(__dadd_rn(u, q22), s6), 8.0);
+  b[7] = __dmul_rn(__dmul_rn(Q, det), P6);
+}
+
+// The 8 bases in float pairs (48-bit significands; see floatpair.cuh): J is
+// scaled by 2^-k so that max |J'| is in [1, 2), kappa and Q to [1, 2) by their
+// own powers of two, and the powers come back in the exponents of the
+// results.  Only the 4 coordinate differences (in the caller) and 8 joins to
+// double are FP64 instructions (about 30 in t6r_bases_fp64).  Elements with
 // det J' < 1/4 (strongly distorted: the pair subtraction in det J' would cost
 // more than 2^-42 relative accuracy) return false and take the FP64 form.
-template <int LD>
-__device__ __forceinline__ bool t6r_record_pair(double J11, double J12, double J21, double J22, double kap, double Q,
-                                                double P6, double* a, double* fa) {
+__device__ __forceinline__ bool t6r_bases_pair(double J11, double J12, double J21, double J22, double kap, double Q,
+                                               double P6, double* bs) {
   const int em = max(max(dexp(J11), dexp(J12)), max(dexp(J21), dexp(J22)));
   const int k = em - 1023;
   const int kk = dexp(kap) - 1023, kq = dexp(Q) == 0 ? 0 : dexp(Q) - 1023;  // Q = 0: no scaling needed
@@ -332,40 +325,54 @@ __device__ __forceinline__ bool t6r_record_pair(double J11, double J12, double J
   const f2 u = f2_sub(q11, q12), v = f2_sub(q22, q12);
   const f2 s = f2_div(kp, det);
   const f2 s6 = f2_mul(s, sixth);
-  const double a1 = join_scaled(f2_mul(u, s6), kk);
-  const double a3 = join_scaled(f2_mul(v, s6), kk);
-  const double a4 = join_scaled(f2_mul(q12, s6), kk);
-  const double g8 = join_scaled(f2_mul(f2_add(u, q22), s6), kk + 3);
-  a[0 * LD] = join_scaled(f2_mul(f2_add(u, v), s), kk - 1);
-  a[1 * LD] = a1;
-  a[2 * LD] = join_scaled(f2_mul(q11, s), kk - 1);
-  a[3 * LD] = a3;
-  a[4 * LD] = a4;
-  a[5 * LD] = join_scaled(f2_mul(q22, s), kk - 1);
-  const double k6 = pow2_scale(-a1, 2), k15 = pow2_scale(-a3, 2), k11 = pow2_scale(-a4, 2);
-  a[6 * LD] = k6;
-  a[7 * LD] = k6;
+  bs[0] = join_scaled(f2_mul(f2_add(u, v), s), kk - 1);
+  bs[1] = join_scaled(f2_mul(u, s6), kk);
+  bs[2] = join_scaled(f2_mul(q11, s), kk - 1);
+  bs[3] = join_scaled(f2_mul(v, s6), kk);
+  bs[4] = join_scaled(f2_mul(q12, s6), kk);
+  bs[5] = join_scaled(f2_mul(q22, s), kk - 1);
+  bs[6] = join_scaled(f2_mul(f2_add(u, q22), s6), kk + 3);
+  bs[7] = join_scaled(f2_mul(f2_mul(qp, det), p6), kq + 2 * k);
+  return true;
+}
+
+__device__ __forceinline__ void t6r_bases(double J11, double J12, double J21, double J22, double kap, double Q,
+                                          double P6, double* b) {
+  if (!t6r_bases_pair(J11, J12, J21, J22, kap, Q, P6, b)) t6r_bases_fp64(J11, J12, J21, J22, kap, Q, P6, b);
+}
+
+// The full K (21) and F (6) records from the bases (written out entry by
+// entry, so that the bases stay in registers).
+template <int LD>
+__device__ __forceinline__ void t6r_expand(const double* b, double* a, double* fa) {
+  const double m1 = t6r_scale(b[1], 1), m4 = t6r_scale(b[4], 1), m3 = t6r_scale(b[3], 1);
+  a[0 * LD] = b[0];
+  a[1 * LD] = b[1];
+  a[2 * LD] = b[2];
+  a[3 * LD] = b[3];
+  a[4 * LD] = b[4];
+  a[5 * LD] = b[5];
+  a[6 * LD] = m1;
+  a[7 * LD] = m1;
   a[8 * LD] = 0.0;
-  a[9 * LD] = g8;
+  a[9 * LD] = b[6];
   a[10 * LD] = 0.0;
-  a[11 * LD] = k11;
-  a[12 * LD] = k11;
-  a[13 * LD] = pow2_scale(-a3, 3);
-  a[14 * LD] = g8;
-  a[15 * LD] = k15;
+  a[11 * LD] = m4;
+  a[12 * LD] = m4;
+  a[13 * LD] = t6r_scale(b[3], 2);
+  a[14 * LD] = b[6];
+  a[15 * LD] = m3;
   a[16 * LD] = 0.0;
-  a[17 * LD] = k15;
-  a[18 * LD] = pow2_scale(-a4, 3);
-  a[19 * LD] = pow2_scale(-a1, 3);
-  a[20 * LD] = g8;
-  const double fm = join_scaled(f2_mul(f2_mul(qp, det), p6), kq + 2 * k);
+  a[17 * LD] = m3;
+  a[18 * LD] = t6r_scale(b[4], 2);
+  a[19 * LD] = t6r_scale(b[1], 2);
+  a[20 * LD] = b[6];
   fa[0 * LD] = 0.0;
   fa[1 * LD] = 0.0;
   fa[2 * LD] = 0.0;
-  fa[3 * LD] = fm;
-  fa[4 * LD] = fm;
-  fa[5 * LD] = fm;
-  return true;
+  fa[3 * LD] = b[7];
+  fa[4 * LD] = b[7];
+  fa[5 * LD] = b[7];
 }
 
 // Records of one straight-sided element from its three vertices (reference-
@@ -380,8 +387,9 @@ __device__ __forceinline__ void straight_record(double x0, double y0, double x1,
   const double J11 = __dsub_rn(x1, x0), J12 = __dsub_rn(x2, x0);
   const double J21 = __dsub_rn(y1, y0), J22 = __dsub_rn(y2, y0);
   if (PAT == kPatT6R) {
-    if (!t6r_record_pair<LD>(J11, J12, J21, J22, kap, Q, tab.P[3], acc + t, fa + t))
-      t6r_record_fp64<LD>(J11, J12, J21, J22, kap, Q, tab.P[3], acc + t, fa + t);
+    double bs[8];
+    t6r_bases(J11, J12, J21, J22, kap, Q, tab.P[3], bs);
+    t6r_expand<LD>(bs, acc + t, fa + t);
     return;
   }
   const double det = __fma_rn(J11, J22, -__dmul_rn(J21, J12));
