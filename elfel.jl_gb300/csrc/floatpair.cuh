@@ -126,12 +126,5 @@ __device__ __forceinline__ double join_scaled(f2 v, int e) {
   return __dadd_rn(f2d_bits(v.hi, e), f2d_bits(v.lo, e));
 }
 
-// x * 2^m by an exponent add, for x zero or normal with x * 2^m normal (the
-// caller's range checks guarantee it).
-__device__ __forceinline__ double pow2_scale(double x, int m) {
-  const long long b = __double_as_longlong(x);
-  if ((b & 0x7fffffffffffffffLL) == 0) return x;
-  return __longlong_as_double(b + ((long long)m << 52));
-}
 
 }  // namespace elfel
