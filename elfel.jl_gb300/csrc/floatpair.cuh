@@ -44,6 +44,13 @@ __device__ __forceinline__ f2 two_prod(float a, float b) {
   return {p, __fmaf_rn(a, b, -p)};
 }
 
+// a + b keeping only the error of the leading terms (QD's "sloppy" addition):
+// accurate when a and b have the same sign, as for sums of squares.
+__device__ __forceinline__ f2 f2_add_same_sign(f2 a, f2 b) {
+  const f2 s = two_sum(a.hi, b.hi);
+  return quick_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+
 // a + b with both error terms kept (the accurate QD addition).
 __device__ __forceinline__ f2 f2_add(f2 a, f2 b) {
   f2 s = two_sum(a.hi, b.hi);
@@ -80,8 +87,7 @@ __device__ __forceinline__ f2 f2_div(f2 a, f2 b) {
   const float q2 = __fmul_rn(r.hi, rb);
   r = f2_sub(r, f2_mul_f(b, q2));
   const float q3 = __fmul_rn(r.hi, rb);
-  const f2 q = quick_two_sum(q1, q2);
-  return f2_add(q, {q3, 0.0f});
+  return quick_two_sum(q1, __fadd_rn(q2, q3));  // |q2 + q3| is far below ulp(q1)
 }
 
 // Biased exponent field of a double.

@@ -150,6 +150,21 @@ __device__ __forceinline__ void write_records(const double* acc, int rec, int64_
   }
 }
 
+// Write entries k0 .. k0 + nk - 1 of a CTA's records, staged as
+// acc[kk * (NT + 1) + t], to out[(e0 + t) * rec + k0 + kk].
+template <int NT = kIntThreads>
+__device__ __forceinline__ void write_records_part(const double* acc, int rec, int k0, int nk, int64_t e0,
+                                                   int64_t nel, double* out) {
+  __syncthreads();
+  const int nvalid = (int)min((int64_t)NT, nel - e0);
+  const int total = nvalid * nk;
+  double* dst = out + e0 * rec + k0;
+  for (int L = threadIdx.x; L < total; L += NT) {
+    const int t = L / nk, kk = L - t * nk;
+    dst[(int64_t)t * rec + kk] = acc[kk * (NT + 1) + t];
+  }
+}
+
 // ------------------------------------------------------------------ heat
 // Structural zeros of the T6 reference tensors for quadrature rules that
 // integrate the products of the (linear) parametric gradients exactly, e.g.
@@ -319,8 +334,8 @@ __device__ __forceinline__ bool t6r_bases_pair(double J11, double J12, double J2
   if (!ok) return false;
   const f2 det = f2_sub(f2_mul(A, D), f2_mul(C, B));
   if (!(fabsf(det.hi) >= 0.25f)) return false;
-  const f2 q11 = f2_add(f2_mul(D, D), f2_mul(B, B));
-  const f2 q22 = f2_add(f2_mul(C, C), f2_mul(A, A));
+  const f2 q11 = f2_add_same_sign(f2_mul(D, D), f2_mul(B, B));
+  const f2 q22 = f2_add_same_sign(f2_mul(C, C), f2_mul(A, A));
   const f2 q12 = f2_add(f2_mul(D, C), f2_mul(B, A));
   const f2 u = f2_sub(q11, q12), v = f2_sub(q22, q12);
   const f2 s = f2_div(kp, det);
@@ -524,6 +539,60 @@ __global__ void __launch_bounds__(kIntThreads) heat_t6s_k(int64_t nel, const int
   __syncthreads();
   const int t = threadIdx.x;
   const int64_t e = e0 + t;
+  if (PAT == kPatT6R) {
+    // The 8 bases stay in registers; the 27 record values are staged and
+    // written in three parts through an 11-entry buffer, which keeps the
+    // shared memory per CTA (and with it the occupancy limit) small.
+    double bs[8];
+    if (e < nel) {
+      const double2 p0 = __ldg(xy + sconn[t * NN]), p1 = __ldg(xy + sconn[t * NN + 1]),
+                    p2 = __ldg(xy + sconn[t * NN + 2]);
+      t6r_bases(__dsub_rn(p1.x, p0.x), __dsub_rn(p2.x, p0.x), __dsub_rn(p1.y, p0.y), __dsub_rn(p2.y, p0.y), kappa[e],
+                Q, tab.P[3], bs);
+    }
+    double* a = acc + t;
+    if (e < nel) {
+      const double m1 = t6r_scale(bs[1], 1);
+      a[0 * LD] = bs[0];
+      a[1 * LD] = bs[1];
+      a[2 * LD] = bs[2];
+      a[3 * LD] = bs[3];
+      a[4 * LD] = bs[4];
+      a[5 * LD] = bs[5];
+      a[6 * LD] = m1;
+      a[7 * LD] = m1;
+      a[8 * LD] = 0.0;
+      a[9 * LD] = bs[6];
+      a[10 * LD] = 0.0;
+    }
+    write_records_part<NT>(acc, NS, 0, 11, e0, nel, kstore);
+    __syncthreads();
+    if (e < nel) {
+      const double m4 = t6r_scale(bs[4], 1), m3 = t6r_scale(bs[3], 1);
+      a[0 * LD] = m4;                       // 11
+      a[1 * LD] = m4;                       // 12
+      a[2 * LD] = t6r_scale(bs[3], 2);      // 13
+      a[3 * LD] = bs[6];                    // 14
+      a[4 * LD] = m3;                       // 15
+      a[5 * LD] = 0.0;                      // 16
+      a[6 * LD] = m3;                       // 17
+      a[7 * LD] = t6r_scale(bs[4], 2);      // 18
+      a[8 * LD] = t6r_scale(bs[1], 2);      // 19
+      a[9 * LD] = bs[6];                    // 20
+    }
+    write_records_part<NT>(acc, NS, 11, 10, e0, nel, kstore);
+    __syncthreads();
+    if (e < nel) {
+      a[0 * LD] = 0.0;
+      a[1 * LD] = 0.0;
+      a[2 * LD] = 0.0;
+      a[3 * LD] = bs[7];
+      a[4 * LD] = bs[7];
+      a[5 * LD] = bs[7];
+    }
+    write_records_part<NT>(acc, NN, 0, NN, e0, nel, fstore);
+    return;
+  }
   double* fa = acc + NS * LD;
   if (e < nel) {
     const double2 p0 = __ldg(xy + sconn[t * NN]), p1 = __ldg(xy + sconn[t * NN + 1]),
@@ -572,7 +641,8 @@ int launch_heat(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* 
   if (nn == 3)
     heat_k<3, kPatGeneric><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, p, kappa, Q, straight, tab, kstore, fstore);
   else if (ncurved == 0 && pat == kPatT6R)
-    heat_t6s_k<kPatT6R><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, p, kappa, Q, tab, kstore, fstore);
+    heat_t6s_k<kPatT6R><<<grid, kIntThreads, 11 * (kIntThreads + 1) * sizeof(double), c->stream>>>(
+        nel, conn, p, kappa, Q, tab, kstore, fstore);
   else if (ncurved == 0 && pat == kPatT6)
     heat_t6s_k<kPatT6><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, p, kappa, Q, tab, kstore, fstore);
   else if (ncurved == 0)
