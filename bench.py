@@ -557,11 +557,11 @@ def main():
     ach = alg[dom] / (per[dom] * 1e-3) / 1e9
     # DRAM traffic of one launch of each kernel (dram__bytes_read.sum + dram__bytes_write.sum)
     # measured with ncu on the 700 x 700 case of this workload (980,000 elements; heat_t6s_k<2>
-    # 47.20 + 151.46 MB, reduce_win_k 426.97 + 155.31 MB, reduce_row0_dense_k 94.17 + 8.09 MB),
+    # 47.34 + 151.06 MB, reduce_win_k 426.95 + 155.19 MB, reduce_row0_dense_k 94.18 + 8.28 MB),
     # scaled by the element count; writes still dirty in L2 when a kernel ends are not counted
-    TRAFFIC_PER_ELEMENT = {"integrate_heat": (47.202304e6 + 151.463424e6) / 980000,
-                           "reduce_K": (426.966016e6 + 155.309568e6) / 980000,
-                           "reduce_F": (94.168832e6 + 8.086528e6) / 980000}
+    TRAFFIC_PER_ELEMENT = {"integrate_heat": (47.341056e6 + 151.063040e6) / 980000,
+                           "reduce_K": (426.946560e6 + 155.187456e6) / 980000,
+                           "reduce_F": (94.176768e6 + 8.283392e6) / 980000}
     traffic = TRAFFIC_PER_ELEMENT[dom] * nel if dom in TRAFFIC_PER_ELEMENT else None
     for k, row in kernel_rows.items():
         row["traffic"] = TRAFFIC_PER_ELEMENT[k] * nel if k in TRAFFIC_PER_ELEMENT else None
