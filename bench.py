@@ -542,12 +542,16 @@ def main():
     hbm, peak_kind = read_peaks()
     nslots = nel * 36
     nnz_est = 46 * N * N + 16 * N + 1
+    per = {k: (ms / cnt if cnt else 0.0) for k, (ms, cnt) in phases.items()}
+    # without a reduce_F phase the integration kernel added the load vector
+    # itself (midside DOFs read, the vector written) instead of writing records
+    f_direct = "reduce_F" not in per
     alg = {  # compulsory bytes of each kernel per launch, as designed
-        "integrate_heat": nel * 6 * 4 + mesh.nnodes * 16 + nel * 8 + nel * 21 * 8 + nel * 6 * 8,
+        "integrate_heat": nel * 6 * 4 + mesh.nnodes * 16 + nel * 8 + nel * 21 * 8 +
+                          (nel * 3 * 4 + n * 8 if f_direct else nel * 6 * 8),
         "reduce_K": (nnz_est + 1) * 4 + nslots * 4 + nel * 21 * 8 + nnz_est * 8,
         "reduce_F": (n + 1) * 8 + (n + 1) * 4 + nel * 6 * 4 + nel * 6 * 8 + n * 8,
     }
-    per = {k: (ms / cnt if cnt else 0.0) for k, (ms, cnt) in phases.items()}
     dom = max(per, key=per.get)
     kernel_rows = {k: {"ms_per_launch": per[k], "alg_bytes": alg.get(k),
                        "gbs": (alg[k] / (per[k] * 1e-3) / 1e9) if k in alg and per[k] else None,
@@ -556,10 +560,12 @@ def main():
     asm_bytes = nel * 6 * 4 + mesh.nnodes * 16 + nel * 8 + nnz_est * 8 + n * 8
     ach = alg[dom] / (per[dom] * 1e-3) / 1e9
     # DRAM traffic of one launch of each kernel (dram__bytes_read.sum + dram__bytes_write.sum)
-    # measured with ncu on the 700 x 700 case of this workload (980,000 elements; heat_t6s_k<2>
-    # 47.34 + 151.06 MB, reduce_win_k 426.95 + 155.19 MB, reduce_row0_dense_k 94.18 + 8.28 MB),
-    # scaled by the element count; writes still dirty in L2 when a kernel ends are not counted
-    TRAFFIC_PER_ELEMENT = {"integrate_heat": (47.341056e6 + 151.063040e6) / 980000,
+    # measured with ncu on the 700 x 700 case of this workload (980,000 elements; heat_t6s_k<2, 1>
+    # adding the load vector 86.84 + 121.46 MB, heat_t6s_k<2, 0> writing load records 47.34 +
+    # 151.06 MB, reduce_win_k 426.95 + 155.19 MB, reduce_row0_dense_k 94.18 + 8.28 MB), scaled
+    # by the element count; writes still dirty in L2 when a kernel ends are not counted
+    TRAFFIC_PER_ELEMENT = {"integrate_heat": ((86.844672e6 + 121.461504e6) if f_direct else
+                                              (47.341056e6 + 151.063040e6)) / 980000,
                            "reduce_K": (426.946560e6 + 155.187456e6) / 980000,
                            "reduce_F": (94.176768e6 + 8.283392e6) / 980000}
     traffic = TRAFFIC_PER_ELEMENT[dom] * nel if dom in TRAFFIC_PER_ELEMENT else None
@@ -678,7 +684,7 @@ def main():
                                   f"fused K+F assembly, pattern reused",
                       "elements": nel, "ndofs": n, "nnz": nnz_dev, "l2": "256 MB buffer written between timed steps",
                       "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU"},
-           "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 3 * args.steps, "clocks": clk,
+           "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": (2 if f_direct else 3) * args.steps, "clocks": clk,
            "pcg": pcg, "serve": serve, "fma_rates": rates, "pattern_build_s": pattern_s, "setup_phases_ms": {k: v[0] for k, v in setup_phases.items()},
            "wall_s_timed": wall, "host_mesh_setup_s": host_setup_s}
     if rank == 0:

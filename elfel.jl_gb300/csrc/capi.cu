@@ -9,7 +9,10 @@ using namespace elfel;
 
 namespace elfel {
 
-// Dense vector from a 1 x n pattern: out[c] = sum of the contributions of column c.
+// Dense vector from a 1 x n pattern: out[c] = 0 + the contributions of
+// column c in slot order, as SysvecAssembler adds element vectors into a
+// zeroed vector (Assemblers.jl:194-207; the leading +0 turns a sum of
+// negative zeros into +0, as there).
 __global__ void reduce_row0_dense_k(const int64_t* __restrict__ colptr, const int32_t* __restrict__ cptr,
                                     const int32_t* __restrict__ contrib, const double* __restrict__ store, int64_t n,
                                     double* __restrict__ out) {
@@ -18,10 +21,20 @@ __global__ void reduce_row0_dense_k(const int64_t* __restrict__ colptr, const in
     double s = 0.0;
     if (k1 > k0) {
       const int32_t b = cptr[k0], e = cptr[k0 + 1];
-      s = store[contrib[b]];
+      s = __dadd_rn(0.0, store[contrib[b]]);
       for (int32_t t = b + 1; t < e; ++t) s += store[contrib[t]];
     }
     out[c] = s;
+  }
+}
+
+// *many = 1 when some DOF is a midside node (local nodes 3..5) of more than
+// two T6 elements; cnt (ndofs, zeroed) counts the occurrences.
+__global__ void midside_count_k(const int32_t* __restrict__ dofs, int64_t nel, int32_t* __restrict__ cnt,
+                                int32_t* __restrict__ many) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nel * 3; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = i / 3;
+    if (atomicAdd(cnt + dofs[e * 6 + 3 + (i - e * 3)], 1) >= 2) *many = 1;
   }
 }
 
@@ -463,6 +476,27 @@ int fused_build(elfel_sysmat* m, int64_t ndofs) {
     ELFEL_TRY(F.pmass_store.alloc(c, (size_t)(F.nel * 3 > 0 ? F.nel * 3 : 1)));
     ELFEL_TRY(F.pmass_diag.alloc(c, (size_t)(ndofs > 0 ? ndofs : 1)));
   }
+  F.f_direct_ok = 0;
+  if (F.physics == ELFEL_HEAT && F.shape == ELFEL_SHAPE_TRIANGLE && F.nn_u == 6 && F.ncomp_u == 1 && F.nel > 0) {
+    // the T6 load vector may be added atomically (launch_heat) when no DOF
+    // collects more than two nonzero element contributions
+    DBuf<int32_t> cnt;  // ndofs counters, then the flag
+    int h_many = 1;
+    auto count = [&]() -> int {
+      ELFEL_TRY(cnt.alloc(c, (size_t)ndofs + 1));
+      ELFEL_CUDA(c, cudaMemsetAsync(cnt.p, 0, sizeof(int32_t) * (ndofs + 1), c->stream));
+      midside_count_k<<<grid_for(F.nel * 3, 256, (int64_t)c->sm_count * 16), 256, 0, c->stream>>>(
+          F.dofs_u.p, F.nel, cnt.p, cnt.p + ndofs);
+      ELFEL_LAUNCH_CHECK(c);
+      ELFEL_CUDA(c, cudaMemcpyAsync(&h_many, cnt.p + ndofs, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+      ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+      return ELFEL_OK;
+    };
+    const int rc = count();
+    cnt.release(c);
+    if (rc != ELFEL_OK) return rc;
+    F.f_direct_ok = h_many == 0;
+  }
   ELFEL_TRY(F.straight.alloc(c, (size_t)(F.nel > 0 ? F.nel : 1)));
   if (F.shape == ELFEL_SHAPE_TRIANGLE)
     ELFEL_TRY(launch_straight(c, F.nn_u, F.nel, F.conn_u.p, F.xy_u.p, F.straight.p, &F.ncurved));
@@ -552,13 +586,14 @@ extern "C" int elfel_fused_set_geometry(elfel_sysmat* m, const double* xy) {
   return launch_straight(c, m->F.nn_u, m->F.nel, m->F.conn_u.p, m->F.xy_u.p, m->F.straight.p, &m->F.ncurved);
 }
 
-static int finish_values(elfel_sysmat* m) {
+// rhs_done: the integration kernel already added the load vector into rhs.
+static int finish_values(elfel_sysmat* m, bool rhs_done = false) {
   Ctx* c = &m->h->c;
   {
     Phase ph(c, "reduce_K");
     ELFEL_TRY(reduce_values(c, m->P, m->F.kstore.p, m->vals.p));
   }
-  {
+  if (!rhs_done) {
     Phase ph(c, "reduce_F");
     ELFEL_TRY(reduce_dense(c, m->F.fpat, m->F.fstore.p, m->rhs.p));
   }
@@ -576,15 +611,21 @@ extern "C" int elfel_fused_heat(elfel_sysmat* m, const double* kappa, double Q) 
   Fused& F = m->F;
   if (kappa && F.nel)
     ELFEL_CUDA(c, cudaMemcpyAsync(F.coef.p, kappa, sizeof(double) * F.nel, cudaMemcpyHostToDevice, c->stream));
+  const bool fdirect = F.shape == ELFEL_SHAPE_TRIANGLE && F.f_direct_ok && heat_f_direct(F.nn_u, F.ncurved, F.tab);
   {
     Phase ph(c, "integrate_heat");
-    if (F.shape == ELFEL_SHAPE_TRIANGLE)
+    if (fdirect) {
+      ELFEL_CUDA(c, cudaMemsetAsync(m->rhs.p, 0, sizeof(double) * m->ncol, c->stream));
+      ELFEL_TRY(launch_heat(c, F.nn_u, F.nel, F.conn_u.p, F.xy_u.p, F.coef.p, Q, F.straight.p, F.ncurved, F.tab,
+                            F.kstore.p, F.fstore.p, F.dofs_u.p, m->rhs.p));
+    } else if (F.shape == ELFEL_SHAPE_TRIANGLE) {
       ELFEL_TRY(launch_heat(c, F.nn_u, F.nel, F.conn_u.p, F.xy_u.p, F.coef.p, Q, F.straight.p, F.ncurved, F.tab,
                             F.kstore.p, F.fstore.p));
-    else
+    } else {
       ELFEL_TRY(launch_heat_shape(c, F.stab, F.nel, F.conn_u.p, F.xy_u.p, F.coef.p, Q, F.kstore.p, F.fstore.p));
+    }
   }
-  return finish_values(m);
+  return finish_values(m, fdirect);
 }
 
 extern "C" int elfel_fused_elasticity(elfel_sysmat* m, double E, double nu, int32_t plane_strain,

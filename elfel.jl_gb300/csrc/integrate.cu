@@ -519,12 +519,22 @@ __device__ __forceinline__ void heat_elems(int64_t e0, int64_t nel, const int32_
 // geometry): only the three vertices are gathered and the per-point branch is
 // absent, which keeps the register count, and with it the occupancy, of the
 // triangle kernel.  Same records, bit for bit, as heat_k's straight branch.
-template <int PAT>
+//
+// FDIRECT (exact-rule form only): the load vector is added into the global
+// vector fglob (zeroed beforehand) instead of being written as records.  The
+// exact element load is zero at the vertices and Q det / 6 at the three
+// midside nodes, and the caller guarantees that no DOF is a midside node of
+// more than two elements.  An IEEE sum of at most two terms onto +0 does not
+// depend on their order ((0 + a) + b == (0 + b) + a, signed zeros included),
+// so the atomic additions give the bits of the in-order vector assembly.
+template <int PAT, bool FDIRECT = false>
 __global__ void __launch_bounds__(kIntThreads) heat_t6s_k(int64_t nel, const int32_t* __restrict__ conn,
                                                          const double2* __restrict__ xy,
                                                          const double* __restrict__ kappa, double Q,
                                                          const __grid_constant__ QPTab tab,
-                                                         double* __restrict__ kstore, double* __restrict__ fstore) {
+                                                         double* __restrict__ kstore, double* __restrict__ fstore,
+                                                         const int32_t* __restrict__ dofs = nullptr,
+                                                         double* __restrict__ fglob = nullptr) {
   constexpr int NN = 6, NS = 21, NT = kIntThreads, LD = NT + 1;
   extern __shared__ double acc[];  // (NS + NN) * LD
   __shared__ int32_t sconn[NT * NN];
@@ -581,6 +591,15 @@ __global__ void __launch_bounds__(kIntThreads) heat_t6s_k(int64_t nel, const int
       a[9 * LD] = bs[6];                    // 20
     }
     write_records_part<NT>(acc, NS, 11, 10, e0, nel, kstore);
+    if (FDIRECT) {
+      if (e < nel) {
+        const int32_t* d = dofs + e * NN;
+        atomicAdd(fglob + __ldg(d + 3), bs[7]);
+        atomicAdd(fglob + __ldg(d + 4), bs[7]);
+        atomicAdd(fglob + __ldg(d + 5), bs[7]);
+      }
+      return;
+    }
     __syncthreads();
     if (e < nel) {
       a[0 * LD] = 0.0;
@@ -631,13 +650,26 @@ __global__ void __launch_bounds__(NT) heat_batch_k(const HeatJob* __restrict__ j
 
 static size_t heat_smem(int nn, int nt) { return (size_t)(nn == 3 ? 6 + 3 : 21 + 6) * (nt + 1) * sizeof(double); }
 
+bool heat_f_direct(int nn, int64_t ncurved, const QPTab& tab) {
+  return nn == 6 && ncurved == 0 && heat_pattern(6, tab) == kPatT6R;
+}
+
 int launch_heat(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* xy, const double* kappa, double Q,
-                const uint8_t* straight, int64_t ncurved, const QPTab& tab, double* kstore, double* fstore) {
+                const uint8_t* straight, int64_t ncurved, const QPTab& tab, double* kstore, double* fstore,
+                const int32_t* dofs, double* fglob) {
   if (nel == 0) return ELFEL_OK;
   const unsigned grid = grid_for(nel, kIntThreads);
   const double2* p = (const double2*)xy;
   const size_t sm = heat_smem(nn, kIntThreads);
   const int pat = nn == 6 ? heat_pattern(6, tab) : kPatGeneric;
+  if (fglob) {
+    if (!heat_f_direct(nn, ncurved, tab) || !dofs)
+      return fail(c, ELFEL_ERR_STATE, "heat: direct load-vector assembly needs the straight-sided exact T6 form");
+    heat_t6s_k<kPatT6R, true><<<grid, kIntThreads, 11 * (kIntThreads + 1) * sizeof(double), c->stream>>>(
+        nel, conn, p, kappa, Q, tab, kstore, fstore, dofs, fglob);
+    ELFEL_LAUNCH_CHECK(c);
+    return ELFEL_OK;
+  }
   if (nn == 3)
     heat_k<3, kPatGeneric><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, p, kappa, Q, straight, tab, kstore, fstore);
   else if (ncurved == 0 && pat == kPatT6R)

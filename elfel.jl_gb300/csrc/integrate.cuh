@@ -33,9 +33,17 @@ int make_tables(int nn, int npts, const double* pc, const double* w, QPTab* t);
 
 // straight: per-element straight-sided flags of the geometry (launch_straight;
 // unused for T3, whose elements always are); ncurved: the number of elements
-// without the flag (0 selects the straight-only T6 kernel).
+// without the flag (0 selects the straight-only T6 kernel).  fglob non-null:
+// the load vector is added into fglob (zeroed, indexed by the nel x 6 table
+// dofs) instead of being written to fstore; allowed only when
+// heat_f_direct() holds and no DOF is a midside node of more than two
+// elements.
 int launch_heat(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* xy, const double* kappa, double Q,
-                const uint8_t* straight, int64_t ncurved, const QPTab& tab, double* kstore, double* fstore);
+                const uint8_t* straight, int64_t ncurved, const QPTab& tab, double* kstore, double* fstore,
+                const int32_t* dofs = nullptr, double* fglob = nullptr);
+// True when the heat load vector of a T6 mesh takes the exact form (zero at
+// the vertices, Q det / 6 at the midside nodes) in the straight-only kernel.
+bool heat_f_direct(int nn, int64_t ncurved, const QPTab& tab);
 // Per-element straight-sided flags (1: every midside node is the exact
 // midpoint of its edge) of a mesh and the count of curved elements;
 // recomputed whenever the coordinates change.  Synchronises the stream.

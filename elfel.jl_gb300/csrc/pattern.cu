@@ -528,6 +528,7 @@ __global__ void reduce_batch_k(const RedJob* __restrict__ jobs, int njobs) {
   }
   const int32_t b = J.cptr[slot], e = J.cptr[slot + 1];
   double s = J.store[J.contrib[b]];
+  if (J.colptr) s = __dadd_rn(0.0, s);  // a vector starts from a zeroed one (SysvecAssembler)
   for (int32_t t = b + 1; t < e; ++t) s += J.store[J.contrib[t]];
   J.out[k] = s;
 }

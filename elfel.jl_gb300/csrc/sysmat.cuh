@@ -151,8 +151,10 @@ struct Fused {
   elfel_block_desc block;
   DBuf<uint8_t> straight;            // nel: 1 = straight-sided element (of the current coordinates)
   int64_t ncurved = -1;              // elements without the flag (-1: not computed)
+  int f_direct_ok = 0;               // T6 heat: no DOF is a midside node of more than two elements
   void release(Ctx* c) {
     is_block = 0;
+    f_direct_ok = 0;
     shape = ELFEL_SHAPE_TRIANGLE;
     sdim = 2;
     ncurved = -1;

@@ -232,6 +232,49 @@ def test_t6_straight_kernel_matches_general(E, gpu):
     assert (K0.row == K1.row).all() and (K0.col == K1.col).all()
     assert (K0.data[far] == K1.data[far]).all()
     assert not (K0.data[~far] == K1.data[~far]).all()
+    # the load vector: added by the straight-only kernel, reduced from records
+    # by the general one; the same bits (signed zeros included) away from it
+    assert (F0[~near].view(np.int64) == F1[~near].view(np.int64)).all()
+
+
+def _phases(am, Q):
+    ctx = am._hd.ctx
+    ctx.profile(True)
+    am.heat(None, Q)
+    ph = ctx.phases()
+    ctx.profile(False)
+    return ph
+
+
+@pytest.mark.parametrize("case", ["conforming", "mirrored_Q0", "duplicate_element"])
+def test_t6_load_vector_paths(E, O, gpu, case):
+    """The straight-only exact T6 kernel adds the load vector into the global
+    vector when no DOF is a midside node of more than two elements (a sum of
+    at most two terms onto +0 is independent of their order); otherwise the
+    records go through the in-order reduction.  Both start from +0 as the
+    zeroed vector of SysvecAssembler (Assemblers.jl:194-207): Q = 0 on
+    clockwise elements (element loads of -0) gives +0 everywhere."""
+    mesh = E.T6block(1.0, 1.0, 9, 8)
+    Q = -6.0
+    if case == "mirrored_Q0":
+        mesh = E.Mesh("T6", mesh.conn, mesh.xy * np.array([-1.0, 1.0]))
+        Q = 0.0
+    if case == "duplicate_element":
+        mesh = E.Mesh("T6", np.vstack([mesh.conn, mesh.conn[mesh.nel // 2]]), mesh.xy)
+    fesp = heat_space(E, mesh, E.FEH1_T6())
+    n = E.ndofs(fesp)
+    kappa = np.linspace(0.5, 2.0, mesh.nel)
+    am = E.start(E.SysmatAssemblerGPU(), n, n)
+    E.assemble_heat(am, E.FEIterator(fesp), E.QPIterator(fesp, {"npts": 3}), kappa, Q)
+    ph = _phases(am, Q)
+    assert ("reduce_F" in ph) == (case == "duplicate_element")
+    K, F = E.finish(am), am.rhs()
+    K0, F0 = heat_oracle(E, O, mesh, fesp, 3, kappa, Q)
+    assert same_pattern(K, K0) and close(K.data, K0.data)
+    if Q == 0.0:
+        assert (F.view(np.int64) == 0).all() and (F0.view(np.int64) == 0).all()
+    else:
+        assert close(F, F0)
 
 
 @pytest.mark.parametrize("case", ["flat", "kappa_range"])
