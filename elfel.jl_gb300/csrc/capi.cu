@@ -355,6 +355,45 @@ static int upload_space(Ctx* c, const elfel_space& s, int64_t ndofs, int sdim, D
   return ELFEL_OK;
 }
 
+// Upload of the mesh tables when every host array is device-readable
+// (host_device_ptr): the element DOFs, which the pattern build reads, on the
+// context stream; connectivity and coordinates on the auxiliary stream, so
+// that they cross the host link while the pattern is built (fused_build joins
+// before it uses them).  The index checks are deferred: bad[0..3] (primary
+// connectivity, primary DOFs, pressure connectivity, pressure DOFs) are read
+// once the work of both streams is done.
+static bool tables_readable(Ctx* c, const elfel_space& s) {
+  if (s.nel < 0 || s.nnodes < 0 || !s.conn || !s.eldofs || (s.nnodes > 0 && !s.xy))
+    return false;  // upload_space reports the error
+  return (s.nel == 0 || (host_device_ptr(c, s.conn) && host_device_ptr(c, s.eldofs))) &&
+         (s.nnodes == 0 || host_device_ptr(c, s.xy));
+}
+
+// Step 1 (context stream): the buffers, then the element DOFs.
+static int upload_direct_dofs(Ctx* c, const elfel_space& s, int64_t ndofs, int sdim, DBuf<int32_t>* conn,
+                              DBuf<double>* xy, DBuf<int32_t>* dofs, int* bad_dofs) {
+  const int64_t nc = s.nel * s.nodes_per_elem, nd = s.nel * s.nodes_per_elem * s.ncomp;
+  ELFEL_TRY(conn->alloc(c, (size_t)(nc > 0 ? nc : 1)));
+  ELFEL_TRY(dofs->alloc(c, (size_t)(nd > 0 ? nd : 1)));
+  if (xy) ELFEL_TRY(xy->alloc(c, (size_t)(s.nnodes > 0 ? sdim * s.nnodes : 1)));
+  return to_index32_direct(c, c->stream, (const int64_t*)host_device_ptr(c, s.eldofs), nd, ndofs, dofs->p,
+                           bad_dofs);
+}
+
+// Step 2 (auxiliary stream, forked after step 1's allocations): connectivity
+// and coordinates.
+static int upload_direct_rest(Ctx* c, const elfel_space& s, int sdim, DBuf<int32_t>* conn, DBuf<double>* xy,
+                              int* bad_conn, cudaStream_t aux) {
+  ELFEL_TRY(to_index32_direct(c, aux, (const int64_t*)host_device_ptr(c, s.conn), s.nel * s.nodes_per_elem,
+                              s.nnodes, conn->p, bad_conn));
+  if (xy && s.nnodes) {
+    int pinned = 0;
+    const double* src = (const double*)host_device_ptr(c, s.xy, &pinned);
+    ELFEL_TRY(copy_host_f64(c, aux, pinned ? s.xy : src, pinned, sdim * s.nnodes, xy->p));
+  }
+  return ELFEL_OK;
+}
+
 extern "C" int elfel_fused_setup(elfel_sysmat* m, const elfel_fused_desc* d) {
   CHECK_FREE(m);
   Ctx* c = &m->h->c;
@@ -404,13 +443,45 @@ extern "C" int elfel_fused_setup(elfel_sysmat* m, const elfel_fused_desc* d) {
     ELFEL_TRY(make_tables(u.nodes_per_elem, d->npts, d->qp_coords, d->qp_weights, &F.tab));
   else
     ELFEL_TRY(make_shape_tables(F.shape, d->npts, d->qp_coords, d->qp_weights, &F.stab));
-  ELFEL_TRY(upload_space(c, u, d->ndofs, sdim, &F.conn_u, &F.xy_u, &F.dofs_u, "primary"));
-  if (d->physics == ELFEL_STOKES) {
+  const bool stokes = d->physics == ELFEL_STOKES;
+  if (stokes) {
     F.nn_p = 3;
     F.nnodes_p = d->p.nnodes;
-    ELFEL_TRY(upload_space(c, d->p, d->ndofs, 2, &F.conn_p, nullptr, &F.dofs_p, "pressure"));
   }
-  return fused_build(m, d->ndofs);
+  if (!tables_readable(c, u) || (stokes && !tables_readable(c, d->p))) {
+    ELFEL_TRY(upload_space(c, u, d->ndofs, sdim, &F.conn_u, &F.xy_u, &F.dofs_u, "primary"));
+    if (stokes) ELFEL_TRY(upload_space(c, d->p, d->ndofs, 2, &F.conn_p, nullptr, &F.dofs_p, "pressure"));
+    return fused_build(m, d->ndofs);
+  }
+  DBuf<int> bad;
+  auto run = [&]() -> int {
+    ELFEL_TRY(bad.alloc(c, 4));
+    ELFEL_CUDA(c, cudaMemsetAsync(bad.p, 0, 4 * sizeof(int), c->stream));
+    ELFEL_TRY(upload_direct_dofs(c, u, d->ndofs, sdim, &F.conn_u, &F.xy_u, &F.dofs_u, bad.p + 1));
+    if (stokes) ELFEL_TRY(upload_direct_dofs(c, d->p, d->ndofs, 2, &F.conn_p, nullptr, &F.dofs_p, bad.p + 3));
+    cudaStream_t aux;
+    ELFEL_TRY(aux_fork(c, &aux));  // after the allocations, which the auxiliary stream then may use
+    ELFEL_TRY(upload_direct_rest(c, u, sdim, &F.conn_u, &F.xy_u, bad.p, aux));
+    if (stokes) ELFEL_TRY(upload_direct_rest(c, d->p, 2, &F.conn_p, nullptr, bad.p + 2, aux));
+    ELFEL_TRY(fused_build(m, d->ndofs));  // joins the auxiliary stream before using conn / xy
+    int hb[4] = {0, 0, 0, 0};
+    ELFEL_CUDA(c, cudaMemcpyAsync(hb, bad.p, sizeof(hb), cudaMemcpyDeviceToHost, c->stream));
+    ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+    static const char* what[4] = {"primary connectivity", "primary eldofs", "pressure connectivity",
+                                  "pressure eldofs"};
+    const int64_t lim[4] = {u.nnodes, d->ndofs, stokes ? d->p.nnodes : 0, d->ndofs};
+    for (int k = 0; k < 4; ++k)
+      if (hb[k]) return fail(c, ELFEL_ERR_ARG, "%s: entry outside 1..%lld", what[k], (long long)lim[k]);
+    return ELFEL_OK;
+  };
+  const int rc = run();
+  if (rc != ELFEL_OK) {
+    aux_join(c);
+    cudaStreamSynchronize(c->stream);
+    release_all(m);
+  }
+  bad.release(c);
+  return rc;
 }
 
 namespace elfel {
@@ -461,7 +532,7 @@ int fused_build(elfel_sysmat* m, int64_t ndofs) {
   fg.b[0].nc = nedof;
   fg.slots_per_elem = nedof;
   fg.store_per_elem = nedof;
-  ELFEL_TRY(build_pattern(c, fg, 1, ndofs, &F.fpat));
+  F.fpat_built = 0;  // built on first use (ensure_fpat)
   if (F.physics == ELFEL_STOKES) {
     SlotGen pg;
     pg.nel = F.nel;
@@ -476,6 +547,7 @@ int fused_build(elfel_sysmat* m, int64_t ndofs) {
     ELFEL_TRY(F.pmass_store.alloc(c, (size_t)(F.nel * 3 > 0 ? F.nel * 3 : 1)));
     ELFEL_TRY(F.pmass_diag.alloc(c, (size_t)(ndofs > 0 ? ndofs : 1)));
   }
+  ELFEL_TRY(aux_join(c));  // tables uploaded on the auxiliary stream
   F.f_direct_ok = 0;
   if (F.physics == ELFEL_HEAT && F.shape == ELFEL_SHAPE_TRIANGLE && F.nn_u == 6 && F.ncomp_u == 1 && F.nel > 0) {
     // the T6 load vector may be added atomically (launch_heat) when no DOF
@@ -586,6 +658,16 @@ extern "C" int elfel_fused_set_geometry(elfel_sysmat* m, const double* xy) {
   return launch_straight(c, m->F.nn_u, m->F.nel, m->F.conn_u.p, m->F.xy_u.p, m->F.straight.p, &m->F.ncurved);
 }
 
+int elfel::ensure_fpat(elfel_sysmat* m) {
+  Fused& F = m->F;
+  if (F.fpat_built) return ELFEL_OK;
+  Ctx* c = &m->h->c;
+  Phase ph(c, "pattern_F");
+  ELFEL_TRY(build_pattern(c, F.fgen, 1, m->ncol, &F.fpat));
+  F.fpat_built = 1;
+  return ELFEL_OK;
+}
+
 // rhs_done: the integration kernel already added the load vector into rhs.
 static int finish_values(elfel_sysmat* m, bool rhs_done = false) {
   Ctx* c = &m->h->c;
@@ -594,6 +676,7 @@ static int finish_values(elfel_sysmat* m, bool rhs_done = false) {
     ELFEL_TRY(reduce_values(c, m->P, m->F.kstore.p, m->vals.p));
   }
   if (!rhs_done) {
+    ELFEL_TRY(ensure_fpat(m));
     Phase ph(c, "reduce_F");
     ELFEL_TRY(reduce_dense(c, m->F.fpat, m->F.fstore.p, m->rhs.p));
   }

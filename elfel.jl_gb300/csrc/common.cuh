@@ -26,6 +26,9 @@ struct Ctx {
   int device = 0;
   cudaStream_t stream = nullptr;      // stream all work is issued on
   cudaStream_t own_stream = nullptr;  // the context's own stream
+  cudaStream_t aux = nullptr;         // second stream for uploads that overlap work on `stream` (lazy)
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  int pageable_access = 0;            // kernels may read pageable host memory (ATS)
   cudaMemPool_t pool = nullptr;  // the context's stream-ordered pool (keeps freed memory for reuse)
   int64_t budget = 0;       // bytes the context may hold on the device (0 = unlimited)
   int64_t in_use = 0;       // bytes currently held
@@ -93,6 +96,18 @@ int fail(Ctx* c, int code, const char* fmt, ...);
   } while (0)
 
 #define ELFEL_LAUNCH_CHECK(ctx) ELFEL_CUDA(ctx, cudaGetLastError())
+
+// The context's auxiliary stream, made to wait for the work issued on
+// c->stream so far (fork); join() makes c->stream wait for it.
+int aux_fork(Ctx* c, cudaStream_t* aux);
+int aux_join(Ctx* c);
+
+// A device-usable address of a host array: the device address of pinned
+// memory, the host address itself where kernels read pageable memory (ATS),
+// else nullptr (the caller then copies with cudaMemcpyAsync).
+// *pinned (optional) = 1 for page-locked memory (copy engines work
+// asynchronously on it).
+const void* host_device_ptr(Ctx* c, const void* host, int* pinned = nullptr);
 
 // Device allocation accounted against the context budget (stream-ordered).
 int dalloc(Ctx* c, void** p, size_t bytes);

@@ -217,6 +217,10 @@ extern "C" int elfel_ctx_create(int device, int64_t mem_budget_bytes, elfel_ctx*
       h->c.pool = nullptr;  // the device's default pool then
     }
   }
+  if (cudaDeviceGetAttribute(&h->c.pageable_access, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) {
+    cudaGetLastError();
+    h->c.pageable_access = 0;
+  }
   const char* tr = getenv("ELFEL_TRACE");
   h->c.trace = (tr && tr[0] == '1') ? 1 : 0;
   const char* tu = getenv("ELFEL_TUNE");
@@ -226,6 +230,41 @@ extern "C" int elfel_ctx_create(int device, int64_t mem_budget_bytes, elfel_ctx*
 }
 
 namespace elfel {
+
+int aux_fork(Ctx* c, cudaStream_t* aux) {
+  if (!c->aux) {
+    ELFEL_CUDA(c, cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking));
+    ELFEL_CUDA(c, cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    ELFEL_CUDA(c, cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+  }
+  ELFEL_CUDA(c, cudaEventRecord(c->ev_fork, c->stream));
+  ELFEL_CUDA(c, cudaStreamWaitEvent(c->aux, c->ev_fork, 0));
+  *aux = c->aux;
+  return ELFEL_OK;
+}
+
+int aux_join(Ctx* c) {
+  if (!c->aux) return ELFEL_OK;
+  ELFEL_CUDA(c, cudaEventRecord(c->ev_join, c->aux));
+  ELFEL_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev_join, 0));
+  return ELFEL_OK;
+}
+
+const void* host_device_ptr(Ctx* c, const void* host, int* pinned) {
+  if (pinned) *pinned = 0;
+  if (!host) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return host;
+  if (a.type == cudaMemoryTypeHost) {
+    if (pinned) *pinned = a.devicePointer != nullptr;
+    return a.devicePointer;
+  }
+  return c->pageable_access ? host : nullptr;
+}
 
 void tune_record(Ctx* c, const char* key, const std::string& cand, int best, const std::vector<double>& ms) {
   std::string line = std::string(key) + ":";
@@ -319,6 +358,12 @@ extern "C" int elfel_ctx_destroy(elfel_ctx* h) {
   cudaStreamSynchronize(h->c.stream);
   clear_phases(&h->c);
   if (h->c.own_stream) cudaStreamDestroy(h->c.own_stream);
+  if (h->c.aux) {
+    cudaStreamSynchronize(h->c.aux);
+    cudaStreamDestroy(h->c.aux);
+  }
+  if (h->c.ev_fork) cudaEventDestroy(h->c.ev_fork);
+  if (h->c.ev_join) cudaEventDestroy(h->c.ev_join);
   // memory still held by live systems is released once they free it
   if (h->c.pool) cudaMemPoolDestroy(h->c.pool);
   delete h;

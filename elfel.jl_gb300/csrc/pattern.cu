@@ -22,6 +22,24 @@ namespace elfel {
 constexpr int kSortThreads = 256;           // 8 warps, one column each
 constexpr int kSortCap = 256;               // keys per warp sorted in shared memory
 
+// Block mode: one thread per column group (one atomic per group instead of
+// one per slot).  The row tables are the uploaded element DOF tables, range
+// checked on upload; the column is checked here.
+__global__ void count_groups_k(SlotGen g, int G, int64_t ngroups, int32_t* colcnt, int64_t ncol, int* bad) {
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < ngroups; q += (int64_t)gridDim.x * blockDim.x) {
+    int32_t c;
+    int64_t s0;
+    int len;
+    const int32_t* rt;
+    group_info(g, G, q, c, s0, len, rt);
+    if (c < 0 || c >= ncol) {
+      atomicExch(bad, 1);
+      continue;
+    }
+    atomicAdd(&colcnt[c], len);
+  }
+}
+
 __global__ void count_cols_k(SlotGen g, int64_t n, int32_t* colcnt, int64_t ncol, int64_t nrow, int* bad) {
   for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
     int32_t r, c;
@@ -217,6 +235,24 @@ __global__ void __launch_bounds__(kSortThreads) sort_cols_k(const int64_t* colst
       if (gl == 0 && cg < ncol) nnzcnt[cg] = __popc(m & (0xffu << (grp * 8)));
       continue;
     }
+    if (__all_sync(0xffffffffu, ng <= 16)) {
+      // two columns at a time, one per half warp (T6 midside columns: 12 keys)
+      const int h = lane >> 4, hl = lane & 15;
+#pragma unroll
+      for (int r = 0; r < kColsPerWarp / 2; ++r) {
+        const int q = 2 * r + h;
+        const int64_t b = __shfl_sync(0xffffffffu, bg, q * 8);
+        const int n = __shfl_sync(0xffffffffu, ng, q * 8);
+        uint64_t v = hl < n ? keys[b + hl] : ~0ull;
+        v = reg_sort<16>(v, hl);  // partners lane ^ j (j < 16) stay inside the half
+        const uint64_t pv = __shfl_up_sync(0xffffffffu, v, 1, 16);
+        const bool first = hl < n && (hl == 0 || (v >> 32) != (pv >> 32));
+        const unsigned m = __ballot_sync(0xffffffffu, first);
+        if (hl < n) keys[b + hl] = v;
+        if (hl == 0 && c0 + q < ncol) nnzcnt[c0 + q] = __popc(m & (0xffffu << (h * 16)));
+      }
+      continue;
+    }
     for (int q = 0; q < kColsPerWarp; ++q) {
       const int64_t col = c0 + q;
       if (col >= ncol) break;
@@ -286,6 +322,33 @@ __global__ void emit_k(SlotGen g, const int64_t* colstart, const int64_t* colptr
       }
       continue;
     }
+    if (__all_sync(0xffffffffu, ng <= 16)) {
+      // two columns at a time, one per half warp
+      const int h = lane >> 4, hl = lane & 15;
+      const unsigned half = 0xffffu << (h * 16);
+#pragma unroll
+      for (int r = 0; r < kColsPerWarp / 2; ++r) {
+        const int q = 2 * r + h;
+        const int64_t b = __shfl_sync(0xffffffffu, bg, q * 8);
+        const int n = __shfl_sync(0xffffffffu, ng, q * 8);
+        const uint64_t key = hl < n ? keys[b + hl] : 0ull;
+        const uint64_t pkey = __shfl_up_sync(0xffffffffu, key, 1, 16);
+        const bool first = hl < n && (hl == 0 || (key >> 32) != (pkey >> 32));
+        if (hl < n) {
+          int32_t rr, cc;
+          int64_t st;
+          slot_rc(g, (int64_t)(key & 0xffffffffull), rr, cc, st);
+          contrib[b + hl] = (int32_t)st;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, first);
+        if (first) {
+          const int64_t kk = colptr[c0 + q] + __popc(m & half & below);
+          rowval[kk] = (int32_t)(key >> 32);
+          cptr[kk] = (int32_t)(b + hl);
+        }
+      }
+      continue;
+    }
     for (int q = 0; q < kColsPerWarp; ++q) {
       const int64_t col = c0 + q;
       if (col >= ncol) break;
@@ -342,7 +405,9 @@ __global__ void window_order_k(const int32_t* __restrict__ cptr, int64_t nnz, ui
   }
 }
 
-int build_pattern(Ctx* c, const SlotGen& g, int64_t nrow, int64_t ncol, Pattern* P) {
+int build_pattern(Ctx* c, const SlotGen& g0, int64_t nrow, int64_t ncol, Pattern* P) {
+  SlotGen g = g0;
+  g.prepare();
   P->release(c);
   const int64_t M = g.total();
   if (M >= (int64_t)0x7fffffff)
@@ -365,8 +430,14 @@ int build_pattern(Ctx* c, const SlotGen& g, int64_t nrow, int64_t ncol, Pattern*
   ELFEL_CUDA(c, cudaMemsetAsync(cursor.p, 0, sizeof(int32_t) * (ncol + 1), st));
   ELFEL_CUDA(c, cudaMemsetAsync(bad.p, 0, sizeof(int), st));
   const unsigned gs = grid_for(M, 256, (int64_t)c->sm_count * 16);
+  const int G = groups_per_elem(g);
+  const int64_t ngroups = g.nblocks ? g.nel * (int64_t)G : 0;
   if (M > 0) {
-    count_cols_k<<<gs, 256, 0, st>>>(g, M, colcnt.p, ncol, nrow, bad.p);
+    if (g.nblocks)
+      count_groups_k<<<grid_for(ngroups, 256, (int64_t)c->sm_count * 16), 256, 0, st>>>(g, G, ngroups, colcnt.p,
+                                                                                        ncol, bad.p);
+    else
+      count_cols_k<<<gs, 256, 0, st>>>(g, M, colcnt.p, ncol, nrow, bad.p);
     ELFEL_LAUNCH_CHECK(c);
   }
   int hbad = 0;
@@ -404,7 +475,7 @@ int build_pattern(Ctx* c, const SlotGen& g, int64_t nrow, int64_t ncol, Pattern*
   }
   set_last_k<<<1, 1, 0, st>>>(P->cptr.p, nnz, M);
   ELFEL_LAUNCH_CHECK(c);
-  if (nnz > 0) {
+  if (nnz > 0 && nrow > 1) {  // 1 x n patterns (vectors) are reduced without windows
     const int64_t nwin = (nnz + kReduceWindow - 1) / kReduceWindow;
     ELFEL_TRY(P->perm.alloc(c, (size_t)(nwin * kReduceWindow)));
     window_order_k<<<grid_for(nwin, 8, (int64_t)c->sm_count * 16), 256, 0, st>>>(P->cptr.p, nnz, P->perm.p);
@@ -565,6 +636,60 @@ __global__ void to_index32_k(const int64_t* src, int64_t n, int64_t limit, int32
       dst[i] = (int32_t)(v - 1);
     }
   }
+}
+
+// The same conversion reading the (device-readable) host array directly:
+// four independent loads per thread keep enough bytes in flight over the
+// host link with a small grid, which leaves most of the SMs to the work on
+// other streams.
+__global__ void to_index32_host_k(const int64_t* __restrict__ src, int64_t n, int64_t limit, int32_t* __restrict__ dst,
+                                  int* __restrict__ bad) {
+  constexpr int U = 4;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i0 < n; i0 += U * stride) {
+    int64_t v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) v[u] = i0 + u * stride < n ? src[i0 + u * stride] : 1;
+    bool b = false;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const bool out = v[u] < 1 || v[u] > limit;
+      b |= out;
+      if (i0 + u * stride < n) dst[i0 + u * stride] = out ? 0 : (int32_t)(v[u] - 1);
+    }
+    if (b) atomicExch(bad, 1);
+  }
+}
+
+__global__ void copy_host_f64_k(const double* __restrict__ src, int64_t n, double* __restrict__ dst) {
+  constexpr int U = 4;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i0 < n; i0 += U * stride) {
+    double v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) v[u] = i0 + u * stride < n ? src[i0 + u * stride] : 0.0;
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (i0 + u * stride < n) dst[i0 + u * stride] = v[u];
+  }
+}
+
+int to_index32_direct(Ctx* c, cudaStream_t st, const int64_t* src, int64_t n, int64_t limit, int32_t* dst, int* bad) {
+  if (n == 0) return ELFEL_OK;
+  to_index32_host_k<<<grid_for(n, 256 * 4, (int64_t)c->sm_count * 2), 256, 0, st>>>(src, n, limit, dst, bad);
+  ELFEL_LAUNCH_CHECK(c);
+  return ELFEL_OK;
+}
+
+int copy_host_f64(Ctx* c, cudaStream_t st, const double* src, int pinned, int64_t n, double* dst) {
+  if (n == 0) return ELFEL_OK;
+  if (pinned) {
+    ELFEL_CUDA(c, cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    return ELFEL_OK;
+  }
+  copy_host_f64_k<<<grid_for(n, 256 * 4, (int64_t)c->sm_count * 2), 256, 0, st>>>(src, n, dst);
+  ELFEL_LAUNCH_CHECK(c);
+  return ELFEL_OK;
 }
 
 int to_index32(Ctx* c, const int64_t* src_host, int64_t n, int64_t limit, DBuf<int32_t>* dst, const char* what) {

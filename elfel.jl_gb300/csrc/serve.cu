@@ -287,6 +287,7 @@ int assemble_batch(elfel_server* s, const std::vector<Sys*>& ys) {
     }
   }
   // K values and rhs of all systems in one launch
+  for (Sys* y : ys) ELFEL_TRY(ensure_fpat(y->m));
   std::vector<RedJob> rj;
   int64_t blk = 0;
   for (Sys* y : ys) {

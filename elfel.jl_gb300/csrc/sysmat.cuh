@@ -25,6 +25,21 @@ struct SlotBlock {
 
 constexpr int kMaxBlocks = 4;
 
+// Division of n < 2^31 by an invariant d >= 1 as a multiply-high, an add and
+// a shift (Granlund and Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994): s = ceil(log2 d), m = floor(2^32 (2^s - d) / d) + 1,
+// n / d = (umulhi(n, m) + n) >> s (the sum stays below 2^32 for n < 2^31).
+struct FastDiv {
+  uint32_t m = 1;
+  int s = 0;
+  void init(uint32_t d) {
+    s = 0;
+    while ((1ull << s) < d) ++s;
+    m = (uint32_t)((((uint64_t)1 << 32) * (((uint64_t)1 << s) - d)) / d + 1);
+  }
+  __device__ __forceinline__ uint32_t div(uint32_t n) const { return (__umulhi(n, m) + n) >> s; }
+};
+
 struct SlotGen {
   int64_t nel = 0;
   int slots_per_elem = 0;   // S
@@ -36,6 +51,16 @@ struct SlotGen {
   const int32_t* J = nullptr;
   int64_t ncoo = 0;
   int64_t total() const { return nblocks ? nel * (int64_t)slots_per_elem : ncoo; }
+  // divisions of slot_rc (prepare() sets them; build_pattern does)
+  FastDiv spe_div, nr_div[kMaxBlocks], nc_div[kMaxBlocks];
+  void prepare() {
+    if (!nblocks) return;
+    spe_div.init((uint32_t)slots_per_elem);
+    for (int k = 0; k < nblocks; ++k) {
+      nr_div[k].init((uint32_t)(b[k].nr > 0 ? b[k].nr : 1));
+      nc_div[k].init((uint32_t)(b[k].nc > 0 ? b[k].nc : 1));
+    }
+  }
 };
 
 // Column-major index within a symmetric nr x nr block stored as its upper
@@ -45,6 +70,47 @@ __host__ __device__ __forceinline__ int sym_index(int i, int j) {
   return j * (j + 1) / 2 + i;
 }
 
+// Block mode: the slots of one element come in runs that share a column --
+// the nr slots of a local column of a plain block, the nc slots of a parent
+// row of a transposed one ("column groups", groups_per_elem() per element).
+__host__ __device__ __forceinline__ int groups_per_elem(const SlotGen& g) {
+  int n = 0;
+  for (int k = 0; k < g.nblocks; ++k) n += g.b[k].transposed ? g.b[k].nr : g.b[k].nc;
+  return n;
+}
+
+// Column group q: its column, first slot, length, and the element's row table
+// (rows of the group's slots: rtab[k], k < len; nullptr: all rows 0).
+__device__ __forceinline__ void group_info(const SlotGen& g, int G, int64_t q, int32_t& col, int64_t& s0, int& len,
+                                           const int32_t*& rtab) {
+  const int64_t e = q / G;
+  int lg = (int)(q - e * G);
+  int bi = 0;
+#pragma unroll
+  for (int k = 0; k < kMaxBlocks; ++k) {
+    if (k >= g.nblocks) break;
+    const int ng = g.b[k].transposed ? g.b[k].nr : g.b[k].nc;
+    if (lg < ng) {
+      bi = k;
+      break;
+    }
+    lg -= ng;
+  }
+  const SlotBlock& B = g.b[bi];
+  const int64_t base = e * (int64_t)g.slots_per_elem + B.slot_off;
+  if (!B.transposed) {  // local column lg: slots lg*nr + i, rows R[e][i]
+    col = B.C[e * B.nc + lg];
+    s0 = base + (int64_t)lg * B.nr;
+    len = B.nr;
+    rtab = B.R ? B.R + e * B.nr : nullptr;
+  } else {  // parent row lg: slots lg*nc + j, column R[e][lg], rows C[e][j]
+    col = B.R ? B.R[e * B.nr + lg] : 0;
+    s0 = base + (int64_t)lg * B.nc;
+    len = B.nc;
+    rtab = B.C + e * B.nc;
+  }
+}
+
 __device__ __forceinline__ void slot_rc(const SlotGen& g, int64_t s, int32_t& r, int32_t& c, int64_t& store) {
   if (g.nblocks == 0) {
     r = g.I[s];
@@ -52,10 +118,12 @@ __device__ __forceinline__ void slot_rc(const SlotGen& g, int64_t s, int32_t& r,
     store = s;
     return;
   }
-  // slot numbers stay below 2^31 (build_pattern checks), so 32-bit division
+  // slot numbers stay below 2^31 (build_pattern checks): multiply-shift
+  // divisions prepared on the host
   const uint32_t su = (uint32_t)s, spe = (uint32_t)g.slots_per_elem;
-  const int64_t e = (int64_t)(su / spe);
-  const int l = (int)(su - (uint32_t)e * spe);
+  const uint32_t eu = g.spe_div.div(su);
+  const int64_t e = (int64_t)eu;
+  const int l = (int)(su - eu * spe);
   int bi = 0;
 #pragma unroll
   for (int k = 1; k < kMaxBlocks; ++k)
@@ -64,13 +132,13 @@ __device__ __forceinline__ void slot_rc(const SlotGen& g, int64_t s, int32_t& r,
   const int t = l - B.slot_off;
   int i, j;  // parent (row, col) index within the local matrix
   if (!B.transposed) {
-    i = t % B.nr;
-    j = t / B.nr;
+    j = (int)g.nr_div[bi].div((uint32_t)t);
+    i = t - j * B.nr;
     r = B.R ? B.R[e * B.nr + i] : 0;
     c = B.C[e * B.nc + j];
   } else {
-    i = t / B.nc;  // parent row
-    j = t % B.nc;  // parent col
+    i = (int)g.nc_div[bi].div((uint32_t)t);  // parent row
+    j = t - i * B.nc;                         // parent col
     r = B.C[e * B.nc + j];
     c = B.R ? B.R[e * B.nr + i] : 0;
   }
@@ -124,6 +192,13 @@ int reduce_batch(Ctx* c, const RedJob* jobs_dev, int njobs, int64_t blocks);
 // Convert 1-based int64 indices to 0-based int32 with a range check.
 int to_index32(Ctx* c, const int64_t* src_host, int64_t n, int64_t limit, DBuf<int32_t>* dst,
                const char* what);
+// The same on stream st from a device-readable host array (host_device_ptr)
+// into dst (n entries); entries outside 1..limit become 0 and set *bad
+// (device), which the caller reads after the stream's work.
+int to_index32_direct(Ctx* c, cudaStream_t st, const int64_t* src, int64_t n, int64_t limit, int32_t* dst, int* bad);
+// n doubles from a device-readable host array to dst on stream st (copy
+// engine for pinned memory, a copy kernel for pageable memory).
+int copy_host_f64(Ctx* c, cudaStream_t st, const double* src, int pinned, int64_t n, double* dst);
 
 // Fused-mode device data.
 struct Fused {
@@ -152,9 +227,11 @@ struct Fused {
   DBuf<uint8_t> straight;            // nel: 1 = straight-sided element (of the current coordinates)
   int64_t ncurved = -1;              // elements without the flag (-1: not computed)
   int f_direct_ok = 0;               // T6 heat: no DOF is a midside node of more than two elements
+  int fpat_built = 0;                // fpat is built on first use (ensure_fpat)
   void release(Ctx* c) {
     is_block = 0;
     f_direct_ok = 0;
+    fpat_built = 0;
     shape = ELFEL_SHAPE_TRIANGLE;
     sdim = 2;
     ncurved = -1;
@@ -190,6 +267,9 @@ namespace elfel {
 // Slot generators, patterns and value buffers of a fused system whose tables
 // (F.conn_u, F.xy_u, F.dofs_u; F.physics, nn, ncomp, nel, tab set) are on the device.
 int fused_build(elfel_sysmat* m, int64_t ndofs);
+// Builds the right-hand side's pattern (F.fgen) if it is not built yet; only
+// assemblies that reduce load records need it.
+int ensure_fpat(elfel_sysmat* m);
 
 // Device tables of a block mesh of the rectangle [0,lx] x [0,ly]: nodes,
 // connectivity and the DOFs of a scalar field fixed on the whole boundary

@@ -305,3 +305,41 @@ def test_t6_pair_and_fp64_paths(E, O, gpu, case):
     scale = np.repeat(rowmax, np.diff(K0.indptr))
     assert (np.abs(K.data - K0.data) <= 1e-11 * scale).all()
     assert np.abs(F - F0).max() <= 1e-11 * np.abs(F0).max()
+
+
+def test_fused_setup_rejects_bad_tables(E, gpu):
+    """Connectivity and element DOFs are read straight from host memory and
+    checked on the device; an entry outside its range fails fused_setup with
+    the table's name, and the system can be set up again afterwards."""
+    import ctypes
+
+    mesh = E.T6block(1.0, 1.0, 4, 4)
+    fesp = heat_space(E, mesh, E.FEH1_T6())
+    n = E.ndofs(fesp)
+    qpit = E.QPIterator(fesp, {"npts": 3})
+    N_ = E._native
+    pc, w = N_.f64(qpit.quadr.param_coords), N_.f64(qpit.quadr.weights)
+    xy = np.ascontiguousarray(mesh.xy)
+    am = E.start(E.SysmatAssemblerGPU(), n, n)
+
+    def setup(conn, dofs):
+        sp = N_.Space(6, 1, mesh.nel, mesh.nnodes, N_.ptr(conn, N_._i64p), N_.ptr(xy), N_.ptr(dofs, N_._i64p))
+        d = N_.FusedDesc(N_.ELFEL_HEAT, 3, N_.ptr(pc), N_.ptr(w), n, sp, N_.Space())
+        am._hd.check(am._hd.lib.elfel_fused_setup(am._hd.h, ctypes.byref(d)))
+
+    conn = np.ascontiguousarray(mesh.conn)
+    dofs = np.ascontiguousarray(E.FEIterator(fesp).eldofs_table())
+    bad_conn = conn.copy()
+    bad_conn[5, 2] = mesh.nnodes + 1
+    with pytest.raises(E.ElfelError, match="primary connectivity"):
+        setup(bad_conn, dofs)
+    bad_dofs = dofs.copy()
+    bad_dofs[7, 1] = 0
+    with pytest.raises(E.ElfelError, match="primary eldofs"):
+        setup(conn, bad_dofs)
+    E.assemble_heat(am, E.FEIterator(fesp), E.QPIterator(fesp, {"npts": 3}), 1.0, -6.0)
+    K, F = E.finish(am), am.rhs()
+    am2 = E.start(E.SysmatAssemblerGPU(), n, n)
+    E.assemble_heat(am2, E.FEIterator(fesp), E.QPIterator(fesp, {"npts": 3}), 1.0, -6.0)
+    K2, F2 = E.finish(am2), am2.rhs()
+    assert same_pattern(K, K2) and (K.data == K2.data).all() and (F == F2).all()
