@@ -53,13 +53,33 @@ __global__ void count_cols_k(SlotGen g, int64_t n, int32_t* colcnt, int64_t ncol
   }
 }
 
+// Consecutive slots mostly share their column (a local column of an element
+// matrix, a run of COO triplets): the lanes of a warp with equal columns in a
+// row form a run whose first lane reserves the run's positions with one
+// atomic and hands them out by shuffle.
 __global__ void bucket_k(SlotGen g, int64_t n, const int64_t* colstart, int32_t* cursor, uint64_t* keys) {
-  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
-    int32_t r, c;
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t s0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); s0 < n; s0 += stride) {
+    const int64_t s = s0 + lane;
+    const bool valid = s < n;
+    int32_t r = 0, c = -1;
     int64_t st;
-    slot_rc(g, s, r, c, st);
-    int32_t pos = atomicAdd(&cursor[c], 1);
-    keys[colstart[c] + pos] = ((uint64_t)(uint32_t)r << 32) | (uint64_t)(uint32_t)s;
+    if (valid) slot_rc(g, s, r, c, st);
+    const int32_t cprev = __shfl_up_sync(0xffffffffu, c, 1);
+    const bool head = valid && (lane == 0 || c != cprev);
+    const unsigned heads = __ballot_sync(0xffffffffu, head);
+    const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+    const unsigned upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
+    const int start = 31 - __clz(heads & upto);  // first lane of this lane's run
+    int32_t base = 0;
+    if (head) {
+      const unsigned after = heads & ~upto;  // heads of later runs
+      const int end = after ? __ffs(after) - 1 : 32 - __clz(vmask);
+      base = atomicAdd(&cursor[c], end - lane);
+    }
+    base = __shfl_sync(0xffffffffu, base, valid ? start : 0);
+    if (valid) keys[colstart[c] + base + (lane - start)] = ((uint64_t)(uint32_t)r << 32) | (uint64_t)(uint32_t)s;
   }
 }
 
@@ -122,35 +142,56 @@ __device__ __forceinline__ uint64_t reg_sort(uint64_t v, int lane) {
   return v;
 }
 
-// Register-resident bitonic sort of 64 keys held two per lane (index lane in
-// v0, lane + 32 in v1), ascending; shuffles exchange keys between lanes, the
-// j = 32 stages compare a lane's own pair.  Unused positions hold ~0.
-__device__ __forceinline__ void reg_sort64(uint64_t& v0, uint64_t& v1, int lane) {
+// Number of keys of a sequence sorted ascending across the warp's lanes
+// (one per lane, padding ~0) that are below x (keys are distinct): a binary
+// search whose probes are per-lane shuffles.
+__device__ __forceinline__ int count_below(uint64_t seq, uint64_t x) {
+  int pos = 0;
 #pragma unroll
-  for (int k = 2; k <= 64; k <<= 1) {
-#pragma unroll
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      if (j == 32) {  // partner of index i is i + 32: the same lane's other key
-        const bool up = ((lane & k) == 0);
-        const uint64_t lo = v0 < v1 ? v0 : v1, hi = v0 < v1 ? v1 : v0;
-        v0 = up ? lo : hi;
-        v1 = up ? hi : lo;
-      } else {
-        const uint64_t o0 = __shfl_xor_sync(0xffffffffu, v0, j);
-        const uint64_t o1 = __shfl_xor_sync(0xffffffffu, v1, j);
-        const bool lower = (lane & j) == 0;
-        const bool up0 = ((lane & k) == 0), up1 = (((lane + 32) & k) == 0);
-        v0 = (lower == up0) ? (v0 < o0 ? v0 : o0) : (v0 < o0 ? o0 : v0);
-        v1 = (lower == up1) ? (v1 < o1 ? v1 : o1) : (v1 < o1 ? o1 : v1);
-      }
-    }
-  }
+  for (int step = 16; step > 0; step >>= 1)
+    if (__shfl_sync(0xffffffffu, seq, pos + step - 1) < x) pos += step;
+  if (__shfl_sync(0xffffffffu, seq, pos) < x) ++pos;
+  return pos;
+}
+
+// Sort 32 < n <= 64 keys (keys[b + lane], keys[b + 32 + lane]) by merging:
+// the first 32 and the other n - 32 are sorted in registers separately, each
+// key's place is its index plus the number of keys of the other sequence
+// below it; the keys are placed in sh, then written back in order with the
+// distinct-row count.
+__device__ __forceinline__ void sort_column_merge(int64_t b, int n, uint64_t* keys, int32_t* cnt_out, uint64_t* sh,
+                                                  int lane) {
+  uint64_t v0 = keys[b + lane];
+  uint64_t v1 = lane + 32 < n ? keys[b + lane + 32] : ~0ull;
+  v0 = reg_sort<32>(v0, lane);
+  const int m = n - 32;
+  if (m > 16) v1 = reg_sort<32>(v1, lane);
+  else if (m > 8) v1 = reg_sort<16>(v1, lane);
+  else if (m > 4) v1 = reg_sort<8>(v1, lane);
+  else if (m > 1) v1 = reg_sort<4>(v1, lane);
+  const int r0 = lane + count_below(v1, v0);
+  const int r1 = lane + count_below(v0, v1);
+  sh[r0] = v0;
+  if (lane < m) sh[r1] = v1;
+  __syncwarp();
+  const uint64_t s0 = sh[lane], s1 = lane + 32 < n ? sh[lane + 32] : ~0ull;
+  const uint64_t p0 = __shfl_up_sync(0xffffffffu, s0, 1);
+  const uint64_t last0 = __shfl_sync(0xffffffffu, s0, 31);
+  uint64_t p1 = __shfl_up_sync(0xffffffffu, s1, 1);
+  if (lane == 0) p1 = last0;
+  const bool f0 = lane == 0 || (s0 >> 32) != (p0 >> 32);
+  const bool f1 = lane + 32 < n && (s1 >> 32) != (p1 >> 32);
+  const int cnt = __popc(__ballot_sync(0xffffffffu, f0)) + __popc(__ballot_sync(0xffffffffu, f1));
+  keys[b + lane] = s0;
+  if (lane + 32 < n) keys[b + lane + 32] = s1;
+  if (lane == 0) *cnt_out = cnt;
+  __syncwarp();  // sh is reused by the warp's next column
 }
 
 // Sort one column's keys by (row, slot) and count its distinct rows (one
-// warp).  Columns of up to 64 keys are sorted in registers (one key per lane
-// up to 32, two up to 64); longer ones with the bitonic network in shared
-// memory (up to kSortCap keys, in sh) or in place in global memory.
+// warp).  Columns of up to 32 keys are sorted in registers, up to 64 by
+// sort_column_merge; longer ones with the bitonic network in shared memory
+// (up to kSortCap keys, in sh) or in place in global memory.
 __device__ void sort_column(int64_t b, int n, uint64_t* keys, int32_t* cnt_out, uint64_t* sh, int lane) {
   if (n <= 32) {
     uint64_t v = lane < n ? keys[b + lane] : ~0ull;
@@ -167,19 +208,7 @@ __device__ void sort_column(int64_t b, int n, uint64_t* keys, int32_t* cnt_out, 
     return;
   }
   if (n <= 64) {
-    uint64_t v0 = keys[b + lane];
-    uint64_t v1 = lane + 32 < n ? keys[b + lane + 32] : ~0ull;
-    reg_sort64(v0, v1, lane);
-    const uint64_t p0 = __shfl_up_sync(0xffffffffu, v0, 1);
-    const uint64_t last0 = __shfl_sync(0xffffffffu, v0, 31);
-    uint64_t p1 = __shfl_up_sync(0xffffffffu, v1, 1);
-    if (lane == 0) p1 = last0;
-    const bool f0 = lane == 0 || (v0 >> 32) != (p0 >> 32);
-    const bool f1 = lane + 32 < n && (v1 >> 32) != (p1 >> 32);
-    const int cnt = __popc(__ballot_sync(0xffffffffu, f0)) + __popc(__ballot_sync(0xffffffffu, f1));
-    keys[b + lane] = v0;
-    if (lane + 32 < n) keys[b + lane + 32] = v1;
-    if (lane == 0) *cnt_out = cnt;
+    sort_column_merge(b, n, keys, cnt_out, sh, lane);
     return;
   }
   uint64_t* a;
