@@ -13,8 +13,9 @@
 //   3. bucket each slot's key (row << 32 | slot) into its column
 //   4. sort each column's keys (one warp per column, bitonic network)
 //   5. count distinct rows per column, scan -> colptr
-//   6. emit rowval, the first contribution of each nonzero (cptr) and the
-//      storage index of every contribution (contrib), in sorted order.
+//   6. the storage index of every contribution (contrib), in sorted order,
+//      written by the sort; rowval and the first contribution of each
+//      nonzero (cptr) compacted from the sort's row starts.
 #include "sysmat.cuh"
 
 namespace elfel {
@@ -154,13 +155,28 @@ __device__ __forceinline__ int count_below(uint64_t seq, uint64_t x) {
   return pos;
 }
 
+// Output of a sorted column: each key's storage index goes to contrib[b + t]
+// (t = its place in the column), and each key that starts a row (its
+// predecessor has another row) to nzkey[b + i] as (row << 32 | b + t), i =
+// the number of rows before it in the column.  compact_k moves the latter to
+// rowval / cptr once the column's first nonzero is known.
+struct ColOut {
+  int32_t* contrib;
+  uint64_t* nzkey;
+};
+
+__device__ __forceinline__ void put_key(const SlotGen& g, const ColOut& o, int64_t b, uint64_t key, int t, bool first,
+                                        int li) {
+  o.contrib[b + t] = (int32_t)slot_store(g, (int64_t)(key & 0xffffffffull));
+  if (first) o.nzkey[b + li] = (key & 0xffffffff00000000ull) | (uint64_t)(uint32_t)(b + t);
+}
+
 // Sort 32 < n <= 64 keys (keys[b + lane], keys[b + 32 + lane]) by merging:
 // the first 32 and the other n - 32 are sorted in registers separately, each
 // key's place is its index plus the number of keys of the other sequence
-// below it; the keys are placed in sh, then written back in order with the
-// distinct-row count.
-__device__ __forceinline__ void sort_column_merge(int64_t b, int n, uint64_t* keys, int32_t* cnt_out, uint64_t* sh,
-                                                  int lane) {
+// below it; the keys are placed in sh and read back in order.
+__device__ __forceinline__ void sort_column_merge(const SlotGen& g, const ColOut& o, int64_t b, int n,
+                                                  const uint64_t* keys, int32_t* cnt_out, uint64_t* sh, int lane) {
   uint64_t v0 = keys[b + lane];
   uint64_t v1 = lane + 32 < n ? keys[b + lane + 32] : ~0ull;
   v0 = reg_sort<32>(v0, lane);
@@ -181,18 +197,22 @@ __device__ __forceinline__ void sort_column_merge(int64_t b, int n, uint64_t* ke
   if (lane == 0) p1 = last0;
   const bool f0 = lane == 0 || (s0 >> 32) != (p0 >> 32);
   const bool f1 = lane + 32 < n && (s1 >> 32) != (p1 >> 32);
-  const int cnt = __popc(__ballot_sync(0xffffffffu, f0)) + __popc(__ballot_sync(0xffffffffu, f1));
-  keys[b + lane] = s0;
-  if (lane + 32 < n) keys[b + lane + 32] = s1;
-  if (lane == 0) *cnt_out = cnt;
+  const unsigned m0 = __ballot_sync(0xffffffffu, f0), m1 = __ballot_sync(0xffffffffu, f1);
+  const unsigned below = (1u << lane) - 1u;
+  put_key(g, o, b, s0, lane, f0, __popc(m0 & below));
+  if (lane + 32 < n) put_key(g, o, b, s1, lane + 32, f1, __popc(m0) + __popc(m1 & below));
+  if (lane == 0) *cnt_out = __popc(m0) + __popc(m1);
   __syncwarp();  // sh is reused by the warp's next column
 }
 
-// Sort one column's keys by (row, slot) and count its distinct rows (one
-// warp).  Columns of up to 32 keys are sorted in registers, up to 64 by
-// sort_column_merge; longer ones with the bitonic network in shared memory
-// (up to kSortCap keys, in sh) or in place in global memory.
-__device__ void sort_column(int64_t b, int n, uint64_t* keys, int32_t* cnt_out, uint64_t* sh, int lane) {
+// Sort one column's keys by (row, slot), write its output (ColOut) and its
+// number of distinct rows (one warp).  Columns of up to 32 keys are sorted in
+// registers, up to 64 by sort_column_merge; longer ones with the bitonic
+// network in shared memory (up to kSortCap keys, in sh) or in place in global
+// memory.
+__device__ void sort_column(const SlotGen& g, const ColOut& o, int64_t b, int n, uint64_t* keys, int32_t* cnt_out,
+                            uint64_t* sh, int lane) {
+  const unsigned below = (1u << lane) - 1u;
   if (n <= 32) {
     uint64_t v = lane < n ? keys[b + lane] : ~0ull;
     if (n > 16) v = reg_sort<32>(v, lane);
@@ -202,13 +222,13 @@ __device__ void sort_column(int64_t b, int n, uint64_t* keys, int32_t* cnt_out, 
     // distinct rows: a key starts a row when its predecessor has another row
     const uint64_t pv = __shfl_up_sync(0xffffffffu, v, 1);
     const bool first = lane < n && (lane == 0 || (v >> 32) != (pv >> 32));
-    const int cnt = __popc(__ballot_sync(0xffffffffu, first));
-    if (lane < n) keys[b + lane] = v;
-    if (lane == 0) *cnt_out = cnt;
+    const unsigned m = __ballot_sync(0xffffffffu, first);
+    if (lane < n) put_key(g, o, b, v, lane, first, __popc(m & below));
+    if (lane == 0) *cnt_out = __popc(m);
     return;
   }
   if (n <= 64) {
-    sort_column_merge(b, n, keys, cnt_out, sh, lane);
+    sort_column_merge(g, o, b, n, keys, cnt_out, sh, lane);
     return;
   }
   uint64_t* a;
@@ -224,26 +244,32 @@ __device__ void sort_column(int64_t b, int n, uint64_t* keys, int32_t* cnt_out, 
   for (int t0 = 0; t0 < n; t0 += 32) {
     const int t = t0 + lane;
     bool first = false;
-    if (t < n) first = (t == 0) || ((a[t] >> 32) != (a[t - 1] >> 32));
-    cnt += __popc(__ballot_sync(0xffffffffu, first));
+    uint64_t key = 0;
+    if (t < n) {
+      key = a[t];
+      first = (t == 0) || ((key >> 32) != (a[t - 1] >> 32));
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, first);
+    if (t < n) put_key(g, o, b, key, t, first, cnt + __popc(m & below));
+    cnt += __popc(m);
   }
-  if (n <= kSortCap)
-    for (int t = lane; t < n; t += 32) keys[b + t] = a[t];
   if (lane == 0) *cnt_out = cnt;
   __syncwarp();
 }
 
 // A warp takes four consecutive columns.  When each has at most 8 keys (the
 // rhs pattern, where a column holds a node's element contributions), the
-// four are sorted at once, one per group of 8 lanes; otherwise one after the
-// other by the whole warp.
+// four are sorted at once, one per group of 8 lanes; when each has at most
+// 16 (T6 midside columns), two at a time; otherwise one after the other by
+// the whole warp.
 constexpr int kColsPerWarp = 4;
 
-__global__ void __launch_bounds__(kSortThreads) sort_cols_k(const int64_t* colstart, int64_t ncol, uint64_t* keys,
-                                                           int32_t* nnzcnt) {
+__global__ void __launch_bounds__(kSortThreads) sort_cols_k(SlotGen g, ColOut o, const int64_t* colstart,
+                                                           int64_t ncol, uint64_t* keys, int32_t* nnzcnt) {
   __shared__ uint64_t sh[kSortThreads / 32][kSortCap];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int grp = lane >> 3, gl = lane & 7;
+  const unsigned below = (1u << lane) - 1u;
   const int64_t warps = (int64_t)gridDim.x * (kSortThreads / 32);
   for (int64_t c0 = ((int64_t)blockIdx.x * (kSortThreads / 32) + wid) * kColsPerWarp; c0 < ncol;
        c0 += warps * kColsPerWarp) {
@@ -259,14 +285,16 @@ __global__ void __launch_bounds__(kSortThreads) sort_cols_k(const int64_t* colst
       v = reg_sort<8>(v, gl);  // partners lane ^ j (j < 8) stay inside the group
       const uint64_t pv = __shfl_up_sync(0xffffffffu, v, 1, 8);
       const bool first = gl < ng && (gl == 0 || (v >> 32) != (pv >> 32));
-      const unsigned m = __ballot_sync(0xffffffffu, first);
-      if (gl < ng) keys[bg + gl] = v;
-      if (gl == 0 && cg < ncol) nnzcnt[cg] = __popc(m & (0xffu << (grp * 8)));
+      const unsigned group = 0xffu << (grp * 8);
+      const unsigned m = __ballot_sync(0xffffffffu, first) & group;
+      if (gl < ng) put_key(g, o, bg, v, gl, first, __popc(m & below));
+      if (gl == 0 && cg < ncol) nnzcnt[cg] = __popc(m);
       continue;
     }
     if (__all_sync(0xffffffffu, ng <= 16)) {
       // two columns at a time, one per half warp (T6 midside columns: 12 keys)
       const int h = lane >> 4, hl = lane & 15;
+      const unsigned half = 0xffffu << (h * 16);
 #pragma unroll
       for (int r = 0; r < kColsPerWarp / 2; ++r) {
         const int q = 2 * r + h;
@@ -276,9 +304,9 @@ __global__ void __launch_bounds__(kSortThreads) sort_cols_k(const int64_t* colst
         v = reg_sort<16>(v, hl);  // partners lane ^ j (j < 16) stay inside the half
         const uint64_t pv = __shfl_up_sync(0xffffffffu, v, 1, 16);
         const bool first = hl < n && (hl == 0 || (v >> 32) != (pv >> 32));
-        const unsigned m = __ballot_sync(0xffffffffu, first);
-        if (hl < n) keys[b + hl] = v;
-        if (hl == 0 && c0 + q < ncol) nnzcnt[c0 + q] = __popc(m & (0xffffu << (h * 16)));
+        const unsigned m = __ballot_sync(0xffffffffu, first) & half;
+        if (hl < n) put_key(g, o, b, v, hl, first, __popc(m & below));
+        if (hl == 0 && c0 + q < ncol) nnzcnt[c0 + q] = __popc(m);
       }
       continue;
     }
@@ -286,103 +314,24 @@ __global__ void __launch_bounds__(kSortThreads) sort_cols_k(const int64_t* colst
       const int64_t col = c0 + q;
       if (col >= ncol) break;
       const int64_t b = colstart[col];
-      sort_column(b, (int)(colstart[col + 1] - b), keys, nnzcnt + col, sh[wid], lane);
+      sort_column(g, o, b, (int)(colstart[col + 1] - b), keys, nnzcnt + col, sh[wid], lane);
     }
   }
 }
 
-// Emit one column's nonzeros (rows, first contributions) and the storage
-// index of each contribution (one warp).
-__device__ void emit_column(const SlotGen& g, int64_t b, int64_t n, int64_t k, const uint64_t* keys,
-                            int32_t* rowval, int32_t* cptr, int32_t* contrib, int lane) {
-  for (int64_t t0 = 0; t0 < n; t0 += 32) {
-    int64_t t = t0 + lane;
-    bool first = false;
-    uint64_t key = 0;
-    if (t < n) {
-      key = keys[b + t];
-      first = (t == 0) || ((key >> 32) != (keys[b + t - 1] >> 32));
-      int32_t r, c;
-      int64_t st;
-      slot_rc(g, (int64_t)(key & 0xffffffffull), r, c, st);
-      contrib[b + t] = (int32_t)st;
-    }
-    unsigned m = __ballot_sync(0xffffffffu, first);
-    if (first) {
-      int64_t kk = k + __popc(m & ((1u << lane) - 1u));
-      rowval[kk] = (int32_t)(key >> 32);
-      cptr[kk] = (int32_t)(b + t);
-    }
-    k += __popc(m);
-  }
-}
-
-__global__ void emit_k(SlotGen g, const int64_t* colstart, const int64_t* colptr, int64_t ncol, const uint64_t* keys,
-                       int32_t* rowval, int32_t* cptr, int32_t* contrib) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int grp = lane >> 3, gl = lane & 7;
-  const unsigned below = (1u << lane) - 1u, group = 0xffu << (grp * 8);
-  const int64_t warps = (int64_t)gridDim.x * (blockDim.x / 32);
-  for (int64_t c0 = ((int64_t)blockIdx.x * (blockDim.x / 32) + wid) * kColsPerWarp; c0 < ncol;
-       c0 += warps * kColsPerWarp) {
-    const int64_t cg = c0 + grp;
-    int64_t bg = 0;
-    int ng = 0;
-    if (cg < ncol) {
-      bg = colstart[cg];
-      ng = (int)(colstart[cg + 1] - bg);
-    }
-    if (__all_sync(0xffffffffu, ng <= 8)) {
-      bool first = false;
-      uint64_t key = 0;
-      if (gl < ng) {
-        key = keys[bg + gl];
-        first = (gl == 0) || ((key >> 32) != (keys[bg + gl - 1] >> 32));
-        int32_t r, c;
-        int64_t st;
-        slot_rc(g, (int64_t)(key & 0xffffffffull), r, c, st);
-        contrib[bg + gl] = (int32_t)st;
-      }
-      const unsigned m = __ballot_sync(0xffffffffu, first);
-      if (first) {
-        const int64_t kk = colptr[cg] + __popc(m & group & below);
-        rowval[kk] = (int32_t)(key >> 32);
-        cptr[kk] = (int32_t)(bg + gl);
-      }
-      continue;
-    }
-    if (__all_sync(0xffffffffu, ng <= 16)) {
-      // two columns at a time, one per half warp
-      const int h = lane >> 4, hl = lane & 15;
-      const unsigned half = 0xffffu << (h * 16);
-#pragma unroll
-      for (int r = 0; r < kColsPerWarp / 2; ++r) {
-        const int q = 2 * r + h;
-        const int64_t b = __shfl_sync(0xffffffffu, bg, q * 8);
-        const int n = __shfl_sync(0xffffffffu, ng, q * 8);
-        const uint64_t key = hl < n ? keys[b + hl] : 0ull;
-        const uint64_t pkey = __shfl_up_sync(0xffffffffu, key, 1, 16);
-        const bool first = hl < n && (hl == 0 || (key >> 32) != (pkey >> 32));
-        if (hl < n) {
-          int32_t rr, cc;
-          int64_t st;
-          slot_rc(g, (int64_t)(key & 0xffffffffull), rr, cc, st);
-          contrib[b + hl] = (int32_t)st;
-        }
-        const unsigned m = __ballot_sync(0xffffffffu, first);
-        if (first) {
-          const int64_t kk = colptr[c0 + q] + __popc(m & half & below);
-          rowval[kk] = (int32_t)(key >> 32);
-          cptr[kk] = (int32_t)(b + hl);
-        }
-      }
-      continue;
-    }
-    for (int q = 0; q < kColsPerWarp; ++q) {
-      const int64_t col = c0 + q;
-      if (col >= ncol) break;
-      const int64_t b = colstart[col];
-      emit_column(g, b, colstart[col + 1] - b, colptr[col], keys, rowval, cptr, contrib, lane);
+// rowval / cptr of every column from its row starts (ColOut.nzkey): one half
+// warp per column.
+__global__ void compact_k(const int64_t* __restrict__ colstart, const int64_t* __restrict__ colptr, int64_t ncol,
+                          const uint64_t* __restrict__ nzkey, int32_t* __restrict__ rowval,
+                          int32_t* __restrict__ cptr) {
+  const int hl = threadIdx.x & 15;
+  const int64_t halves = (int64_t)gridDim.x * (blockDim.x / 16);
+  for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 4; c < ncol; c += halves) {
+    const int64_t k0 = colptr[c], cnt = colptr[c + 1] - k0, b = colstart[c];
+    for (int64_t i = hl; i < cnt; i += 16) {
+      const uint64_t v = nzkey[b + i];
+      rowval[k0 + i] = (int32_t)(v >> 32);
+      cptr[k0 + i] = (int32_t)(uint32_t)v;
     }
   }
 }
@@ -484,8 +433,12 @@ int build_pattern(Ctx* c, const SlotGen& g0, int64_t nrow, int64_t ncol, Pattern
   // sort + distinct counts (reuse colcnt as per-column nonzero counts)
   const unsigned gsort = grid_for((ncol + kColsPerWarp - 1) / kColsPerWarp, kSortThreads / 32,
                                   (int64_t)c->sm_count * 32);
+  DBuf<uint64_t> nzkey;  // row starts of each column (ColOut), compacted after the scan
+  ELFEL_TRY(nzkey.alloc(c, (size_t)(M > 0 ? M : 1)));
+  ELFEL_TRY(P->contrib.alloc(c, (size_t)(M > 0 ? M : 1)));
   if (ncol > 0) {
-    sort_cols_k<<<gsort, kSortThreads, 0, st>>>(colstart.p, ncol, keys.p, colcnt.p);
+    sort_cols_k<<<gsort, kSortThreads, 0, st>>>(g, ColOut{P->contrib.p, nzkey.p}, colstart.p, ncol, keys.p,
+                                               colcnt.p);
     ELFEL_LAUNCH_CHECK(c);
   }
   ELFEL_TRY(P->colptr.alloc(c, (size_t)ncol + 1));
@@ -496,12 +449,12 @@ int build_pattern(Ctx* c, const SlotGen& g0, int64_t nrow, int64_t ncol, Pattern
   P->nnz = nnz;
   ELFEL_TRY(P->rowval.alloc(c, (size_t)(nnz > 0 ? nnz : 1)));
   ELFEL_TRY(P->cptr.alloc(c, (size_t)nnz + 1));
-  ELFEL_TRY(P->contrib.alloc(c, (size_t)(M > 0 ? M : 1)));
   if (ncol > 0) {
-    emit_k<<<gsort, kSortThreads, 0, st>>>(g, colstart.p, P->colptr.p, ncol, keys.p, P->rowval.p, P->cptr.p,
-                                           P->contrib.p);
+    compact_k<<<grid_for(ncol, 16, (int64_t)c->sm_count * 32), 256, 0, st>>>(colstart.p, P->colptr.p, ncol,
+                                                                            nzkey.p, P->rowval.p, P->cptr.p);
     ELFEL_LAUNCH_CHECK(c);
   }
+  nzkey.release(c);
   set_last_k<<<1, 1, 0, st>>>(P->cptr.p, nnz, M);
   ELFEL_LAUNCH_CHECK(c);
   if (nnz > 0 && nrow > 1) {  // 1 x n patterns (vectors) are reduced without windows

@@ -70,6 +70,30 @@ __host__ __device__ __forceinline__ int sym_index(int i, int j) {
   return j * (j + 1) / 2 + i;
 }
 
+// The storage index of slot s alone (no table reads).
+__device__ __forceinline__ int64_t slot_store(const SlotGen& g, int64_t s) {
+  if (g.nblocks == 0) return s;
+  const uint32_t su = (uint32_t)s, spe = (uint32_t)g.slots_per_elem;
+  const uint32_t eu = g.spe_div.div(su);
+  const int l = (int)(su - eu * spe);
+  int bi = 0;
+#pragma unroll
+  for (int k = 1; k < kMaxBlocks; ++k)
+    if (k < g.nblocks && l >= g.b[k].slot_off) bi = k;
+  const SlotBlock& B = g.b[bi];
+  const int t = l - B.slot_off;
+  int i, j;
+  if (!B.transposed) {
+    j = (int)g.nr_div[bi].div((uint32_t)t);
+    i = t - j * B.nr;
+  } else {
+    i = (int)g.nc_div[bi].div((uint32_t)t);
+    j = t - i * B.nc;
+  }
+  const int loc = B.sym ? sym_index(i, j) : (i + j * B.nr);
+  return (int64_t)eu * g.store_per_elem + B.store_off + loc;
+}
+
 // Block mode: the slots of one element come in runs that share a column --
 // the nr slots of a local column of a plain block, the nc slots of a parent
 // row of a transposed one ("column groups", groups_per_elem() per element).
