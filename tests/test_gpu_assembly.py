@@ -343,3 +343,38 @@ def test_fused_setup_rejects_bad_tables(E, gpu):
     E.assemble_heat(am2, E.FEIterator(fesp), E.QPIterator(fesp, {"npts": 3}), 1.0, -6.0)
     K2, F2 = E.finish(am2), am2.rhs()
     assert same_pattern(K, K2) and (K.data == K2.data).all() and (F == F2).all()
+
+
+def test_fused_edge_cases(E, O, gpu):
+    """One T6 element (every midside DOF with a single contribution), and a
+    mesh without elements through the C ABI (empty pattern, zero vector)."""
+    import ctypes
+
+    m2 = E.T6block(1.0, 1.0, 1, 1)
+    mesh = E.Mesh("T6", m2.conn[:1], m2.xy)
+    fesp = heat_space(E, mesh, E.FEH1_T6())
+    n = E.ndofs(fesp)
+    am = E.start(E.SysmatAssemblerGPU(), n, n)
+    E.assemble_heat(am, E.FEIterator(fesp), E.QPIterator(fesp, {"npts": 3}), 1.5, -6.0)
+    K, F = E.finish(am), am.rhs()
+    K0, F0 = heat_oracle(E, O, mesh, fesp, 3, np.array([1.5]), -6.0)
+    assert same_pattern(K, K0) and close(K.data, K0.data) and close(F, F0)
+    assert K.nnz == 36  # one element: a dense 6 x 6 block (unused nodes have empty columns)
+
+    N_ = E._native
+    qpit = E.QPIterator(fesp, {"npts": 3})
+    pc, w = N_.f64(qpit.quadr.param_coords), N_.f64(qpit.quadr.weights)
+    conn = np.zeros((0, 6), dtype=np.int64)
+    dofs = np.zeros((0, 6), dtype=np.int64)
+    xy = np.ascontiguousarray(m2.xy)
+    nn = xy.shape[0]
+    sp = N_.Space(6, 1, 0, nn, N_.ptr(conn, N_._i64p), N_.ptr(xy), N_.ptr(dofs, N_._i64p))
+    d = N_.FusedDesc(N_.ELFEL_HEAT, 3, N_.ptr(pc), N_.ptr(w), nn, sp, N_.Space())
+    am0 = E.start(E.SysmatAssemblerGPU(), nn, nn)
+    lib, h = am0._hd.lib, am0._hd.h
+    am0._hd.check(lib.elfel_fused_setup(h, ctypes.byref(d)))
+    am0._hd.check(lib.elfel_fused_heat(h, None, -6.0))
+    K = am0._hd.csc()
+    F = np.ones(nn)
+    am0._hd.check(lib.elfel_sysmat_rhs(h, N_.ptr(F)))
+    assert K.shape == (nn, nn) and K.nnz == 0 and (F == 0.0).all()
