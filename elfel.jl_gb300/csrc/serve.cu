@@ -382,7 +382,6 @@ int finish_request(elfel_server* s, Sys* y, const elfel_solve_stats& sst, int st
 }
 
 int admit(elfel_server* s, std::vector<Sys*>* admitted) {
-  Ctx* c = &s->h->c;
   int active = (int)s->by_slot.size();
   while (!s->pending.empty() && active + (int)admitted->size() < s->cfg.max_active) {
     const Req q = s->pending.front();
@@ -421,7 +420,6 @@ int admit(elfel_server* s, std::vector<Sys*>* admitted) {
     y->t_admit = now_s(s);
     admitted->push_back(y);
   }
-  (void)c;
   return ELFEL_OK;
 }
 
