@@ -165,6 +165,32 @@ __device__ __forceinline__ void write_records_part(const double* acc, int rec, i
   }
 }
 
+// The same with compile-time widths: in a full CTA every thread writes NK
+// values, its (element, entry) pair advancing by (NT / NK, NT % NK) per value
+// (no division in the loop).
+template <int NT, int REC, int NK>
+__device__ __forceinline__ void write_records_fixed(const double* acc, int k0, int64_t e0, int64_t nel,
+                                                    double* out) {
+  if (e0 + NT > nel) {
+    write_records_part<NT>(acc, REC, k0, NK, e0, nel, out);
+    return;
+  }
+  __syncthreads();
+  constexpr int DT = NT / NK, DK = NT % NK;
+  double* dst = out + e0 * REC + k0;
+  int t = (int)threadIdx.x / NK, kk = (int)threadIdx.x - t * NK;
+#pragma unroll
+  for (int i = 0; i < NK; ++i) {
+    dst[t * REC + kk] = acc[kk * (NT + 1) + t];
+    t += DT;
+    kk += DK;
+    if (kk >= NK) {
+      kk -= NK;
+      ++t;
+    }
+  }
+}
+
 // ------------------------------------------------------------------ heat
 // Structural zeros of the T6 reference tensors for quadrature rules that
 // integrate the products of the (linear) parametric gradients exactly, e.g.
@@ -575,7 +601,7 @@ __global__ void __launch_bounds__(kIntThreads) heat_t6s_k(int64_t nel, const int
       a[9 * LD] = bs[6];
       a[10 * LD] = 0.0;
     }
-    write_records_part<NT>(acc, NS, 0, 11, e0, nel, kstore);
+    write_records_fixed<NT, NS, 11>(acc, 0, e0, nel, kstore);
     __syncthreads();
     if (e < nel) {
       const double m4 = t6r_scale(bs[4], 1), m3 = t6r_scale(bs[3], 1);
@@ -590,7 +616,7 @@ __global__ void __launch_bounds__(kIntThreads) heat_t6s_k(int64_t nel, const int
       a[8 * LD] = t6r_scale(bs[1], 2);      // 19
       a[9 * LD] = bs[6];                    // 20
     }
-    write_records_part<NT>(acc, NS, 11, 10, e0, nel, kstore);
+    write_records_fixed<NT, NS, 10>(acc, 11, e0, nel, kstore);
     if (FDIRECT) {
       if (e < nel) {
         const int32_t* d = dofs + e * NN;
