@@ -457,12 +457,6 @@ int build_pattern(Ctx* c, const SlotGen& g0, int64_t nrow, int64_t ncol, Pattern
   nzkey.release(c);
   set_last_k<<<1, 1, 0, st>>>(P->cptr.p, nnz, M);
   ELFEL_LAUNCH_CHECK(c);
-  if (nnz > 0 && nrow > 1) {  // 1 x n patterns (vectors) are reduced without windows
-    const int64_t nwin = (nnz + kReduceWindow - 1) / kReduceWindow;
-    ELFEL_TRY(P->perm.alloc(c, (size_t)(nwin * kReduceWindow)));
-    window_order_k<<<grid_for(nwin, 8, (int64_t)c->sm_count * 16), 256, 0, st>>>(P->cptr.p, nnz, P->perm.p);
-    ELFEL_LAUNCH_CHECK(c);
-  }
   keys.release(c);
   colcnt.release(c);
   colstart.release(c);
@@ -594,8 +588,19 @@ int reduce_batch(Ctx* c, const RedJob* jobs_dev, int njobs, int64_t blocks) {
   return ELFEL_OK;
 }
 
-int reduce_values(Ctx* c, const Pattern& P, const double* store, double* vals_out) {
+int reduce_values(Ctx* c, Pattern& P, const double* store, double* vals_out) {
   if (P.nnz == 0) return ELFEL_OK;
+  // The count order (window_order_k) pays for itself from a pattern's second
+  // reduction on; a pattern reduced once (an end-to-end call) does without it.
+  // Both kernels add every nonzero's contributions in slot order: same bits.
+  // 1 x n patterns (vectors) are reduced by reduce_dense.
+  if (!P.perm.p && P.reductions >= 1 && P.nrow > 1) {
+    const int64_t nwin = (P.nnz + kReduceWindow - 1) / kReduceWindow;
+    ELFEL_TRY(P.perm.alloc(c, (size_t)(nwin * kReduceWindow)));
+    window_order_k<<<grid_for(nwin, 8, (int64_t)c->sm_count * 16), 256, 0, c->stream>>>(P.cptr.p, P.nnz, P.perm.p);
+    ELFEL_LAUNCH_CHECK(c);
+  }
+  P.reductions++;
   if (P.perm.p) {
     const int64_t nwin = (P.nnz + kReduceWindow - 1) / kReduceWindow;
     reduce_win_k<<<grid_for(nwin, 8, (int64_t)c->sm_count * 16), 256, 0, c->stream>>>(

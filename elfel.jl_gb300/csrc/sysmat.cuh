@@ -182,12 +182,14 @@ struct Pattern {
   DBuf<int32_t> cptr;     // nnz+1: contributors of nonzero k are contrib[cptr[k] .. cptr[k+1])
   DBuf<int32_t> contrib;  // nslots: storage index of each contribution, ascending slot order
   DBuf<uint8_t> perm;     // per window of kReduceWindow nonzeros: their order by contributor count
+  int reductions = 0;     // value reductions run on this pattern (perm is built for the second)
   void release(Ctx* c) {
     colptr.release(c);
     rowval.release(c);
     cptr.release(c);
     contrib.release(c);
     perm.release(c);
+    reductions = 0;
     nrow = ncol = nnz = nslots = 0;
   }
 };
@@ -196,7 +198,7 @@ struct Pattern {
 int build_pattern(Ctx* c, const SlotGen& g, int64_t nrow, int64_t ncol, Pattern* P);
 
 // vals_out[k] = sum of store[contrib[t]] over t in [cptr[k], cptr[k+1]), in order.
-int reduce_values(Ctx* c, const Pattern& P, const double* store, double* vals_out);
+int reduce_values(Ctx* c, Pattern& P, const double* store, double* vals_out);
 // Dense vector of a 1 x n pattern (the rhs): out[c] = contributions of column c.
 int reduce_dense(Ctx* c, const Pattern& P, const double* store, double* out);
 
