@@ -28,7 +28,7 @@ struct Ctx {
   cudaStream_t own_stream = nullptr;  // the context's own stream
   cudaStream_t aux = nullptr;         // second stream for uploads that overlap work on `stream` (lazy)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  int pageable_access = 0;            // kernels may read pageable host memory (ATS)
+  int pageable_access = 0;            // kernels may read pageable host memory in place (ATS)
   cudaMemPool_t pool = nullptr;  // the context's stream-ordered pool (keeps freed memory for reuse)
   int64_t budget = 0;       // bytes the context may hold on the device (0 = unlimited)
   int64_t in_use = 0;       // bytes currently held

@@ -217,9 +217,17 @@ extern "C" int elfel_ctx_create(int device, int64_t mem_budget_bytes, elfel_ctx*
       h->c.pool = nullptr;  // the device's default pool then
     }
   }
-  if (cudaDeviceGetAttribute(&h->c.pageable_access, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) {
-    cudaGetLastError();
-    h->c.pageable_access = 0;
+  {
+    // Kernels read pageable host memory in place only where the device walks
+    // the host's page tables (ATS, as on Grace); with HMM alone an access
+    // faults and migrates pages, and the copy engines are used instead.
+    int pa = 0, hpt = 0;
+    if (cudaDeviceGetAttribute(&pa, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&hpt, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device) != cudaSuccess) {
+      cudaGetLastError();
+      pa = hpt = 0;
+    }
+    h->c.pageable_access = pa && hpt;
   }
   const char* tr = getenv("ELFEL_TRACE");
   h->c.trace = (tr && tr[0] == '1') ? 1 : 0;
