@@ -129,13 +129,13 @@ __device__ void warp_sort(uint64_t* a, int n, int lane) {
 // Register-resident bitonic sort of P <= 32 keys, one per lane: lanes 0..P-1
 // end ascending (every group of P lanes is sorted, in alternating
 // directions); shuffles exchange the partners.  Unused lanes hold ~0.
-template <int P>
-__device__ __forceinline__ uint64_t reg_sort(uint64_t v, int lane) {
+template <int P, typename K>
+__device__ __forceinline__ K reg_sort(K v, int lane) {
 #pragma unroll
   for (int k = 2; k <= P; k <<= 1) {
 #pragma unroll
     for (int j = k >> 1; j > 0; j >>= 1) {
-      const uint64_t o = __shfl_xor_sync(0xffffffffu, v, j);
+      const K o = __shfl_xor_sync(0xffffffffu, v, j);
       const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
       v = keep_min ? (v < o ? v : o) : (v < o ? o : v);
     }
@@ -146,13 +146,61 @@ __device__ __forceinline__ uint64_t reg_sort(uint64_t v, int lane) {
 // Number of keys of a sequence sorted ascending across the warp's lanes
 // (one per lane, padding ~0) that are below x (keys are distinct): a binary
 // search whose probes are per-lane shuffles.
-__device__ __forceinline__ int count_below(uint64_t seq, uint64_t x) {
+template <typename K>
+__device__ __forceinline__ int count_below(K seq, K x) {
   int pos = 0;
 #pragma unroll
   for (int step = 16; step > 0; step >>= 1)
     if (__shfl_sync(0xffffffffu, seq, pos + step - 1) < x) pos += step;
   if (__shfl_sync(0xffffffffu, seq, pos) < x) ++pos;
   return pos;
+}
+
+// A column's (row, slot) keys as 32 bits, (row - rmin) << sb | (slot - smin),
+// when the two spans fit in 31 bits together: the order is kept, ~0u stays
+// above every key (padding), and a compare-exchange stage of the register
+// sorts costs half the instructions of the 64-bit one.
+struct Pack32 {
+  uint32_t rmin, smin;
+  int sb;
+};
+
+__device__ __forceinline__ uint32_t pack32(uint64_t v, const Pack32& p) {
+  return (((uint32_t)(v >> 32) - p.rmin) << p.sb) | ((uint32_t)v - p.smin);
+}
+
+__device__ __forceinline__ uint64_t unpack32(uint32_t k, const Pack32& p) {
+  return ((uint64_t)(p.rmin + (k >> p.sb)) << 32) | (uint64_t)(p.smin + (k & ((1u << p.sb) - 1u)));
+}
+
+__device__ __forceinline__ int bit_length(uint32_t x) { return x ? 32 - __clz((int)x) : 0; }
+
+// The packing of the keys of the whole warp (valid keys: lo <= hi per field;
+// lanes without keys pass lo = ~0u, hi = 0); false when it does not fit.
+__device__ __forceinline__ bool pack_warp(uint32_t rlo, uint32_t rhi, uint32_t slo, uint32_t shi, Pack32* p) {
+  const uint32_t rmin = __reduce_min_sync(0xffffffffu, rlo), rmax = __reduce_max_sync(0xffffffffu, rhi);
+  const uint32_t smin = __reduce_min_sync(0xffffffffu, slo), smax = __reduce_max_sync(0xffffffffu, shi);
+  if (rmax < rmin || smax < smin) return false;
+  const int sb = bit_length(smax - smin);
+  if (bit_length(rmax - rmin) + sb > 31) return false;
+  *p = Pack32{rmin, smin, sb};
+  return true;
+}
+
+// The same for each half warp separately (xor partners below 16).
+__device__ __forceinline__ bool pack_half(uint32_t rlo, uint32_t rhi, uint32_t slo, uint32_t shi, Pack32* p) {
+#pragma unroll
+  for (int o = 8; o > 0; o >>= 1) {
+    rlo = min(rlo, __shfl_xor_sync(0xffffffffu, rlo, o));
+    rhi = max(rhi, __shfl_xor_sync(0xffffffffu, rhi, o));
+    slo = min(slo, __shfl_xor_sync(0xffffffffu, slo, o));
+    shi = max(shi, __shfl_xor_sync(0xffffffffu, shi, o));
+  }
+  if (rhi < rlo || shi < slo) return false;
+  const int sb = bit_length(shi - slo);
+  if (bit_length(rhi - rlo) + sb > 31) return false;
+  *p = Pack32{rlo, slo, sb};
+  return true;
 }
 
 // Output of a sorted column: each key's storage index goes to contrib[b + t]
@@ -179,16 +227,34 @@ __device__ __forceinline__ void sort_column_merge(const SlotGen& g, const ColOut
                                                   const uint64_t* keys, int32_t* cnt_out, uint64_t* sh, int lane) {
   uint64_t v0 = keys[b + lane];
   uint64_t v1 = lane + 32 < n ? keys[b + lane + 32] : ~0ull;
-  v0 = reg_sort<32>(v0, lane);
   const int m = n - 32;
-  if (m > 16) v1 = reg_sort<32>(v1, lane);
-  else if (m > 8) v1 = reg_sort<16>(v1, lane);
-  else if (m > 4) v1 = reg_sort<8>(v1, lane);
-  else if (m > 1) v1 = reg_sort<4>(v1, lane);
-  const int r0 = lane + count_below(v1, v0);
-  const int r1 = lane + count_below(v0, v1);
-  sh[r0] = v0;
-  if (lane < m) sh[r1] = v1;
+  const bool has1 = lane < m;
+  const uint32_t r0v = (uint32_t)(v0 >> 32), s0v = (uint32_t)v0;
+  const uint32_t r1v = (uint32_t)(v1 >> 32), s1v = (uint32_t)v1;
+  Pack32 pk;
+  if (pack_warp(has1 ? min(r0v, r1v) : r0v, has1 ? max(r0v, r1v) : r0v, has1 ? min(s0v, s1v) : s0v,
+                has1 ? max(s0v, s1v) : s0v, &pk)) {
+    uint32_t k0 = pack32(v0, pk), k1 = has1 ? pack32(v1, pk) : ~0u;
+    k0 = reg_sort<32>(k0, lane);
+    if (m > 16) k1 = reg_sort<32>(k1, lane);
+    else if (m > 8) k1 = reg_sort<16>(k1, lane);
+    else if (m > 4) k1 = reg_sort<8>(k1, lane);
+    else if (m > 1) k1 = reg_sort<4>(k1, lane);
+    const int r0 = lane + count_below(k1, k0);
+    const int r1 = lane + count_below(k0, k1);
+    sh[r0] = unpack32(k0, pk);
+    if (has1) sh[r1] = unpack32(k1, pk);
+  } else {
+    v0 = reg_sort<32>(v0, lane);
+    if (m > 16) v1 = reg_sort<32>(v1, lane);
+    else if (m > 8) v1 = reg_sort<16>(v1, lane);
+    else if (m > 4) v1 = reg_sort<8>(v1, lane);
+    else if (m > 1) v1 = reg_sort<4>(v1, lane);
+    const int r0 = lane + count_below(v1, v0);
+    const int r1 = lane + count_below(v0, v1);
+    sh[r0] = v0;
+    if (has1) sh[r1] = v1;
+  }
   __syncwarp();
   const uint64_t s0 = sh[lane], s1 = lane + 32 < n ? sh[lane + 32] : ~0ull;
   const uint64_t p0 = __shfl_up_sync(0xffffffffu, s0, 1);
@@ -214,11 +280,23 @@ __device__ void sort_column(const SlotGen& g, const ColOut& o, int64_t b, int n,
                             uint64_t* sh, int lane) {
   const unsigned below = (1u << lane) - 1u;
   if (n <= 32) {
-    uint64_t v = lane < n ? keys[b + lane] : ~0ull;
-    if (n > 16) v = reg_sort<32>(v, lane);
-    else if (n > 8) v = reg_sort<16>(v, lane);
-    else if (n > 4) v = reg_sort<8>(v, lane);
-    else if (n > 1) v = reg_sort<4>(v, lane);
+    const bool has = lane < n;
+    uint64_t v = has ? keys[b + lane] : ~0ull;
+    Pack32 pk;
+    const uint32_t rv = (uint32_t)(v >> 32), sv = (uint32_t)v;
+    if (n > 1 && pack_warp(has ? rv : ~0u, has ? rv : 0u, has ? sv : ~0u, has ? sv : 0u, &pk)) {
+      uint32_t k = has ? pack32(v, pk) : ~0u;
+      if (n > 16) k = reg_sort<32>(k, lane);
+      else if (n > 8) k = reg_sort<16>(k, lane);
+      else if (n > 4) k = reg_sort<8>(k, lane);
+      else k = reg_sort<4>(k, lane);
+      v = has ? unpack32(k, pk) : ~0ull;
+    } else {
+      if (n > 16) v = reg_sort<32>(v, lane);
+      else if (n > 8) v = reg_sort<16>(v, lane);
+      else if (n > 4) v = reg_sort<8>(v, lane);
+      else if (n > 1) v = reg_sort<4>(v, lane);
+    }
     // distinct rows: a key starts a row when its predecessor has another row
     const uint64_t pv = __shfl_up_sync(0xffffffffu, v, 1);
     const bool first = lane < n && (lane == 0 || (v >> 32) != (pv >> 32));
@@ -300,8 +378,20 @@ __global__ void __launch_bounds__(kSortThreads) sort_cols_k(SlotGen g, ColOut o,
         const int q = 2 * r + h;
         const int64_t b = __shfl_sync(0xffffffffu, bg, q * 8);
         const int n = __shfl_sync(0xffffffffu, ng, q * 8);
-        uint64_t v = hl < n ? keys[b + hl] : ~0ull;
-        v = reg_sort<16>(v, hl);  // partners lane ^ j (j < 16) stay inside the half
+        const bool has = hl < n;
+        uint64_t v = has ? keys[b + hl] : ~0ull;
+        const uint32_t rv = (uint32_t)(v >> 32), sv = (uint32_t)v;
+        Pack32 pk;
+        // partners lane ^ j (j < 16) stay inside the half; both halves take
+        // the same branch only when both packings fit
+        const bool fit = pack_half(has ? rv : ~0u, has ? rv : 0u, has ? sv : ~0u, has ? sv : 0u, &pk);
+        if (__all_sync(0xffffffffu, fit || n <= 1)) {
+          uint32_t k = has && n > 1 ? pack32(v, pk) : ~0u;
+          k = reg_sort<16>(k, hl);
+          if (n > 1) v = has ? unpack32(k, pk) : ~0ull;
+        } else {
+          v = reg_sort<16>(v, hl);
+        }
         const uint64_t pv = __shfl_up_sync(0xffffffffu, v, 1, 16);
         const bool first = hl < n && (hl == 0 || (v >> 32) != (pv >> 32));
         const unsigned m = __ballot_sync(0xffffffffu, first) & half;
