@@ -8,19 +8,25 @@
 //   * rows ascend within each column.
 //
 // Steps (all deterministic; integer atomics only count and bucket):
-//   1. column counts                           (int32 atomics)
+//   1. column counts (one int32 atomic per column group in block mode, per
+//      slot in COO mode)
 //   2. exclusive scan -> column starts
-//   3. bucket each slot's key (row << 32 | slot) into its column
-//   4. sort each column's keys (one warp per column, bitonic network)
-//   5. count distinct rows per column, scan -> colptr
-//   6. the storage index of every contribution (contrib), in sorted order,
-//      written by the sort; rowval and the first contribution of each
-//      nonzero (cptr) compacted from the sort's row starts.
+//   3. bucket each slot's key (row << 32 | slot) into its column (one cursor
+//      atomic per run of equal columns within a warp; the order inside a
+//      column does not matter, the keys carry the slot)
+//   4. sort each column's keys in registers (bitonic networks sized to the
+//      column, 32-bit packed keys where the spans fit, 33-64 keys merged by
+//      rank), count its distinct rows, write the storage index of every
+//      contribution (contrib) in sorted order and the column's row starts
+//   5. scan -> colptr; compact the row starts into rowval and the first
+//      contribution of each nonzero (cptr)
+//   6. (at a pattern's second value reduction) the contributor-count order
+//      of each window of 128 nonzeros (window_order_k).
 #include "sysmat.cuh"
 
 namespace elfel {
 
-constexpr int kSortThreads = 256;           // 8 warps, one column each
+constexpr int kSortThreads = 256;           // 8 warps
 constexpr int kSortCap = 256;               // keys per warp sorted in shared memory
 
 // Block mode: one thread per column group (one atomic per group instead of
