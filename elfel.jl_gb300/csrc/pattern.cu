@@ -22,6 +22,7 @@
 //      contribution of each nonzero (cptr)
 //   6. (at a pattern's second value reduction) the contributor-count order
 //      of each window of 128 nonzeros (window_order_k).
+#include "pack32.cuh"
 #include "sysmat.cuh"
 
 namespace elfel {
@@ -162,27 +163,13 @@ __device__ __forceinline__ int count_below(K seq, K x) {
   return pos;
 }
 
-// A column's (row, slot) keys as 32 bits, (row - rmin) << sb | (slot - smin),
-// when the two spans fit in 31 bits together: the order is kept, ~0u stays
-// above every key (padding), and a compare-exchange stage of the register
-// sorts costs half the instructions of the 64-bit one.
-struct Pack32 {
-  uint32_t rmin, smin;
-  int sb;
-};
-
-__device__ __forceinline__ uint32_t pack32(uint64_t v, const Pack32& p) {
-  return (((uint32_t)(v >> 32) - p.rmin) << p.sb) | ((uint32_t)v - p.smin);
-}
-
-__device__ __forceinline__ uint64_t unpack32(uint32_t k, const Pack32& p) {
-  return ((uint64_t)(p.rmin + (k >> p.sb)) << 32) | (uint64_t)(p.smin + (k & ((1u << p.sb) - 1u)));
-}
-
 __device__ __forceinline__ int bit_length(uint32_t x) { return x ? 32 - __clz((int)x) : 0; }
 
-// The packing of the keys of the whole warp (valid keys: lo <= hi per field;
-// lanes without keys pass lo = ~0u, hi = 0); false when it does not fit.
+// A column whose row and slot spans fit in 31 bits together is sorted on
+// 32-bit packed keys (pack32.cuh): a compare-exchange stage of the register
+// sorts then costs half the instructions of the 64-bit one.  The packing of
+// the keys of the whole warp (valid keys: lo <= hi per field; lanes without
+// keys pass lo = ~0u, hi = 0); false when it does not fit.
 __device__ __forceinline__ bool pack_warp(uint32_t rlo, uint32_t rhi, uint32_t slo, uint32_t shi, Pack32* p) {
   const uint32_t rmin = __reduce_min_sync(0xffffffffu, rlo), rmax = __reduce_max_sync(0xffffffffu, rhi);
   const uint32_t smin = __reduce_min_sync(0xffffffffu, slo), smax = __reduce_max_sync(0xffffffffu, shi);

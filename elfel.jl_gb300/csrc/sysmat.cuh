@@ -37,7 +37,13 @@ struct FastDiv {
     while ((1ull << s) < d) ++s;
     m = (uint32_t)((((uint64_t)1 << 32) * (((uint64_t)1 << s) - d)) / d + 1);
   }
-  __device__ __forceinline__ uint32_t div(uint32_t n) const { return (__umulhi(n, m) + n) >> s; }
+  __host__ __device__ __forceinline__ uint32_t div(uint32_t n) const {
+#ifdef __CUDA_ARCH__
+    return (__umulhi(n, m) + n) >> s;
+#else
+    return (uint32_t)((((uint64_t)n * m) >> 32) + n) >> s;
+#endif
+  }
 };
 
 struct SlotGen {
