@@ -390,6 +390,16 @@ def max_over_ranks(x, dist, device="cpu"):
     return float(t.item())
 
 
+def heat_config(N, ws):
+    """The workload both arms report: the T6 heat problem on N x N cells."""
+    nel, nnodes = 2 * N * N, (2 * N + 1) ** 2
+    return {"workload": f"heat T6 {N}x{N} ({nel} elements, {nnodes} nodes), 3-point rule, "
+                        f"fused K+F assembly, pattern reused",
+            "elements": nel, "ndofs": nnodes, "nnz": 46 * N * N + 16 * N + 1,
+            "l2": "256 MB buffer written between timed steps",
+            "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU"}
+
+
 def reference_arm(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -420,8 +430,7 @@ def reference_arm(args):
     out = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-           "config": {"workload": "heat T6 1000x1000 (2M elements), reference CPU path on a 200x200 sample",
-                      "sample_elements": int(mesh.nel), "parallelism": "host threads"},
+           "config": heat_config(args.n or 1000, ws),
            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                             "sample": f"T6 heat 200x200 ({mesh.nel} elements): element loop (OpenMP) + COO + "
                                       f"sparse() (1 thread) + vector assembly, mean of {len(step_times)} steps"},
@@ -680,10 +689,7 @@ def main():
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f64", "data": "synthetic (seeded T6 mesh, jitter 0.2h, kappa log-uniform [0.5,2])",
-           "config": {"workload": f"heat T6 {N}x{N} ({nel} elements, {mesh.nnodes} nodes), 3-point rule, "
-                                  f"fused K+F assembly, pattern reused",
-                      "elements": nel, "ndofs": n, "nnz": nnz_dev, "l2": "256 MB buffer written between timed steps",
-                      "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU"},
+           "config": heat_config(N, ws),
            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": (2 if f_direct else 3) * args.steps, "clocks": clk,
            "pcg": pcg, "serve": serve, "fma_rates": rates, "pattern_build_s": pattern_s, "setup_phases_ms": {k: v[0] for k, v in setup_phases.items()},
            "wall_s_timed": wall, "host_mesh_setup_s": host_setup_s}
