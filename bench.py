@@ -40,6 +40,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+CLOCK_WINDOW_S = 1.5
 METRIC = "elems assembled/s; PCG time (FP32+refine vs FP64) at 1e-10; serve p50/p99"
 UNIT = "elements/s"
 
@@ -303,7 +304,7 @@ class Clocks:
         try:
             self.f = open(self.path, "w")
             self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={self.Q}", "--format=csv,noheader",
-                                       "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+                                       "-lms", "50"], stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.p = None
 
@@ -348,27 +349,38 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_assembly_rate(E, O, N, threads, budget_s):
-    """Oracle (CPU restatement of the reference path) assembly throughput on a bounded sample."""
-    mesh, fesp, kappa = build_problem(E, N)
+def cpu_reference_step(O, conn0, xy, ed, kappa, n):
+    """One assembly of K and F by the CPU restatement of the reference path
+    (test/test_heat.jl:35-71): the element loop (OpenMP over elements), the
+    COO triplets of assemble! (column-major init!), SparseArrays.sparse
+    semantics (single-threaded counting sorts, duplicates summed in append
+    order) and the SysvecAssembler accumulation."""
+    ke, fe = O.heat_element_matrices(6, 3, conn0, xy, kappa, -6.0)
+    I, J, V = O.local_coo(ed, ed, ke)
+    del ke
+    K = O.sparse(I, J, V, n, n)
+    del I, J, V
+    F = O.vec_assemble(n, ed, fe)
+    return K, F
+
+
+def cpu_reference_rate(O, mesh, fesp, kappa, E, threads, steps, warmup=0):
+    """Elements per second of cpu_reference_step on the whole mesh with
+    `threads` OpenMP threads (mean over `steps` timed steps after `warmup`)."""
     ed = E.FEIterator(fesp).eldofs_table() - 1
+    conn0 = np.ascontiguousarray(mesh.conn - 1)
     n = E.ndofs(fesp)
     O.set_threads(threads)
-    conn0 = mesh.conn - 1
     times = []
-    t_end = time.perf_counter() + budget_s
-    while True:
+    for k in range(warmup + steps):
         t0 = time.perf_counter()
-        ke, fe = O.heat_element_matrices(6, 3, conn0, mesh.xy, kappa, -6.0)
-        I, J, V = O.local_coo(ed, ed, ke)
-        K = O.sparse(I, J, V, n, n)
-        F = O.vec_assemble(n, ed, fe)
-        times.append(time.perf_counter() - t0)
-        if time.perf_counter() > t_end and len(times) >= 2:
-            break
-    del K, F
-    t = statistics.median(times)
-    return mesh.nel / t, t, len(times), mesh.nel
+        K, F = cpu_reference_step(O, conn0, mesh.xy, ed, kappa, n)
+        dt = time.perf_counter() - t0
+        del K, F
+        if k >= warmup:
+            times.append(dt)
+    t = sum(times) / len(times)
+    return mesh.nel / t, t, len(times)
 
 
 def dist_env():
@@ -401,6 +413,11 @@ def heat_config(N, ws):
 
 
 def reference_arm(args):
+    """The reference's own CPU path on the host cores, on the GPU arm's
+    workload (the whole 2M-element mesh at the default size): every step is
+    one complete assembly of K and F.  The steps run with all host threads in
+    the element loop; one more step runs single-threaded, as the reference
+    itself does (Julia, no threads), and is reported beside them."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
@@ -409,31 +426,20 @@ def reference_arm(args):
     E = entry.package()
     O = entry.oracle()
     threads = os.cpu_count() or 1
-    # bounded sample of the same workload: 200 x 200 cells (80,000 T6 elements)
-    N = 200
+    N = args.n or 1000
     mesh, fesp, kappa = build_problem(E, N)
-    ed = E.FEIterator(fesp).eldofs_table() - 1
-    n = E.ndofs(fesp)
-    O.set_threads(threads)
-    step_times = []
-    for k in range(args.warmup + args.steps):
-        t0 = time.perf_counter()
-        ke, fe = O.heat_element_matrices(6, 3, mesh.conn - 1, mesh.xy, kappa, -6.0)
-        I, J, V = O.local_coo(ed, ed, ke)
-        K = O.sparse(I, J, V, n, n)
-        F = O.vec_assemble(n, ed, fe)
-        dt = time.perf_counter() - t0
-        if k >= args.warmup:
-            step_times.append(dt)
-    t = sum(step_times) / len(step_times)
-    v = mesh.nel / t
+    v, t, nsteps = cpu_reference_rate(O, mesh, fesp, kappa, E, threads, args.steps, args.warmup)
+    v1, t1, _ = cpu_reference_rate(O, mesh, fesp, kappa, E, 1, 1)
+    what = (f"T6 heat {N}x{N} ({mesh.nel} elements), the whole mesh every step: element loop + COO triplets + "
+            f"sparse() (single-threaded) + vector assembly")
     out = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-           "config": heat_config(args.n or 1000, ws),
+           "config": heat_config(N, ws),
            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                            "sample": f"T6 heat 200x200 ({mesh.nel} elements): element loop (OpenMP) + COO + "
-                                      f"sparse() (1 thread) + vector assembly, mean of {len(step_times)} steps"},
+                            "sample": f"{what}; element loop on {threads} threads; mean of {nsteps} steps",
+                            "single_thread": {"value": v1, "unit": UNIT, "cores": 1, "ms_per_step": t1 * 1e3,
+                                              "sample": f"{what}; one thread throughout; one step"}},
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
     return 0
@@ -452,7 +458,7 @@ def main():
     ap.add_argument("--no-pcg", action="store_true")
     ap.add_argument("--pcg-methods", default="pcg64,pcg32_ir", help="solves to run, in order")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--cpu-steps", type=int, default=2, help="full-size CPU reference steps of the cpu_baseline")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=512, help="requests of the serving stream (4096: all)")
     ap.add_argument("--serve-rates", default="0.5,0.7,0.9", help="arrival rates as fractions of the capacity")
@@ -538,10 +544,22 @@ def main():
             evs.append((a, b))
         torch.cuda.synchronize()
         wall = time.perf_counter() - wall0
+        ctx.profile(False)
+        # the timed steps take milliseconds, shorter than the sampler's period:
+        # the same steps continue, untimed, for CLOCK_WINDOW_S so that the
+        # clock record covers the timed steps and this continuation
+        t_ext = time.perf_counter()
+        ext = 0
+        while time.perf_counter() - t_ext < CLOCK_WINDOW_S:
+            for _ in range(50):
+                flush.zero_()
+                am.heat(None, -6.0)
+            torch.cuda.synchronize()
+            ext += 50
         clocks.mark(dt0, datetime.datetime.now())
         clk = clocks.stop()
+        clk["window"] = f"the {args.steps} timed steps and {ext} more of the same steps right after them"
     phases = ctx.phases()
-    ctx.profile(False)
     step_ms = [a.elapsed_time(b) for a, b in evs]
     t_step = sum(step_ms) / len(step_ms) / 1e3
     t_step = max_over_ranks(t_step, dist, f"cuda:{local}" if torch.cuda.is_available() else "cpu")
@@ -555,19 +573,22 @@ def main():
     # without a reduce_F phase the integration kernel added the load vector
     # itself (midside DOFs read, the vector written) instead of writing records
     f_direct = "reduce_F" not in per
-    alg = {  # compulsory bytes of each kernel per launch, as designed
+    design = {  # bytes each kernel itself must move per launch, as designed (its own inputs and outputs)
         "integrate_heat": nel * 6 * 4 + mesh.nnodes * 16 + nel * 8 + nel * 21 * 8 +
                           (nel * 3 * 4 + n * 8 if f_direct else nel * 6 * 8),
         "reduce_K": (nnz_est + 1) * 4 + nslots * 4 + nel * 21 * 8 + nnz_est * 8,
         "reduce_F": (n + 1) * 8 + (n + 1) * 4 + nel * 6 * 4 + nel * 6 * 8 + n * 8,
     }
     dom = max(per, key=per.get)
-    kernel_rows = {k: {"ms_per_launch": per[k], "alg_bytes": alg.get(k),
-                       "gbs": (alg[k] / (per[k] * 1e-3) / 1e9) if k in alg and per[k] else None,
-                       "share": per[k] / sum(per.values())} for k in per}
-    # whole-assembly algorithmic bytes (conn + coords + coefficient + K values + F)
+    # algorithmic bytes of one assembly, the roofline's numerator: connectivity
+    # (6 x int32 per element) + node coordinates (16 B per node) + conductivity
+    # (8 B per element) + K values (8 B per nonzero) + F (8 B per DOF), each
+    # read or written once -- 264 B per element, 528.2 MB at 2M elements
     asm_bytes = nel * 6 * 4 + mesh.nnodes * 16 + nel * 8 + nnz_est * 8 + n * 8
-    ach = alg[dom] / (per[dom] * 1e-3) / 1e9
+    kernel_rows = {k: {"ms_per_launch": per[k], "share": per[k] / sum(per.values()),
+                       "design_bytes": design.get(k),
+                       "design_gbs": (design[k] / (per[k] * 1e-3) / 1e9) if k in design and per[k] else None}
+                   for k in per}
     # DRAM traffic of one launch of each kernel (dram__bytes_read.sum + dram__bytes_write.sum)
     # measured with ncu on the 700 x 700 case of this workload (980,000 elements; heat_t6s_k<2, 1>
     # adding the load vector 86.84 + 121.46 MB, heat_t6s_k<2, 0> writing load records 47.34 +
@@ -580,11 +601,15 @@ def main():
     traffic = TRAFFIC_PER_ELEMENT[dom] * nel if dom in TRAFFIC_PER_ELEMENT else None
     for k, row in kernel_rows.items():
         row["traffic"] = TRAFFIC_PER_ELEMENT[k] * nel if k in TRAFFIC_PER_ELEMENT else None
+    ach = asm_bytes / (per[dom] * 1e-3) / 1e9
     roofline = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-                "traffic": traffic, "kernel": dom, "peak_kind": peak_kind,
+                "traffic": traffic, "kernel": dom, "peak_kind": peak_kind, "alg_bytes": asm_bytes,
+                "alg_bytes_what": "one assembly: connectivity + coordinates + conductivity + K values + F, once each "
+                                  "(264 B/element); achieved = these bytes / the dominant kernel's mean CUDA-event "
+                                  "time",
                 "traffic_source": "ncu DRAM bytes of the kernel at 980,000 elements, scaled per element",
                 "assembly": {"alg_bytes": asm_bytes, "achieved": asm_bytes / t_step / 1e9,
-                             "frac": asm_bytes / t_step / 1e9 / hbm},
+                             "frac": asm_bytes / t_step / 1e9 / hbm, "what": "the same bytes / the whole step"},
                 "kernels": kernel_rows}
 
     # --- e2e through the C ABI from pinned host buffers -------------------
@@ -681,10 +706,11 @@ def main():
     if rank == 0 and not args.no_cpu:
         O = entry.oracle()
         threads = os.cpu_count() or 1
-        rate, tper, reps, sel = cpu_assembly_rate(E, O, 200, threads, args.cpu_budget)
+        rate, tper, reps = cpu_reference_rate(O, mesh, fesp, kappa, E, threads, args.cpu_steps)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"T6 heat 200x200 ({sel} elements): element loop (OpenMP) + COO + sparse() (1 thread) + "
-                         f"vector assembly; median of {reps} runs, {tper:.3f} s each"}
+               "sample": f"T6 heat {N}x{N} ({nel} elements), the whole mesh: element loop ({threads} threads) + "
+                         f"COO triplets + sparse() (single-threaded) + vector assembly; mean of {reps} steps, "
+                         f"{tper:.3f} s each"}
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

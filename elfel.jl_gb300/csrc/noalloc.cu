@@ -8,9 +8,10 @@
 // scratch in one file-scope device array of fixed size (kNaBytes, about 16 MB,
 // held by every GPU that loads the library until the process exits).
 //
-// Result: out[r] = sum of vals[s] over the entries s with rows[s] == r + 1,
-// added in increasing s -- the same order, hence the same bits, as
-// elfel_sysvec_assemble and the reference's SysvecAssembler.
+// Result: out[r] = +0 plus vals[s] over the entries s with rows[s] == r + 1,
+// added in increasing s -- the same order, hence the same bits (signed zeros
+// included), as elfel_sysvec_assemble and the reference's SysvecAssembler.
+// A row number outside 1..nrow fails the call and leaves out unchanged.
 //
 // Steps: clear counters, count per row (integer atomics), exclusive scan,
 // bucket entry indices per row, sort each row's indices (one warp per row),
@@ -169,6 +170,9 @@ __global__ void __launch_bounds__(256) na_sum_k(View v, const double* __restrict
                                                 double* __restrict__ out) {
   __shared__ uint32_t sh[256 / 32][kNaSortCap];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  // a row number out of range (flagged by na_count_k, earlier on the stream)
+  // fails the call: out keeps its contents, as with the allocating path
+  if (*(volatile int*)v.bad) return;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x / 32);
   for (int64_t r = (int64_t)blockIdx.x * (blockDim.x / 32) + wid; r < nrow; r += warps) {
     const int64_t b = v.offsets[r];
@@ -202,11 +206,10 @@ __global__ void __launch_bounds__(256) na_sum_k(View v, const double* __restrict
       }
     }
     if (lane == 0) {
+      // from +0, as the allocating path and SysvecAssembler (which adds into
+      // zeros(T, n)): a row of negative zeros sums to +0
       double s = 0.0;
-      if (n > 0) {
-        s = vals[a[0]];
-        for (int64_t t = 1; t < n; ++t) s += vals[a[t]];
-      }
+      for (int64_t t = 0; t < n; ++t) s = __dadd_rn(s, vals[a[t]]);
       out[r] = s;
     }
     __syncwarp();
@@ -242,7 +245,11 @@ extern "C" int elfel_sysvec_assemble_noalloc(elfel_ctx* h, int64_t nrow, const i
     }
     base = g_na_addr[c->device];
   }
-  if (nrow == 0) return ELFEL_OK;
+  if (nrow == 0) {
+    if (n > 0) return fail(c, ELFEL_ERR_ARG, "sysvec_noalloc: %lld entries but no rows (every row out of range)",
+                           (long long)n);
+    return ELFEL_OK;
+  }
   const View v = carve(base);
   cudaStream_t st = c->stream;
   const unsigned g1 = grid_for(nrow, 256, (int64_t)c->sm_count * 8);

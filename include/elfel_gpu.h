@@ -110,8 +110,10 @@ ELFEL_API int elfel_sysvec_assemble(elfel_ctx* ctx, int64_t nrow, const int64_t*
  * runtime manages, or loops that must not call cudaMalloc because it
  * synchronises the device and takes unbounded time.  rows (1-based) and vals
  * (n entries) are device pointers, out (nrow doubles) is a device pointer the
- * caller owns; out[r] = sum of vals[s] over rows[s] == r+1 in increasing s, the
- * same bits as elfel_sysvec_assemble.
+ * caller owns; out[r] = +0 plus vals[s] over rows[s] == r+1 in increasing s, the
+ * same bits as elfel_sysvec_assemble (a row of negative zeros gives +0).  A row
+ * number outside 1..nrow (any entry at all when nrow is 0) returns
+ * ELFEL_ERR_ARG and leaves out unchanged.
  * Scratch: one fixed device array inside the library (about 16 MB, kept by
  * every GPU that loads the library until the process exits), so
  *   - sizes are limited to ELFEL_NOALLOC_MAX_ROWS rows and

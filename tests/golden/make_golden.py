@@ -5,10 +5,10 @@ known-answer tests are read as text and their literal values are written to
 ``tests/golden/*.json``.  Only numbers that the reference's own tests assert
 are extracted; nothing is computed here.
 
-Run from the repository root with the reference checked out at
-``ELFEL_REFERENCE`` (default: the read-only mount used while building):
+Run from the repository root with ``ELFEL_REFERENCE`` set to a checkout of
+the reference project (required; there is no default):
 
-    python tests/golden/make_golden.py
+    ELFEL_REFERENCE=/path/to/Elfel.jl python tests/golden/make_golden.py
 
 Sources (file:line in the reference project):
   test/test_assemblers.jl:6-34      7x7 COO assembly with duplicate summation
@@ -33,7 +33,7 @@ import os
 import re
 import sys
 
-REF = os.environ.get("ELFEL_REFERENCE", "/root/reference")
+REF = os.environ.get("ELFEL_REFERENCE")
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 NUM = r"[-+]?(?:\d+\.\d*|\.\d+|\d+)(?:[eE][-+]?\d+)?"
@@ -279,6 +279,8 @@ def datfile(rel):
 
 
 def main():
+    if not REF:
+        sys.exit("set ELFEL_REFERENCE to a checkout of the reference project (Elfel.jl v0.4.0)")
     if not os.path.isdir(REF):
         sys.exit(f"reference not found at {REF}")
     out = {

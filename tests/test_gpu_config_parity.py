@@ -1,0 +1,107 @@
+"""Parity at the sizes the benchmarks run: the device system against the oracle.
+
+The 2M-element T6 heat system that bench.py times (1000 x 1000 cells, jittered
+vertices, conductivity log-uniform in [0.5, 2] per element, Q = -6) is
+assembled on the device and by the oracle (element loop, COO triplets,
+SparseArrays.sparse semantics, test/test_heat.jl:35-71); the plane-strain
+elasticity and Taylor-Hood cavity systems are compared at 200 x 100 and
+100 x 100 cells.  Bars: pattern bit-exact, values within 1e-12 of the largest
+entry (relative), as in the small-mesh parity tests.
+
+The FP32-refinement solution of the 2M-element system (FP32 CG with FP64
+residual replacement, stopped at relative residual 1e-10) is compared with a
+tight FP64 reference: FP64 Jacobi-PCG driven to relative residual 1e-13 (the
+reference's own solve is SuiteSparse's direct `\\`, test/test_heat.jl:75,
+which cannot run at 4M unknowns here).  Error: max |x - x_ref| / max |x_ref|
+over the free DOFs.
+"""
+import numpy as np
+import pytest
+
+from problems import elasticity_D, elasticity_setup, stokes_oracle_K, stokes_setup, traction_oracle
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+def _close(a, b):
+    return np.abs(a - b).max() <= TOL * np.abs(b).max()
+
+
+def _same_pattern(K, K0):
+    return (K.shape == K0.shape and K.nnz == K0.nnz and np.array_equal(K.indptr, K0.indptr)
+            and np.array_equal(K.indices, K0.indices))
+
+
+@pytest.fixture(scope="module")
+def c1(E, O, gpu):
+    """The benchmark's 2M-element system, assembled on the device and by the oracle."""
+    import bench
+
+    mesh, fesp, kappa = bench.build_problem(E, 1000)
+    n, nu = E.ndofs(fesp), E.nunknowns(fesp)
+    elit, qpit = E.FEIterator(fesp), E.QPIterator(fesp, {"kind": "default", "npts": 3})
+    am = E.start(E.SysmatAssemblerGPU(gpu), n, n)
+    E.assemble_heat(am, elit, qpit, kappa, -6.0)
+    am.heat(None, -6.0)  # the benchmark's step: re-assembly on the resident pattern
+    K, F = E.finish(am), am.rhs()
+    O.set_threads(0)
+    K0, F0 = O.assemble_heat(6, 3, mesh.conn - 1, mesh.xy, elit.eldofs_table() - 1, n, kappa, -6.0)
+    yield {"am": am, "K": K, "F": F, "K0": K0, "F0": F0, "n": n, "nu": nu, "fesp": fesp, "nel": mesh.nel}
+    del am
+
+
+def test_c1_full_size_assembly_parity(E, c1):
+    K, K0, F, F0 = c1["K"], c1["K0"], c1["F"], c1["F0"]
+    assert c1["nel"] == 2_000_000 and c1["n"] == 4_004_001
+    assert K0.nnz == 46_016_001 == 46 * 1000 ** 2 + 16 * 1000 + 1
+    assert _same_pattern(K, K0), "pattern differs from the oracle at 2M elements"
+    assert _close(K.data, K0.data), np.abs(K.data - K0.data).max() / np.abs(K0.data).max()
+    assert _close(F, F0), np.abs(F - F0).max() / np.abs(F0).max()
+
+
+def test_c1_fp32_refinement_error(E, c1):
+    am, fesp, n, nu = c1["am"], c1["fesp"], c1["n"], c1["nu"]
+    T0 = np.zeros(n)
+    E.gathersysvec(T0, fesp)
+    ref = T0.copy()
+    st_ref = am.solve(ref, nu, None, method="pcg64", rtol=1e-13, maxit=200000)
+    assert st_ref["converged"], st_ref
+    errs = {}
+    for method in ("pcg64", "pcg32_ir"):
+        T = T0.copy()
+        st = am.solve(T, nu, None, method=method, rtol=1e-10, maxit=200000)
+        assert st["converged"] and st["relres"] <= 1e-10, (method, st)
+        errs[method] = float(np.abs(T[:nu] - ref[:nu]).max() / np.abs(ref[:nu]).max())
+    print(f"C1 solution error vs FP64 PCG at 1e-13 (max norm, relative): {errs}")
+    assert errs["pcg32_ir"] <= 1e-8, errs
+
+
+def test_c2_elasticity_parity(E, O, gpu):
+    """Plane-strain T6 elasticity on [0,2]x[0,1] with 200 x 100 cells."""
+    mesh, fesp, bforce, right = elasticity_setup(E, 200, 100)
+    n = E.ndofs(fesp)
+    elit = E.FEIterator(fesp)
+    am = E.start(E.SysmatAssemblerGPU(gpu), n, n)
+    E.assemble_elasticity(am, elit, E.QPIterator(fesp, {"npts": 3}), 1.0, 0.3, True, bforce, right, (1.0, 0.0))
+    K, F = E.finish(am), am.rhs()
+    ke, fe = O.elasticity_element_matrices(3, mesh.conn - 1, mesh.xy, elasticity_D(1.0, 0.3, True), bforce)
+    ed = elit.eldofs_table() - 1
+    K0 = O.sparse(*O.local_coo(ed, ed, ke), n, n)
+    F0 = O.vec_assemble(n, ed, fe) + traction_oracle(mesh, ed, right, (1.0, 0.0), n)
+    assert K0.nnz == 368 * 100 ** 2 + 96 * 100 + 4
+    assert _same_pattern(K, K0)
+    assert _close(K.data, K0.data) and _close(F, F0)
+
+
+def test_c3_stokes_cavity_parity(E, O, gpu):
+    """Taylor-Hood lid-driven cavity with 100 x 100 cells."""
+    vmesh, pmesh, ufesp, pfesp = stokes_setup(E, 100, lid=True)
+    K0, n = stokes_oracle_K(E, O, vmesh, ufesp, pfesp)
+    am = E.start(E.SysmatAssemblerGPU(gpu), n, n)
+    E.assemble_stokes(am, E.FEIterator(ufesp), E.FEIterator(pfesp), E.QPIterator(ufesp, {"npts": 3}), 1.0)
+    K = E.finish(am)
+    assert K0.nnz == 260 * 100 ** 2 + 104 * 100 + 8
+    assert _same_pattern(K, K0)
+    assert _close(K.data, K0.data)

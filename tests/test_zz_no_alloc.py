@@ -45,13 +45,23 @@ def test_noalloc_matches_allocating_entry_point(E, gpu):
         rows = rng.integers(1, nrow + 1, n)
         rows[: n // 50] = 3  # one long row (sorted in global memory)
         vals = rng.standard_normal(n)
+        # signed zeros: rows 1 and 2 receive only -0.0 (the sum is +0, as in
+        # SysvecAssembler, which adds into zeros(T, n)); the first entry of row
+        # 5 is -0.0 and the others cancel to zero
+        rows[rows == 1] = 4
+        rows[rows == 2] = 4
+        rows[rows == 5] = 6
+        rows[-6:] = [1, 1, 2, 5, 5, 5]
+        vals[-6:] = [-0.0, -0.0, -0.0, -0.0, 1.5, -1.5]
         expected = _reference(E, ctx, nrow, rows, vals)
+        assert np.signbit(expected[0]) == 0 and np.signbit(expected[1]) == 0
         rows_d = torch.from_numpy(rows).cuda()
         vals_d = torch.from_numpy(vals).cuda()
         out_d = torch.full((nrow,), float("nan"), dtype=torch.float64, device="cuda")
         ctx.check(_noalloc(ctx, nrow, rows_d, vals_d, out_d))
         got = out_d.cpu().numpy()
-        assert np.array_equal(got, expected), f"call {call}"
+        # bit for bit, signed zeros included
+        assert np.array_equal(got.view(np.int64), expected.view(np.int64)), f"call {call}"
 
 
 def test_noalloc_limits_and_errors(E, gpu):
@@ -66,5 +76,13 @@ def test_noalloc_limits_and_errors(E, gpu):
     assert rc == E._native.ELFEL_ERR_ARG
     assert "exceed" in ctx.lib.elfel_ctx_last_error(ctx.h).decode()
     bad = torch.tensor([1, 9, 2], dtype=torch.int64, device="cuda")  # row 9 > nrow = 5
+    out_d[:5] = 7.0
     rc = _noalloc(ctx, 5, bad, vals_d[:3].contiguous(), out_d)
     assert rc == E._native.ELFEL_ERR_ARG
+    assert (out_d[:5].cpu() == 7.0).all(), "out must stay unchanged when a row is out of range"
+    # entries but no rows: every row number is out of range
+    rc = _noalloc(ctx, 0, rows_d, vals_d, out_d)
+    assert rc == E._native.ELFEL_ERR_ARG
+    assert "no rows" in ctx.lib.elfel_ctx_last_error(ctx.h).decode()
+    empty = torch.empty(0, dtype=torch.int64, device="cuda")
+    assert _noalloc(ctx, 0, empty, torch.empty(0, dtype=torch.float64, device="cuda"), out_d) == 0
