@@ -448,7 +448,9 @@ def reference_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: 300 on the GPU; 10 for the reference arm, whose every step is a "
+                         "full CPU assembly of seconds)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=None, help="cells per side (heat, elasticity: 1000; Stokes: 600)")
@@ -465,6 +467,8 @@ def main():
     ap.add_argument("--serve-plain-sample", type=int, default=48)
     ap.add_argument("--probe-rates", action="store_true", help="print the device's FP64/FP32 FMA rates and exit")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 10 if args.impl == "reference" else 300
     if args.impl == "reference":
         return reference_arm(args)
     assert args.warmup >= 3 or os.environ.get("ELFEL_BENCH_ALLOW_FEW_WARMUP"), "at least 3 warm-up steps"

@@ -9,7 +9,7 @@ that scripts written against Elfel.jl translate line by line.
 """
 from . import _native
 from .assemblers import (SysmatAssemblerGPU, SysmatAssemblerSparse, SysvecAssembler, assemble, assemble_elasticity,
-                         assemble_heat, assemble_stokes, finish, solve, start)
+                         assemble_heat, assemble_stokes, finish, numberdofs_device, solve, start)
 from .batching import BatchSolver
 from .serving import HeatServer, heat_request
 from .feiterators import (FEIterator, QPIterator, bfun, bfungrad, bfungradpar, eldofcomps, eldofentmdims, eldofs,

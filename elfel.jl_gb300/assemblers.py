@@ -245,6 +245,50 @@ class SysmatAssemblerGPU:
         self._setup_key = (id(elit.fesp), id(pelit.fesp) if pelit is not None else None, qr.npts, physics, n)
         return self
 
+    def setup_numbered(self, physics, fesp, qpit, pfesp=None):
+        """Set-up with numberdofs! on the device (elfel_fused_setup_numbered):
+        only the connectivity, the coordinates and the essential-BC masks
+        (one byte per DOF) are uploaded; the DOF numbers come back into the
+        spaces' FEFields (as numberdofs!(fesp) or numberdofs!([fesp, pfesp])
+        would set them) and the element DOF tables are built on the device.
+        Returns the number of unknowns."""
+        spaces = [fesp] + ([pfesp] if pfesp is not None else [])
+        keep, structs, masks, nums = [], [], [], []
+        for sp in spaces:
+            if list(sp._fields) != [0]:
+                raise N.ElfelError(N.ELFEL_ERR_UNSUPPORTED, "device numbering takes spaces with nodal DOFs only")
+            mesh = sp.mesh
+            conn, xy = N.i64(mesh.conn), N.f64(mesh.xy)
+            mask = np.ascontiguousarray(sp.field.isdatum, dtype=np.uint8)
+            keep.extend([conn, xy, mask])
+            structs.append(N.Space(mesh.nodes_per_elem, sp.nfecopies, mesh.nel, mesh.nnodes, N.ptr(conn, N._i64p),
+                                   N.ptr(xy), None))
+            masks.append(mask)
+            nums.append(np.zeros(sp.field.dofnums.shape, dtype=np.int64))
+        qr = qpit.quadr
+        pc, w = N.f64(qr.param_coords), N.f64(qr.weights)
+        keep.extend([pc, w])
+        n = sum(sp.field.dofnums.size for sp in spaces)
+        shape, sdim = _shape_of(fesp)
+        d = N.FusedDesc(physics, qr.npts, N.ptr(pc), N.ptr(w), n, structs[0],
+                        structs[1] if len(structs) > 1 else N.Space(), shape, sdim)
+        nfree = ctypes.c_int64()
+        self._hd.check(self._hd.lib.elfel_fused_setup_numbered(
+            self._hd.h, ctypes.byref(d), masks[0].ctypes.data_as(ctypes.c_void_p),
+            masks[1].ctypes.data_as(ctypes.c_void_p) if len(masks) > 1 else None, N.ptr(nums[0], N._i64p),
+            N.ptr(nums[1], N._i64p) if len(nums) > 1 else None, ctypes.byref(nfree)))
+        for sp, nm in zip(spaces, nums):
+            sp.field.dofnums = nm
+        self._keep = keep
+        self.physics = physics
+        self.nrow = self.ncol = n
+        self.nel = fesp.mesh.nel
+        self._nn = fesp.mesh.nodes_per_elem
+        self._nedof = self._nn * fesp.nfecopies
+        self._sdim = sdim
+        self._setup_key = (id(fesp), id(pfesp) if pfesp is not None else None, qr.npts, physics, n)
+        return nfree.value
+
     def setup_block(self, etype, nx, ny, lx=1.0, ly=1.0, orientation="a", npts=3):
         """Heat set-up from a block mesh generated on the device (T3block /
         T6block of [0,lx] x [0,ly], boundary fixed, numberdofs! order).
@@ -333,6 +377,14 @@ class SysmatAssemblerGPU:
         self._hd.check(self._hd.lib.elfel_fused_stokes(self._hd.h, float(mu)))
         return self
 
+    def tile_stats(self):
+        """(tiles, distinct tile programs, tiles on the contributor-list path) of the K pattern's
+        tile reduction plan; zeros before the plan is built."""
+        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        self._hd.check(self._hd.lib.elfel_sysmat_tile_stats(self._hd.h, ctypes.byref(a), ctypes.byref(b),
+                                                            ctypes.byref(c)))
+        return a.value, b.value, c.value
+
     def set_geometry(self, xy):
         xy = N.f64(xy)
         self._hd.check(self._hd.lib.elfel_fused_set_geometry(self._hd.h, N.ptr(xy)))
@@ -348,6 +400,30 @@ class SysmatAssemblerGPU:
     def solve(self, T, nu, F=None, method="pcg32_ir", rtol=1e-10, maxit=200000):
         """solve!(T, K, F, nu) of test/test_heat.jl:73-76, on the device.  T is updated in place."""
         return _solve_handle(self._hd, T, nu, F, method, rtol, maxit)
+
+
+def numberdofs_device(fesp, ctx=None):
+    """numberdofs!(fesp) / numberdofs!([fesp1, fesp2, ...]) (src/FESpaces.jl:250-259)
+    computed on the device (elfel_number_dofs) from the spaces' essential-BC
+    masks; the numbers are written into the spaces' fields.  Returns the
+    number of unknowns.  Spaces with nodal DOFs only."""
+    spaces = list(fesp) if isinstance(fesp, (list, tuple)) else [fesp]
+    ctx = ctx or N.default_context()
+    for sp in spaces:
+        if list(sp._fields) != [0]:
+            raise N.ElfelError(N.ELFEL_ERR_UNSUPPORTED, "device numbering takes spaces with nodal DOFs only")
+    ns = len(spaces)
+    masks = [np.ascontiguousarray(sp.field.isdatum, dtype=np.uint8) for sp in spaces]
+    nums = [np.zeros(sp.field.dofnums.shape, dtype=np.int64) for sp in spaces]
+    nterms = (ctypes.c_int64 * ns)(*[sp.field.dofnums.shape[0] for sp in spaces])
+    ncomp = (ctypes.c_int32 * ns)(*[sp.field.dofnums.shape[1] for sp in spaces])
+    mp = (ctypes.c_void_p * ns)(*[m.ctypes.data_as(ctypes.c_void_p).value for m in masks])
+    np_ = (N._i64p * ns)(*[N.ptr(x, N._i64p) for x in nums])
+    nfree = ctypes.c_int64()
+    ctx.check(ctx.lib.elfel_number_dofs(ctx.h, ns, nterms, ncomp, mp, np_, ctypes.byref(nfree)))
+    for sp, nm in zip(spaces, nums):
+        sp.field.dofnums = nm
+    return nfree.value
 
 
 def assemble_heat(am, elit, qpit, kappa, Q):

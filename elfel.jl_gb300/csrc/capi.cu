@@ -4,6 +4,7 @@
 #include "integrate.cuh"
 #include "solve.cuh"
 #include "sysmat.cuh"
+#include "t6r.cuh"
 
 using namespace elfel;
 
@@ -408,11 +409,10 @@ static int upload_direct_rest(Ctx* c, const elfel_space& s, int sdim, DBuf<int32
   return ELFEL_OK;
 }
 
-extern "C" int elfel_fused_setup(elfel_sysmat* m, const elfel_fused_desc* d) {
-  CHECK_FREE(m);
-  Ctx* c = &m->h->c;
+// The checks of a fused descriptor shared by both set-ups (the element DOF
+// tables are checked where they are read).
+static int check_fused_desc(Ctx* c, const elfel_fused_desc* d) {
   if (!d) return fail(c, ELFEL_ERR_ARG, "fused_setup: NULL descriptor");
-  cudaSetDevice(c->device);
   if (d->ndofs < 0) return fail(c, ELFEL_ERR_ARG, "fused_setup: negative ndofs");
   const elfel_space& u = d->u;
   const int sdim = d->sdim ? d->sdim : 2;
@@ -443,12 +443,19 @@ extern "C" int elfel_fused_setup(elfel_sysmat* m, const elfel_fused_desc* d) {
   } else if (d->physics != ELFEL_HEAT && d->physics != ELFEL_ELASTICITY) {
     return fail(c, ELFEL_ERR_ARG, "fused_setup: unknown physics %d", d->physics);
   }
+  return ELFEL_OK;
+}
+
+// Releases the system's buffers and records the descriptor's sizes and tables.
+static int init_fused(elfel_sysmat* m, const elfel_fused_desc* d) {
+  Ctx* c = &m->h->c;
+  const elfel_space& u = d->u;
   release_all(m);
   Fused& F = m->F;
   F.physics = d->physics;
   F.npts = d->npts;
   F.shape = d->shape;
-  F.sdim = sdim;
+  F.sdim = d->sdim ? d->sdim : 2;
   F.nn_u = u.nodes_per_elem;
   F.ncomp_u = u.ncomp;
   F.nel = u.nel;
@@ -457,11 +464,23 @@ extern "C" int elfel_fused_setup(elfel_sysmat* m, const elfel_fused_desc* d) {
     ELFEL_TRY(make_tables(u.nodes_per_elem, d->npts, d->qp_coords, d->qp_weights, &F.tab));
   else
     ELFEL_TRY(make_shape_tables(F.shape, d->npts, d->qp_coords, d->qp_weights, &F.stab));
-  const bool stokes = d->physics == ELFEL_STOKES;
-  if (stokes) {
+  if (d->physics == ELFEL_STOKES) {
     F.nn_p = 3;
     F.nnodes_p = d->p.nnodes;
   }
+  return ELFEL_OK;
+}
+
+extern "C" int elfel_fused_setup(elfel_sysmat* m, const elfel_fused_desc* d) {
+  CHECK_FREE(m);
+  Ctx* c = &m->h->c;
+  cudaSetDevice(c->device);
+  ELFEL_TRY(check_fused_desc(c, d));
+  const elfel_space& u = d->u;
+  const int sdim = d->sdim ? d->sdim : 2;
+  ELFEL_TRY(init_fused(m, d));
+  Fused& F = m->F;
+  const bool stokes = d->physics == ELFEL_STOKES;
   if (!tables_readable(c, u) || (stokes && !tables_readable(c, d->p))) {
     ELFEL_TRY(upload_space(c, u, d->ndofs, sdim, &F.conn_u, &F.xy_u, &F.dofs_u, "primary"));
     if (stokes) ELFEL_TRY(upload_space(c, d->p, d->ndofs, 2, &F.conn_p, nullptr, &F.dofs_p, "pressure"));
@@ -626,6 +645,117 @@ extern "C" int elfel_fused_setup_block(elfel_sysmat* m, const elfel_block_desc* 
   return ELFEL_OK;
 }
 
+extern "C" int elfel_number_dofs(elfel_ctx* h, int32_t nspaces, const int64_t* nterms, const int32_t* ncomp,
+                                 const uint8_t* const* isdatum, int64_t* const* dofnums, int64_t* nfree) {
+  if (!h) return ELFEL_ERR_ARG;
+  Ctx* c = &h->c;
+  if (nspaces < 1 || nspaces > 64 || !nterms || !ncomp || !isdatum)
+    return fail(c, ELFEL_ERR_ARG, "number_dofs: %d spaces", (int)nspaces);
+  cudaSetDevice(c->device);
+  std::vector<int64_t> n(nspaces);
+  int64_t total = 0;
+  for (int s = 0; s < nspaces; ++s) {
+    if (nterms[s] < 0 || ncomp[s] < 1 || (nterms[s] > 0 && !isdatum[s]))
+      return fail(c, ELFEL_ERR_ARG, "number_dofs: space %d: %lld terms of %d components", s, (long long)nterms[s],
+                  (int)ncomp[s]);
+    n[s] = nterms[s] * ncomp[s];
+    total += n[s];
+  }
+  if (total >= 0x7fffffff) return fail(c, ELFEL_ERR_ARG, "number_dofs: %lld DOFs (at most 2^31 - 1)", (long long)total);
+  std::vector<DBuf<uint8_t>> mk(nspaces);
+  std::vector<DBuf<int32_t>> nm(nspaces);
+  auto run = [&]() -> int {
+    std::vector<const uint8_t*> masks(nspaces);
+    std::vector<int32_t*> nums(nspaces);
+    for (int s = 0; s < nspaces; ++s) {
+      ELFEL_TRY(mk[s].alloc(c, (size_t)(n[s] > 0 ? n[s] : 1)));
+      ELFEL_TRY(nm[s].alloc(c, (size_t)(n[s] > 0 ? n[s] : 1)));
+      if (n[s]) ELFEL_CUDA(c, cudaMemcpyAsync(mk[s].p, isdatum[s], n[s], cudaMemcpyHostToDevice, c->stream));
+      masks[s] = mk[s].p;
+      nums[s] = nm[s].p;
+    }
+    ELFEL_TRY(number_spaces(c, nspaces, masks.data(), n.data(), nums.data(), nfree));
+    for (int s = 0; s < nspaces; ++s)
+      if (dofnums && dofnums[s]) ELFEL_TRY(numbers_to_host(c, nm[s].p, n[s], dofnums[s]));
+    return ELFEL_OK;
+  };
+  const int rc = run();
+  for (int s = 0; s < nspaces; ++s) {
+    mk[s].release(c);
+    nm[s].release(c);
+  }
+  return rc;
+}
+
+extern "C" int elfel_fused_setup_numbered(elfel_sysmat* m, const elfel_fused_desc* d, const uint8_t* isdatum_u,
+                                          const uint8_t* isdatum_p, int64_t* dofnums_u, int64_t* dofnums_p,
+                                          int64_t* nfree) {
+  CHECK_FREE(m);
+  Ctx* c = &m->h->c;
+  cudaSetDevice(c->device);
+  ELFEL_TRY(check_fused_desc(c, d));
+  const bool stokes = d->physics == ELFEL_STOKES;
+  const elfel_space& u = d->u;
+  const int sdim = d->sdim ? d->sdim : 2;
+  const int64_t nu_terms = u.nnodes * u.ncomp, np_terms = stokes ? d->p.nnodes : 0;
+  if (!isdatum_u || (stokes && !isdatum_p))
+    return fail(c, ELFEL_ERR_ARG, "fused_setup_numbered: NULL essential-BC mask");
+  if (u.nel < 0 || u.nnodes < 0 || !u.conn || (u.nnodes > 0 && !u.xy) || (stokes && !d->p.conn))
+    return fail(c, ELFEL_ERR_ARG, "fused_setup_numbered: missing connectivity or coordinates");
+  if (d->ndofs != nu_terms + np_terms)
+    return fail(c, ELFEL_ERR_ARG, "fused_setup_numbered: ndofs %lld, the spaces hold %lld DOFs",
+                (long long)d->ndofs, (long long)(nu_terms + np_terms));
+  ELFEL_TRY(init_fused(m, d));
+  Fused& F = m->F;
+  DBuf<uint8_t> mu, mp;
+  DBuf<int32_t> nu_, np_;
+  auto run = [&]() -> int {
+    ELFEL_TRY(to_index32(c, u.conn, u.nel * u.nodes_per_elem, u.nnodes, &F.conn_u, "primary connectivity"));
+    ELFEL_TRY(F.xy_u.alloc(c, (size_t)(u.nnodes > 0 ? sdim * u.nnodes : 1)));
+    if (u.nnodes)
+      ELFEL_CUDA(c, cudaMemcpyAsync(F.xy_u.p, u.xy, sizeof(double) * sdim * u.nnodes, cudaMemcpyHostToDevice,
+                                    c->stream));
+    if (stokes)
+      ELFEL_TRY(to_index32(c, d->p.conn, d->p.nel * 3, d->p.nnodes, &F.conn_p, "pressure connectivity"));
+    ELFEL_TRY(mu.alloc(c, (size_t)(nu_terms > 0 ? nu_terms : 1)));
+    ELFEL_TRY(nu_.alloc(c, (size_t)(nu_terms > 0 ? nu_terms : 1)));
+    if (nu_terms)
+      ELFEL_CUDA(c, cudaMemcpyAsync(mu.p, isdatum_u, nu_terms, cudaMemcpyHostToDevice, c->stream));
+    if (stokes) {
+      ELFEL_TRY(mp.alloc(c, (size_t)(np_terms > 0 ? np_terms : 1)));
+      ELFEL_TRY(np_.alloc(c, (size_t)(np_terms > 0 ? np_terms : 1)));
+      if (np_terms)
+        ELFEL_CUDA(c, cudaMemcpyAsync(mp.p, isdatum_p, np_terms, cudaMemcpyHostToDevice, c->stream));
+    }
+    const uint8_t* masks[2] = {mu.p, mp.p};
+    const int64_t ns[2] = {nu_terms, np_terms};
+    int32_t* nums[2] = {nu_.p, np_.p};
+    int64_t nf = 0;
+    ELFEL_TRY(number_spaces(c, stokes ? 2 : 1, masks, ns, nums, &nf));
+    const int nedof_u = u.nodes_per_elem * u.ncomp;
+    ELFEL_TRY(F.dofs_u.alloc(c, (size_t)(u.nel * nedof_u > 0 ? u.nel * nedof_u : 1)));
+    ELFEL_TRY(element_dofs(c, F.conn_u.p, u.nel, u.nodes_per_elem, u.ncomp, nu_.p, F.dofs_u.p));
+    if (stokes) {
+      ELFEL_TRY(F.dofs_p.alloc(c, (size_t)(d->p.nel * 3 > 0 ? d->p.nel * 3 : 1)));
+      ELFEL_TRY(element_dofs(c, F.conn_p.p, d->p.nel, 3, 1, np_.p, F.dofs_p.p));
+    }
+    ELFEL_TRY(numbers_to_host(c, nu_.p, nu_terms, dofnums_u));
+    if (stokes) ELFEL_TRY(numbers_to_host(c, np_.p, np_terms, dofnums_p));
+    if (nfree) *nfree = nf;
+    return fused_build(m, d->ndofs);
+  };
+  const int rc = run();
+  mu.release(c);
+  mp.release(c);
+  nu_.release(c);
+  np_.release(c);
+  if (rc != ELFEL_OK) {
+    cudaStreamSynchronize(c->stream);
+    release_all(m);
+  }
+  return rc;
+}
+
 extern "C" int elfel_block_dirichlet(elfel_sysmat* m, const double* coef6, double* T) {
   CHECK_M(m);
   Ctx* c = &m->h->c;
@@ -656,6 +786,15 @@ extern "C" int elfel_fused_dims(elfel_sysmat* m, int64_t* nel, int64_t* nnodes, 
   if (nel) *nel = m->F.nel;
   if (nnodes) *nnodes = m->F.nnodes_u;
   if (ndofs) *ndofs = m->nrow;
+  return ELFEL_OK;
+}
+
+extern "C" int elfel_sysmat_tile_stats(elfel_sysmat* m, int64_t* ntiles, int64_t* nprograms, int64_t* nfallback) {
+  CHECK_M(m);
+  const TilePlan& T = m->P.tiles;
+  if (ntiles) *ntiles = T.built ? T.ntiles : 0;
+  if (nprograms) *nprograms = T.built ? T.nprograms : 0;
+  if (nfallback) *nfallback = T.built ? T.nfallback : 0;
   return ELFEL_OK;
 }
 
@@ -709,6 +848,39 @@ extern "C" int elfel_fused_heat(elfel_sysmat* m, const double* kappa, double Q) 
   if (kappa && F.nel)
     ELFEL_CUDA(c, cudaMemcpyAsync(F.coef.p, kappa, sizeof(double) * F.nel, cudaMemcpyHostToDevice, c->stream));
   const bool fdirect = F.shape == ELFEL_SHAPE_TRIANGLE && F.f_direct_ok && heat_f_direct(F.nn_u, F.ncurved, F.tab);
+  // From a pattern's second assembly on, an exact-rule straight-sided T6 mesh
+  // writes 8 bases per element and the tile reduction expands and sums them
+  // (the plan is built once, at that assembly); a pattern assembled once (an
+  // end-to-end call) keeps the records and the contributor-list reduction.
+  // Both give the same bits.
+  const bool tiles = c->tiles && F.shape == ELFEL_SHAPE_TRIANGLE && heat_bases_ok(F.nn_u, F.ncurved, F.tab) &&
+                     m->P.reductions >= 1 && m->P.nslots < 0x7fffffff;
+  if (tiles) {
+    if (!(m->P.tiles.built && m->P.tiles.V == kT6RTable && m->P.tiles.S == 21)) {
+      Phase ph(c, "tile_plan");
+      ELFEL_TRY(build_tile_plan(c, m->P, 21, kT6RTable, kT6REntry));
+    }
+    {
+      Phase ph(c, "integrate_heat");
+      if (fdirect) ELFEL_CUDA(c, cudaMemsetAsync(m->rhs.p, 0, sizeof(double) * m->ncol, c->stream));
+      ELFEL_TRY(launch_heat_bases(c, F.nel, F.conn_u.p, F.xy_u.p, F.coef.p, Q, F.tab, F.kstore.p, F.fstore.p,
+                                  fdirect ? F.dofs_u.p : nullptr, fdirect ? m->rhs.p : nullptr));
+    }
+    {
+      Phase ph(c, "reduce_K");
+      ELFEL_TRY(tile_reduce(c, m->P, F.kstore.p, 1, m->vals.p));
+    }
+    m->P.reductions++;
+    if (!fdirect) {
+      ELFEL_TRY(ensure_fpat(m));
+      Phase ph(c, "reduce_F");
+      ELFEL_TRY(reduce_dense(c, m->F.fpat, m->F.fstore.p, m->rhs.p));
+    }
+    m->has_rhs = 1;
+    m->finished = 1;
+    m->values_version++;
+    return ELFEL_OK;
+  }
   {
     Phase ph(c, "integrate_heat");
     if (fdirect) {

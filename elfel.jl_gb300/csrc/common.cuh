@@ -42,6 +42,8 @@ struct Ctx {
   // phase timing: CUDA events recorded on `stream` around each kernel launch
   int profiling = 0;
   std::vector<PhaseRec> phases;
+  // tile reduction of resident T6 heat patterns: on unless ELFEL_TILES=0
+  int tiles = 1;
   // autotuner: on unless ELFEL_TUNE=0; one line per tuned key
   int tune = 1;
   std::vector<std::string> tune_lines;

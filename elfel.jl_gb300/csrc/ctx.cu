@@ -233,6 +233,8 @@ extern "C" int elfel_ctx_create(int device, int64_t mem_budget_bytes, elfel_ctx*
   h->c.trace = (tr && tr[0] == '1') ? 1 : 0;
   const char* tu = getenv("ELFEL_TUNE");
   h->c.tune = (tu && tu[0] == '0') ? 0 : 1;
+  const char* ti = getenv("ELFEL_TILES");
+  h->c.tiles = (ti && ti[0] == '0') ? 0 : 1;
   *out = h;
   return ELFEL_OK;
 }

@@ -25,6 +25,7 @@
 // the per-quadrature-point path, which mirrors the reference loop.
 #include "integrate.cuh"
 #include "floatpair.cuh"
+#include "t6r.cuh"
 
 namespace elfel {
 
@@ -298,27 +299,6 @@ int heat_pattern(int nn, const QPTab& t) {
   return kPatT6R;
 }
 
-// The exact-rational T6 record is determined by 8 base values: the stored K
-// entries k0..k5, k9 (= k14 = k20) and the load at the midside nodes; every
-// other entry is one of them times -4 or -8, or zero (t6r_expand).
-// t6r_scale: code 0: b; 1: -4 b; 2: -8 b; 3: +0, by integer operations only:
-// normal values are scaled exactly by an exponent add; a result above the
-// double range is the infinity of its sign, infinities and NaNs keep their
-// exponent, and subnormal values (below 2^-1022, negligible next to any entry
-// of an element record) become zero of their sign.
-__device__ __forceinline__ double t6r_scale(double b, int code) {
-  const long long bits = __double_as_longlong(b) ^ (long long)(1ull << 63);  // -b
-  const long long sign = bits & (long long)(1ull << 63);
-  const int ex = (int)((bits >> 52) & 0x7ff);
-  const int m = code == 1 ? 2 : 3;
-  long long r = bits + ((long long)m << 52);
-  r = ex == 0 ? sign : r;                                                        // zero or subnormal
-  r = ex == 0x7ff ? bits : r;                                                    // inf, NaN
-  r = (ex != 0 && ex != 0x7ff && ex + m > 2046) ? (sign | 0x7ff0000000000000LL) : r;  // overflow
-  const double scaled = __longlong_as_double(r);
-  return code == 0 ? b : (code == 3 ? 0.0 : scaled);
-}
-
 // The 8 bases in FP64: the fallback of t6r_bases_pair for elements outside
 // its accuracy range.
 __device__ __forceinline__ void t6r_bases_fp64(double J11, double J12, double J21, double J22, double kap, double Q,
@@ -553,7 +533,11 @@ __device__ __forceinline__ void heat_elems(int64_t e0, int64_t nel, const int32_
 // more than two elements.  An IEEE sum of at most two terms onto +0 does not
 // depend on their order ((0 + a) + b == (0 + b) + a, signed zeros included),
 // so the atomic additions give the bits of the in-order vector assembly.
-template <int PAT, bool FDIRECT = false>
+//
+// BASES (exact-rule form only): the 8 bases of each element are written as
+// one 64-byte record (kstore: nel x 8) instead of the 21 K values; the tile
+// reduction (tiles.cu) expands them to the same values, bit for bit.
+template <int PAT, bool FDIRECT = false, bool BASES = false>
 __global__ void __launch_bounds__(kIntThreads) heat_t6s_k(int64_t nel, const int32_t* __restrict__ conn,
                                                          const double2* __restrict__ xy,
                                                          const double* __restrict__ kappa, double Q,
@@ -587,6 +571,33 @@ __global__ void __launch_bounds__(kIntThreads) heat_t6s_k(int64_t nel, const int
                 Q, tab.P[3], bs);
     }
     double* a = acc + t;
+    if (BASES) {
+      if (e < nel) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k * LD] = bs[k];
+      }
+      write_records_fixed<NT, 8, 8>(acc, 0, e0, nel, kstore);
+      if (FDIRECT) {
+        if (e < nel) {
+          const int32_t* d = dofs + e * NN;
+          atomicAdd(fglob + __ldg(d + 3), bs[7]);
+          atomicAdd(fglob + __ldg(d + 4), bs[7]);
+          atomicAdd(fglob + __ldg(d + 5), bs[7]);
+        }
+        return;
+      }
+      __syncthreads();
+      if (e < nel) {
+        a[0 * LD] = 0.0;
+        a[1 * LD] = 0.0;
+        a[2 * LD] = 0.0;
+        a[3 * LD] = bs[7];
+        a[4 * LD] = bs[7];
+        a[5 * LD] = bs[7];
+      }
+      write_records_part<NT>(acc, NN, 0, NN, e0, nel, fstore);
+      return;
+    }
     if (e < nel) {
       const double m1 = t6r_scale(bs[1], 1);
       a[0 * LD] = bs[0];
@@ -675,6 +686,27 @@ __global__ void __launch_bounds__(NT) heat_batch_k(const HeatJob* __restrict__ j
 }
 
 static size_t heat_smem(int nn, int nt) { return (size_t)(nn == 3 ? 6 + 3 : 21 + 6) * (nt + 1) * sizeof(double); }
+
+bool heat_bases_ok(int nn, int64_t ncurved, const QPTab& tab) {
+  return nn == 6 && ncurved == 0 && heat_pattern(6, tab) == kPatT6R;
+}
+
+int launch_heat_bases(Ctx* c, int64_t nel, const int32_t* conn, const double* xy, const double* kappa, double Q,
+                      const QPTab& tab, double* bases, double* fstore, const int32_t* dofs, double* fglob) {
+  if (nel == 0) return ELFEL_OK;
+  const unsigned grid = grid_for(nel, kIntThreads);
+  const size_t sm = 11 * (kIntThreads + 1) * sizeof(double);
+  if (fglob) {
+    if (!dofs) return fail(c, ELFEL_ERR_STATE, "heat: direct load-vector assembly needs the DOF table");
+    heat_t6s_k<kPatT6R, true, true><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, (const double2*)xy, kappa, Q,
+                                                                           tab, bases, fstore, dofs, fglob);
+  } else {
+    heat_t6s_k<kPatT6R, false, true><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, (const double2*)xy, kappa, Q,
+                                                                            tab, bases, fstore);
+  }
+  ELFEL_LAUNCH_CHECK(c);
+  return ELFEL_OK;
+}
 
 bool heat_f_direct(int nn, int64_t ncurved, const QPTab& tab) {
   return nn == 6 && ncurved == 0 && heat_pattern(6, tab) == kPatT6R;

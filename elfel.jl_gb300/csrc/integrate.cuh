@@ -41,6 +41,14 @@ int make_tables(int nn, int npts, const double* pc, const double* w, QPTab* t);
 int launch_heat(Ctx* c, int nn, int64_t nel, const int32_t* conn, const double* xy, const double* kappa, double Q,
                 const uint8_t* straight, int64_t ncurved, const QPTab& tab, double* kstore, double* fstore,
                 const int32_t* dofs = nullptr, double* fglob = nullptr);
+// True when every element of a T6 mesh takes the exact-rule straight-sided
+// form, whose K record is determined by 8 bases (t6r_bases).
+bool heat_bases_ok(int nn, int64_t ncurved, const QPTab& tab);
+// The T6 heat integration writing the 8 bases per element (bases: nel x 8)
+// instead of the 21-entry K records; the load vector as in launch_heat.
+int launch_heat_bases(Ctx* c, int64_t nel, const int32_t* conn, const double* xy, const double* kappa, double Q,
+                      const QPTab& tab, double* bases, double* fstore, const int32_t* dofs = nullptr,
+                      double* fglob = nullptr);
 // True when the heat load vector of a T6 mesh takes the exact form (zero at
 // the vertices, Q det / 6 at the midside nodes) in the straight-only kernel.
 bool heat_f_direct(int nn, int64_t ncurved, const QPTab& tab);

@@ -180,6 +180,42 @@ __device__ __forceinline__ void slot_rc(const SlotGen& g, int64_t s, int32_t& r,
 // 32 lanes, the window's nonzeros taken in order of their contributor count.
 constexpr int kReduceWindow = 128;
 
+// Tile reduction plan of a pattern (tiles.cu).
+constexpr int kTileThreads = 256;
+constexpr int kTileMaxNz = 2048;       // nonzeros of a tile
+constexpr int kTileMaxContrib = 4096;  // contributions of a tile
+constexpr int kTileMaxCols = 256;      // columns of a tile
+constexpr int kTileMaxClass = 15;      // contributions of one nonzero (more: the tile takes the slow path)
+constexpr int kTileMaxEl = 320;        // distinct elements of a tile
+constexpr int kTileMaxS = 128;         // stored values per element record
+constexpr int kTileTableBytes = 40960; // shared memory for the tile's value table
+constexpr int kTileFallback = 1, kTileSplit = 2, kTileEmpty = 4;
+
+struct TileHdr {
+  int64_t p0;       // first nonzero of the tile (CSC position)
+  int64_t q0;       // first contribution (cptr[p0])
+  int32_t col0, ncols;
+  int32_t nz, nc;   // nonzeros, contributions
+  int32_t nel;      // distinct elements
+  int32_t maxcnt;   // largest contributor count
+  int32_t emin;     // smallest element
+  int32_t flags;    // kTileFallback: summed from the contributor lists; kTileEmpty: no nonzero
+  int32_t prog;     // tile whose program this tile reads
+  int32_t pad;
+};
+
+struct TilePlan {
+  int built = 0;
+  int S = 0, V = 0, emax = 0;  // record entries, value-table entries per element, elements per tile
+  int64_t ntiles = 0, nprograms = 0, nfallback = 0;
+  DBuf<TileHdr> hdr;
+  DBuf<int32_t> elist;    // ntiles x emax: element - emin, ascending
+  DBuf<uint16_t> cls;     // ntiles x (kTileMaxClass + 2): first nonzero (count order) of each count
+  DBuf<uint32_t> firsts;  // nnz, count order within each tile: position << 16 | table index
+  DBuf<uint16_t> rest;    // nslots - nnz: table indices of the further contributions
+  void release(Ctx* c);
+};
+
 // CSC pattern with the contributor lists of each nonzero.
 struct Pattern {
   int64_t nrow = 0, ncol = 0, nnz = 0, nslots = 0;
@@ -189,7 +225,9 @@ struct Pattern {
   DBuf<int32_t> contrib;  // nslots: storage index of each contribution, ascending slot order
   DBuf<uint8_t> perm;     // per window of kReduceWindow nonzeros: their order by contributor count
   int reductions = 0;     // value reductions run on this pattern (perm is built for the second)
+  TilePlan tiles;         // built on request (build_tile_plan)
   void release(Ctx* c) {
+    tiles.release(c);
     colptr.release(c);
     rowval.release(c);
     cptr.release(c);
@@ -207,6 +245,14 @@ int build_pattern(Ctx* c, const SlotGen& g, int64_t nrow, int64_t ncol, Pattern*
 int reduce_values(Ctx* c, Pattern& P, const double* store, double* vals_out);
 // Dense vector of a 1 x n pattern (the rhs): out[c] = contributions of column c.
 int reduce_dense(Ctx* c, const Pattern& P, const double* store, double* out);
+
+// The tile plan of P for element records of S stored values; map[s] (NULL:
+// identity) is the value-table index of stored entry s, V the table size.
+int build_tile_plan(Ctx* c, Pattern& P, int S, int V, const uint8_t* map);
+// vals = the K values of P from element records (src: nel x S doubles), or,
+// with t6r_bases, from the 8 bases per element of the exact-rational T6
+// heat record; the same bits as reduce_values.
+int tile_reduce(Ctx* c, const Pattern& P, const double* src, int t6r_bases, double* vals);
 
 // One reduction of a batched launch (device array ordered by blk0).
 constexpr int kRedJobThreads = 256;
@@ -302,6 +348,16 @@ int fused_build(elfel_sysmat* m, int64_t ndofs);
 // Builds the right-hand side's pattern (F.fgen) if it is not built yet; only
 // assemblies that reduce load records need it.
 int ensure_fpat(elfel_sysmat* m);
+
+// numberdofs! of ns spaces on the device (numbering.cu): mask[s] (n[s]
+// entries, term-major / component-minor, nonzero = data DOF) -> num0[s], the
+// 0-based DOF numbers; *nfree = the free DOFs of all spaces.
+int number_spaces(Ctx* c, int ns, const uint8_t* const* mask, const int64_t* n, int32_t* const* num0,
+                  int64_t* nfree);
+// dofs (nel x nn*ncomp, node-major / component-minor) = num0 of each node of conn.
+int element_dofs(Ctx* c, const int32_t* conn, int64_t nel, int nn, int ncomp, const int32_t* num0, int32_t* dofs);
+// host[0..n) = num0 + 1 (int64).
+int numbers_to_host(Ctx* c, const int32_t* num0, int64_t n, int64_t* host);
 
 // Device tables of a block mesh of the rectangle [0,lx] x [0,ly]: nodes,
 // connectivity and the DOFs of a scalar field fixed on the whole boundary

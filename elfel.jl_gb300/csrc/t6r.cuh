@@ -1,0 +1,56 @@
+// The exact-rational T6 heat record (straight-sided elements, quadrature
+// rules exact for the gradient products): the 21 stored K entries of an
+// element are b0..b6 (its 7 K bases), -4 or -8 times b1, b3, b4, or zero.
+// Shared by the integration kernels, which write records or bases, and the
+// tile reduction, which expands bases; both use t6r_scale, so the values
+// agree bit for bit.
+#pragma once
+#include <stdint.h>
+
+namespace elfel {
+
+// The exact-rational T6 record is determined by 8 base values: the stored K
+// entries k0..k5, k9 (= k14 = k20) and the load at the midside nodes; every
+// other entry is one of them times -4 or -8, or zero (t6r_expand).
+// t6r_scale: code 0: b; 1: -4 b; 2: -8 b; 3: +0, by integer operations only:
+// normal values are scaled exactly by an exponent add; a result above the
+// double range is the infinity of its sign, infinities and NaNs keep their
+// exponent, and subnormal values (below 2^-1022, negligible next to any entry
+// of an element record) become zero of their sign.
+__device__ __forceinline__ double t6r_scale(double b, int code) {
+  const long long bits = __double_as_longlong(b) ^ (long long)(1ull << 63);  // -b
+  const long long sign = bits & (long long)(1ull << 63);
+  const int ex = (int)((bits >> 52) & 0x7ff);
+  const int m = code == 1 ? 2 : 3;
+  long long r = bits + ((long long)m << 52);
+  r = ex == 0 ? sign : r;                                                        // zero or subnormal
+  r = ex == 0x7ff ? bits : r;                                                    // inf, NaN
+  r = (ex != 0 && ex != 0x7ff && ex + m > 2046) ? (sign | 0x7ff0000000000000LL) : r;  // overflow
+  const double scaled = __longlong_as_double(r);
+  return code == 0 ? b : (code == 3 ? 0.0 : scaled);
+}
+
+// Value table of one element for the tile reduction: v[0..6] = b0..b6,
+// v[7] = +0, v[8..10] = -4 b1, -4 b3, -4 b4, v[11..13] = -8 b1, -8 b3, -8 b4.
+constexpr int kT6RTable = 14;
+// Stored K entry k (0..20, column-packed upper triangle) -> its table index.
+constexpr uint8_t kT6REntry[21] = {0, 1, 2, 3, 4, 5, 8, 8, 7, 6, 7, 10, 10, 12, 6, 9, 7, 9, 13, 11, 6};
+
+// kT6REntry[s] in device code: 4-bit fields of two packed words.
+__device__ __forceinline__ int t6r_entry(int s) {
+  return s < 16 ? (int)((0x96caa76788543210ull >> (4 * s)) & 15u) : (int)((0x6bd97u >> (4 * (s - 16))) & 15u);
+}
+
+__device__ __forceinline__ void t6r_table(const double* b, double* v) {
+#pragma unroll
+  for (int k = 0; k < 7; ++k) v[k] = b[k];
+  v[7] = 0.0;
+  v[8] = t6r_scale(b[1], 1);
+  v[9] = t6r_scale(b[3], 1);
+  v[10] = t6r_scale(b[4], 1);
+  v[11] = t6r_scale(b[1], 2);
+  v[12] = t6r_scale(b[3], 2);
+  v[13] = t6r_scale(b[4], 2);
+}
+
+}  // namespace elfel

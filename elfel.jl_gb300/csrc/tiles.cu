@@ -1,0 +1,554 @@
+// Tile reduction of the K values: the element contributions of a resident
+// pattern summed without the per-contribution index lists of reduce_win_k.
+//
+// The columns of the CSC pattern are cut into tiles (consecutive columns, at
+// most kTileMaxNz nonzeros and kTileMaxContrib contributions each).  For each
+// tile a program is built once per pattern:
+//   - the distinct elements contributing to the tile, as offsets from the
+//     tile's smallest element;
+//   - the tile's nonzeros in order of their contributor count (a stable
+//     counting sort), so that the lanes of a warp issue about as many FP64
+//     adds as their nonzeros need;
+//   - per nonzero its first code (its position in the tile << 16 | the index
+//     of its first contribution in the tile's value table), and its further
+//     codes, stored count class by count class, contribution-major, so that
+//     each round of a warp reads consecutive codes.
+// A value table holds V values per element of the tile: the element's K
+// record (V = S), or for the exact-rational T6 heat record the 14 values its
+// 8 bases expand to (t6r_table).  Every nonzero adds its contributions in
+// slot order -- the order of the contributor lists of the pattern, which is
+// the order in which SparseArrays.sparse adds duplicates -- so the values are
+// the bits of reduce_values.
+//
+// Tiles whose programs are equal word for word (the tiles of a structured
+// mesh away from its boundary are translates of a few) share one copy of the
+// program: per step a tile reads its own first nonzero and smallest element
+// and the program of its representative, which stays in L2.
+#include <algorithm>
+#include <unordered_map>
+#include <vector>
+
+#include "sysmat.cuh"
+#include "t6r.cuh"
+
+namespace elfel {
+
+namespace {
+
+constexpr int kTT = kTileThreads;
+
+struct TileBuildArgs {
+  const int64_t* colptr;
+  const int32_t* cptr;
+  const int32_t* contrib;
+  int S, V;
+  FastDiv sdiv;
+  uint8_t map[kTileMaxS];
+  int emax;
+};
+
+// cq[k] = cptr[colptr[k]]: the first contribution of each column (k <= ncol).
+__global__ void cptr_at_cols_k(const int64_t* __restrict__ colptr, const int32_t* __restrict__ cptr, int64_t ncol,
+                               int32_t* __restrict__ cq) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k <= ncol; k += (int64_t)gridDim.x * blockDim.x)
+    cq[k] = cptr[colptr[k]];
+}
+
+// Sort n <= kTileMaxContrib ints in shared memory ascending (bitonic network
+// over the next power of two, padded with INT32_MAX).
+__device__ void smem_sort(int32_t* a, int n) {
+  int np = 1;
+  while (np < n) np <<= 1;
+  for (int i = n + threadIdx.x; i < np; i += blockDim.x) a[i] = 0x7fffffff;
+  __syncthreads();
+  for (int size = 2; size <= np; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = threadIdx.x; i < np / 2; i += blockDim.x) {
+        const int lo = 2 * i - (i & (stride - 1));
+        const int hi = lo + stride;
+        const bool up = (lo & size) == 0;
+        const int32_t x = a[lo], y = a[hi];
+        if ((x > y) == up) {
+          a[lo] = y;
+          a[hi] = x;
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// First pass: the size of each tile (nonzeros, contributions, distinct
+// elements, largest contributor count); tiles beyond the limits are marked.
+__global__ void __launch_bounds__(kTT) tile_count_k(TileHdr* __restrict__ hdr, int64_t ntiles, TileBuildArgs a) {
+  __shared__ int32_t el[kTileMaxContrib];
+  __shared__ int red[2];
+  const int64_t t = blockIdx.x;
+  if (t >= ntiles) return;
+  TileHdr H = hdr[t];
+  const int64_t p0 = a.colptr[H.col0], p1 = a.colptr[H.col0 + H.ncols];
+  const int64_t q0 = a.cptr[p0], q1 = a.cptr[p1];
+  H.p0 = p0;
+  H.q0 = q0;
+  H.nz = (int32_t)(p1 - p0);
+  H.nc = (int32_t)(q1 - q0);
+  if (H.nz > kTileMaxNz || H.nc > kTileMaxContrib || H.nz == 0) {
+    if (threadIdx.x == 0) {
+      H.flags = H.nz == 0 ? kTileEmpty : kTileFallback;
+      H.nel = 0;
+      H.maxcnt = 0;
+      hdr[t] = H;
+    }
+    return;
+  }
+  if (threadIdx.x == 0) red[0] = red[1] = 0;
+  for (int i = threadIdx.x; i < H.nc; i += kTT) el[i] = (int32_t)a.sdiv.div((uint32_t)a.contrib[q0 + i]);
+  int mx = 0;
+  for (int i = threadIdx.x; i < H.nz; i += kTT) mx = max(mx, a.cptr[p0 + i + 1] - a.cptr[p0 + i]);
+  smem_sort(el, H.nc);  // contains __syncthreads
+  int nuniq = 0;
+  for (int i = threadIdx.x; i < H.nc; i += kTT) nuniq += (i == 0 || el[i] != el[i - 1]) ? 1 : 0;
+  atomicAdd(&red[0], nuniq);
+  atomicMax(&red[1], mx);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    H.nel = red[0];
+    H.maxcnt = red[1];
+    H.emin = el[0];
+    H.flags = (red[0] > a.emax || red[1] > kTileMaxClass) ? kTileSplit : 0;
+    hdr[t] = H;
+  }
+}
+
+// Second pass: the program of every tile within the limits.
+__global__ void __launch_bounds__(kTT) tile_build_k(TileHdr* __restrict__ hdr, int64_t ntiles, TileBuildArgs a,
+                                                    int32_t* __restrict__ elist, uint16_t* __restrict__ cls,
+                                                    uint32_t* __restrict__ firsts, uint16_t* __restrict__ rest) {
+  __shared__ int32_t el[kTileMaxContrib];
+  __shared__ uint8_t cnt[kTileMaxNz];
+  __shared__ uint16_t sidx[kTileMaxNz];
+  __shared__ int cstart[kTileMaxClass + 2], rbase[kTileMaxClass + 2];
+  __shared__ int nuniq;
+  __shared__ int wsum[kTT / 32];
+  const int64_t t = blockIdx.x;
+  if (t >= ntiles) return;
+  const TileHdr H = hdr[t];
+  if (H.flags) return;
+  const int64_t p0 = H.p0, q0 = H.q0;
+  const int nz = H.nz, nc = H.nc;
+  for (int i = threadIdx.x; i < nc; i += kTT) el[i] = (int32_t)a.sdiv.div((uint32_t)a.contrib[q0 + i]);
+  for (int i = threadIdx.x; i < nz; i += kTT) cnt[i] = (uint8_t)(a.cptr[p0 + i + 1] - a.cptr[p0 + i]);
+  if (threadIdx.x < kTileMaxClass + 2) cstart[threadIdx.x] = 0;
+  smem_sort(el, nc);
+  // distinct elements, compacted in place by one warp (ordered ballots)
+  if (threadIdx.x < 32) {
+    int w = 0;
+    for (int base = 0; base < nc; base += 32) {
+      const int i = base + threadIdx.x;
+      const bool keep = i < nc && (i == 0 || el[i] != el[i - 1]);
+      const int32_t v = i < nc ? el[i] : 0;
+      const unsigned m = __ballot_sync(0xffffffffu, keep);
+      __syncwarp();
+      if (keep) el[w + __popc(m & ((1u << threadIdx.x) - 1))] = v;
+      w += __popc(m);
+      __syncwarp();
+    }
+    if (threadIdx.x == 0) nuniq = w;
+  }
+  __syncthreads();
+  const int nel = nuniq;
+  const int32_t emin = el[0];
+  for (int k = threadIdx.x; k < nel; k += kTT) elist[t * (int64_t)a.emax + k] = el[k] - emin;
+  // count classes and the stable order within each class
+  for (int i = threadIdx.x; i < nz; i += kTT) atomicAdd(&cstart[cnt[i] + 1], 1);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int run = 0, rb = 0;
+    for (int c = 1; c <= kTileMaxClass + 1; ++c) {
+      const int n = c <= kTileMaxClass ? cstart[c + 1] : 0;
+      cstart[c] = run;
+      rbase[c] = rb;
+      run += n;
+      rb += n * (c - 1);
+    }
+    cstart[0] = 0;
+  }
+  __syncthreads();
+  for (int c = 1; c <= kTileMaxClass; ++c) {
+    int before = cstart[c];
+    for (int base = 0; base < nz; base += kTT) {
+      const int i = base + threadIdx.x;
+      const bool in = i < nz && cnt[i] == c;
+      const unsigned m = __ballot_sync(0xffffffffu, in);
+      const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+      if (lane == 0) wsum[wid] = __popc(m);
+      __syncthreads();
+      int off = before;
+      for (int w = 0; w < wid; ++w) off += wsum[w];
+      if (in) sidx[i] = (uint16_t)(off + __popc(m & ((1u << lane) - 1)));
+      int tot = 0;
+      for (int w = 0; w < kTT / 32; ++w) tot += wsum[w];
+      __syncthreads();
+      before += tot;
+    }
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < kTileMaxClass + 2; k += kTT)
+    cls[t * (kTileMaxClass + 2) + k] = (uint16_t)(k == kTileMaxClass + 1 ? nz : cstart[k]);
+  // codes: table index of every contribution
+  for (int i = threadIdx.x; i < nz; i += kTT) {
+    const int c = cnt[i];
+    const int si = sidx[i];
+    const int nclass = cstart[c + 1] - cstart[c];
+    const int32_t b = a.cptr[p0 + i];
+    for (int k = 0; k < c; ++k) {
+      const uint32_t st = (uint32_t)a.contrib[b + k];
+      const uint32_t e = a.sdiv.div(st);
+      const int s = (int)(st - e * (uint32_t)a.S);
+      int lo = 0, hi = nel - 1;  // e's index in the distinct list
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (el[mid] < (int32_t)e) lo = mid + 1; else hi = mid;
+      }
+      const uint32_t code = (uint32_t)(lo * a.V + a.map[s]);
+      if (k == 0)
+        firsts[p0 + si] = ((uint32_t)i << 16) | code;
+      else
+        rest[(q0 - p0) + rbase[c] + (k - 1) * nclass + (si - cstart[c])] = (uint16_t)code;
+    }
+  }
+  if (threadIdx.x == 0) {
+    TileHdr h = H;
+    h.emin = emin;
+    h.nel = nel;
+    hdr[t] = h;
+  }
+}
+
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {
+  x ^= x >> 30;
+  x *= 0xbf58476d1ce4e5b9ull;
+  x ^= x >> 27;
+  x *= 0x94d049bb133111ebull;
+  x ^= x >> 31;
+  return x;
+}
+
+// A 64-bit digest of each program: a sum of mixed (word, index) pairs, so
+// that it does not depend on the order threads add them.
+__global__ void __launch_bounds__(kTT) tile_hash_k(const TileHdr* __restrict__ hdr, int64_t ntiles, int emax,
+                                                   const int32_t* __restrict__ elist, const uint16_t* __restrict__ cls,
+                                                   const uint32_t* __restrict__ firsts,
+                                                   const uint16_t* __restrict__ rest, uint64_t* __restrict__ hash) {
+  __shared__ unsigned long long part;
+  const int64_t t = blockIdx.x;
+  if (t >= ntiles) return;
+  const TileHdr H = hdr[t];
+  if (H.flags) {
+    if (threadIdx.x == 0) hash[t] = 0;
+    return;
+  }
+  if (threadIdx.x == 0) part = 0;
+  __syncthreads();
+  uint64_t h = 0;
+  for (int k = threadIdx.x; k < H.nel; k += kTT) h += mix64(((uint64_t)1 << 60) + ((uint64_t)k << 32) + (uint32_t)elist[t * (int64_t)emax + k]);
+  for (int k = threadIdx.x; k < kTileMaxClass + 2; k += kTT)
+    h += mix64(((uint64_t)2 << 60) + ((uint64_t)k << 32) + cls[t * (kTileMaxClass + 2) + k]);
+  for (int k = threadIdx.x; k < H.nz; k += kTT) h += mix64(((uint64_t)3 << 60) + ((uint64_t)k << 32) + firsts[H.p0 + k]);
+  for (int k = threadIdx.x; k < H.nc - H.nz; k += kTT)
+    h += mix64(((uint64_t)4 << 60) + ((uint64_t)k << 32) + rest[(H.q0 - H.p0) + k]);
+  atomicAdd(&part, (unsigned long long)h);
+  __syncthreads();
+  if (threadIdx.x == 0) hash[t] = mix64(part ^ ((uint64_t)H.nz << 40) ^ ((uint64_t)H.nc << 20) ^ (uint64_t)H.nel);
+}
+
+// A tile keeps its representative's program only if the two are equal word
+// for word; otherwise it reads its own.
+__global__ void __launch_bounds__(kTT) tile_verify_k(TileHdr* __restrict__ hdr, int64_t ntiles, int emax,
+                                                     const int32_t* __restrict__ elist, const uint16_t* __restrict__ cls,
+                                                     const uint32_t* __restrict__ firsts,
+                                                     const uint16_t* __restrict__ rest) {
+  __shared__ int diff;
+  const int64_t t = blockIdx.x;
+  if (t >= ntiles) return;
+  const TileHdr H = hdr[t];
+  if (H.flags || H.prog == t) return;
+  const TileHdr R = hdr[H.prog];
+  if (threadIdx.x == 0) diff = (R.nz != H.nz || R.nc != H.nc || R.nel != H.nel || R.flags) ? 1 : 0;
+  __syncthreads();
+  if (!diff) {
+    int d = 0;
+    for (int k = threadIdx.x; k < H.nel; k += kTT) d |= elist[t * (int64_t)emax + k] != elist[H.prog * (int64_t)emax + k];
+    for (int k = threadIdx.x; k < kTileMaxClass + 2; k += kTT)
+      d |= cls[t * (kTileMaxClass + 2) + k] != cls[H.prog * (kTileMaxClass + 2) + k];
+    for (int k = threadIdx.x; k < H.nz; k += kTT) d |= firsts[H.p0 + k] != firsts[R.p0 + k];
+    for (int k = threadIdx.x; k < H.nc - H.nz; k += kTT) d |= rest[(H.q0 - H.p0) + k] != rest[(R.q0 - R.p0) + k];
+    if (d) atomicOr(&diff, 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && diff) hdr[t].prog = t;
+}
+
+// Per-element value tables.  Full records: the S stored values.
+struct RecFull {
+  const double* store;
+  int S;
+  __device__ __forceinline__ void stage(int64_t e, double* v) const {
+    for (int k = 0; k < S; ++k) v[k] = __ldg(store + e * S + k);
+  }
+  __device__ __forceinline__ double value(uint32_t st) const { return __ldg(store + st); }
+};
+
+// The 8 bases of the exact-rational T6 record (64 bytes per element).
+struct RecT6R {
+  const double* bases;
+  __device__ __forceinline__ void stage(int64_t e, double* v) const {
+    const double2* p = reinterpret_cast<const double2*>(bases + e * 8);
+    double b[8];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const double2 x = __ldg(p + k);
+      b[2 * k] = x.x;
+      b[2 * k + 1] = x.y;
+    }
+    t6r_table(b, v);
+  }
+  // stored entry st = e * 21 + s of the record
+  __device__ __forceinline__ double value(uint32_t st) const {
+    const uint32_t e = st / 21u, s = st - e * 21u;
+    double b[8], v[kT6RTable];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) b[k] = __ldg(bases + (int64_t)e * 8 + k);
+    t6r_table(b, v);
+    return v[t6r_entry((int)s)];
+  }
+};
+
+// One CTA per tile: the value table of the tile's elements in shared memory,
+// one thread per nonzero in count order, the tile's values written out in
+// CSC order.
+template <class Rec>
+__global__ void __launch_bounds__(kTT) tile_reduce_k(const TileHdr* __restrict__ hdr, int emax, int V,
+                                                     const int32_t* __restrict__ elist, const uint16_t* __restrict__ cls,
+                                                     const uint32_t* __restrict__ firsts,
+                                                     const uint16_t* __restrict__ rest, const int32_t* __restrict__ cptr,
+                                                     const int32_t* __restrict__ contrib, Rec rec,
+                                                     double* __restrict__ vals) {
+  extern __shared__ double sm[];
+  __shared__ int cstart[kTileMaxClass + 2], rbase[kTileMaxClass + 2];
+  const TileHdr H = hdr[blockIdx.x];
+  if (H.flags) {
+    if (H.flags & kTileEmpty) return;
+    // beyond the limits: every nonzero from its contributor list
+    for (int i = threadIdx.x; i < H.nz; i += kTT) {
+      const int32_t b = cptr[H.p0 + i], e = cptr[H.p0 + i + 1];
+      double s = rec.value((uint32_t)contrib[b]);
+      for (int32_t k = b + 1; k < e; ++k) s = __dadd_rn(s, rec.value((uint32_t)contrib[k]));
+      vals[H.p0 + i] = s;
+    }
+    return;
+  }
+  const TileHdr P = H.prog == blockIdx.x ? H : hdr[H.prog];
+  double* tbl = sm;
+  double* out = sm + (size_t)emax * V;
+  const int32_t* el = elist + (int64_t)H.prog * emax;
+  for (int k = threadIdx.x; k < H.nel; k += kTT) rec.stage((int64_t)H.emin + el[k], tbl + k * V);
+  if (threadIdx.x < kTileMaxClass + 2) {
+    cstart[threadIdx.x] = cls[(int64_t)H.prog * (kTileMaxClass + 2) + threadIdx.x];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int rb = 0;
+    for (int c = 1; c <= kTileMaxClass; ++c) {
+      rbase[c] = rb;
+      rb += (cstart[c + 1] - cstart[c]) * (c - 1);
+    }
+  }
+  __syncthreads();
+  const uint32_t* fp = firsts + P.p0;
+  const uint16_t* rp = rest + (P.q0 - P.p0);
+  int c = 1;
+  for (int i = threadIdx.x; i < H.nz; i += kTT) {
+    while (i >= cstart[c + 1]) ++c;
+    const uint32_t f = __ldg(fp + i);
+    double s = tbl[f & 0xffffu];
+    const int n = cstart[c + 1] - cstart[c];
+    const uint16_t* r = rp + rbase[c] + (i - cstart[c]);
+    for (int k = 1; k < c; ++k) s = __dadd_rn(s, tbl[__ldg(r + (k - 1) * n)]);
+    out[f >> 16] = s;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < H.nz; i += kTT) vals[H.p0 + i] = out[i];
+}
+
+}  // namespace
+
+void TilePlan::release(Ctx* c) {
+  hdr.release(c);
+  elist.release(c);
+  cls.release(c);
+  firsts.release(c);
+  rest.release(c);
+  ntiles = 0;
+  built = 0;
+  S = V = emax = 0;
+  nprograms = nfallback = 0;
+}
+
+int build_tile_plan(Ctx* c, Pattern& P, int S, int V, const uint8_t* map) {
+  TilePlan& T = P.tiles;
+  T.release(c);
+  if (P.nnz == 0 || P.ncol == 0) return ELFEL_OK;
+  if (S < 1 || S > kTileMaxS || V < 1) return fail(c, ELFEL_ERR_ARG, "tile plan: record of %d entries", S);
+  T.S = S;
+  T.V = V;
+  T.emax = std::min(kTileMaxEl, (int)(kTileTableBytes / (V * (int)sizeof(double))));
+  if (T.emax * V > 0xffff) T.emax = 0xffff / V;
+  // column sizes on the host: nonzeros from colptr, contributions from cptr at the column starts
+  const int64_t ncol = P.ncol;
+  std::vector<int64_t> colptr((size_t)ncol + 1);
+  ELFEL_CUDA(c, cudaMemcpyAsync(colptr.data(), P.colptr.p, sizeof(int64_t) * (ncol + 1), cudaMemcpyDeviceToHost,
+                                c->stream));
+  ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+  std::vector<int32_t> cq((size_t)ncol + 1);
+  {
+    DBuf<int32_t> d;
+    ELFEL_TRY(d.alloc(c, (size_t)ncol + 1));
+    cptr_at_cols_k<<<grid_for(ncol + 1, 256, (int64_t)c->sm_count * 8), 256, 0, c->stream>>>(P.colptr.p, P.cptr.p,
+                                                                                             ncol, d.p);
+    ELFEL_LAUNCH_CHECK(c);
+    ELFEL_CUDA(c, cudaMemcpyAsync(cq.data(), d.p, sizeof(int32_t) * (ncol + 1), cudaMemcpyDeviceToHost, c->stream));
+    ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+    d.release(c);
+  }
+  // greedy tiles of consecutive columns within the limits
+  std::vector<TileHdr> tiles;
+  for (int64_t c0 = 0; c0 < ncol;) {
+    int64_t c1 = c0 + 1;
+    while (c1 < ncol && c1 - c0 < kTileMaxCols && colptr[c1 + 1] - colptr[c0] <= kTileMaxNz &&
+           (int64_t)cq[c1 + 1] - cq[c0] <= kTileMaxContrib)
+      ++c1;
+    TileHdr h{};
+    h.col0 = (int32_t)c0;
+    h.ncols = (int32_t)(c1 - c0);
+    tiles.push_back(h);
+    c0 = c1;
+  }
+  TileBuildArgs a;
+  a.colptr = P.colptr.p;
+  a.cptr = P.cptr.p;
+  a.contrib = P.contrib.p;
+  a.S = S;
+  a.V = V;
+  a.sdiv.init((uint32_t)S);
+  memset(a.map, 0, sizeof(a.map));
+  for (int s = 0; s < S; ++s) a.map[s] = map ? map[s] : (uint8_t)s;
+  a.emax = T.emax;
+  // count, split the tiles beyond the element or class limits, count again
+  for (int round = 0;; ++round) {
+    const int64_t nt = (int64_t)tiles.size();
+    ELFEL_TRY(T.hdr.alloc(c, (size_t)nt));
+    ELFEL_CUDA(c, cudaMemcpyAsync(T.hdr.p, tiles.data(), sizeof(TileHdr) * nt, cudaMemcpyHostToDevice, c->stream));
+    tile_count_k<<<(unsigned)nt, kTT, 0, c->stream>>>(T.hdr.p, nt, a);
+    ELFEL_LAUNCH_CHECK(c);
+    ELFEL_CUDA(c, cudaMemcpyAsync(tiles.data(), T.hdr.p, sizeof(TileHdr) * nt, cudaMemcpyDeviceToHost, c->stream));
+    ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+    std::vector<TileHdr> next;
+    bool split = false;
+    for (const TileHdr& h : tiles) {
+      if ((h.flags & kTileSplit) && h.ncols > 1 && round < 12) {
+        TileHdr x{}, y{};
+        x.col0 = h.col0;
+        x.ncols = h.ncols / 2;
+        y.col0 = h.col0 + x.ncols;
+        y.ncols = h.ncols - x.ncols;
+        next.push_back(x);
+        next.push_back(y);
+        split = true;
+      } else {
+        TileHdr k = h;
+        if (k.flags & kTileSplit) k.flags = kTileFallback;
+        next.push_back(k);
+      }
+    }
+    if (!split) {
+      tiles.swap(next);
+      break;
+    }
+    tiles.swap(next);
+    T.hdr.release(c);
+  }
+  const int64_t nt = (int64_t)tiles.size();
+  ELFEL_CUDA(c, cudaMemcpyAsync(T.hdr.p, tiles.data(), sizeof(TileHdr) * nt, cudaMemcpyHostToDevice, c->stream));
+  T.ntiles = nt;
+  ELFEL_TRY(T.elist.alloc(c, (size_t)(nt * T.emax)));
+  ELFEL_TRY(T.cls.alloc(c, (size_t)(nt * (kTileMaxClass + 2))));
+  ELFEL_TRY(T.firsts.alloc(c, (size_t)P.nnz));
+  ELFEL_TRY(T.rest.alloc(c, (size_t)std::max<int64_t>(1, P.nslots - P.nnz)));
+  tile_build_k<<<(unsigned)nt, kTT, 0, c->stream>>>(T.hdr.p, nt, a, T.elist.p, T.cls.p, T.firsts.p, T.rest.p);
+  ELFEL_LAUNCH_CHECK(c);
+  // deduplicate equal programs: digests on the device, groups on the host,
+  // then a word-for-word check of every tile against its representative
+  DBuf<uint64_t> hash;
+  ELFEL_TRY(hash.alloc(c, (size_t)nt));
+  tile_hash_k<<<(unsigned)nt, kTT, 0, c->stream>>>(T.hdr.p, nt, T.emax, T.elist.p, T.cls.p, T.firsts.p, T.rest.p,
+                                                   hash.p);
+  ELFEL_LAUNCH_CHECK(c);
+  std::vector<uint64_t> hh((size_t)nt);
+  ELFEL_CUDA(c, cudaMemcpyAsync(hh.data(), hash.p, sizeof(uint64_t) * nt, cudaMemcpyDeviceToHost, c->stream));
+  ELFEL_CUDA(c, cudaMemcpyAsync(tiles.data(), T.hdr.p, sizeof(TileHdr) * nt, cudaMemcpyDeviceToHost, c->stream));
+  ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+  hash.release(c);
+  std::unordered_map<uint64_t, int32_t> first;
+  first.reserve((size_t)nt);
+  int64_t nprog = 0, nfb = 0;
+  for (int64_t t = 0; t < nt; ++t) {
+    TileHdr& h = tiles[t];
+    h.prog = (int32_t)t;
+    if (h.flags) {
+      nfb += (h.flags & kTileFallback) ? 1 : 0;
+      continue;
+    }
+    auto it = first.find(hh[t]);
+    if (it == first.end()) {
+      first.emplace(hh[t], (int32_t)t);
+      ++nprog;
+    } else {
+      h.prog = it->second;
+    }
+  }
+  ELFEL_CUDA(c, cudaMemcpyAsync(T.hdr.p, tiles.data(), sizeof(TileHdr) * nt, cudaMemcpyHostToDevice, c->stream));
+  tile_verify_k<<<(unsigned)nt, kTT, 0, c->stream>>>(T.hdr.p, nt, T.emax, T.elist.p, T.cls.p, T.firsts.p, T.rest.p);
+  ELFEL_LAUNCH_CHECK(c);
+  ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+  T.nprograms = nprog;
+  T.nfallback = nfb;
+  T.built = 1;
+  return ELFEL_OK;
+}
+
+static size_t tile_smem(const TilePlan& T) { return (size_t)T.emax * T.V * sizeof(double) + kTileMaxNz * sizeof(double); }
+
+int tile_reduce(Ctx* c, const Pattern& P, const double* src, int t6r_bases, double* vals) {
+  const TilePlan& T = P.tiles;
+  if (!T.built) return fail(c, ELFEL_ERR_STATE, "tile reduction without a plan");
+  if (T.ntiles == 0) return ELFEL_OK;
+  const size_t sm = tile_smem(T);
+  if (t6r_bases) {
+    if (T.V != kT6RTable || T.S != 21) return fail(c, ELFEL_ERR_STATE, "tile plan is not for T6 bases");
+    RecT6R r{src};
+    ELFEL_CUDA(c, cudaFuncSetAttribute(tile_reduce_k<RecT6R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    tile_reduce_k<RecT6R><<<(unsigned)T.ntiles, kTT, sm, c->stream>>>(
+        T.hdr.p, T.emax, T.V, T.elist.p, T.cls.p, T.firsts.p, T.rest.p, P.cptr.p, P.contrib.p, r, vals);
+  } else {
+    if (T.V != T.S) return fail(c, ELFEL_ERR_STATE, "tile plan is not for full records");
+    RecFull r{src, T.S};
+    ELFEL_CUDA(c, cudaFuncSetAttribute(tile_reduce_k<RecFull>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    tile_reduce_k<RecFull><<<(unsigned)T.ntiles, kTT, sm, c->stream>>>(
+        T.hdr.p, T.emax, T.V, T.elist.p, T.cls.p, T.firsts.p, T.rest.p, P.cptr.p, P.contrib.p, r, vals);
+  }
+  ELFEL_LAUNCH_CHECK(c);
+  return ELFEL_OK;
+}
+
+}  // namespace elfel

@@ -176,6 +176,30 @@ typedef struct {
  * slot-to-nonzero map once (device key sort).  Later elfel_fused_* calls
  * reuse them.  Triplet order is that of the reference's assemble! calls. */
 ELFEL_API int elfel_fused_setup(elfel_sysmat* m, const elfel_fused_desc* d);
+/* numberdofs!(fesps) of src/FESpaces.jl:250-259 on the device for nspaces
+ * spaces with one field each: space s has nterms[s] terms of ncomp[s]
+ * components and the essential-BC mask isdatum[s] (nterms x ncomp bytes,
+ * term-major, nonzero = data DOF, as setebc! leaves FEField.isdatum).  Free
+ * DOFs are numbered space by space, term-major/component-minor, then the data
+ * DOFs (src/FEFields.jl:137-177), with the reference's chaining of first
+ * numbers.  dofnums[s] (nterms x ncomp, may be NULL) receives the 1-based
+ * numbers, *nfree (may be NULL) the number of unknowns. */
+ELFEL_API int elfel_number_dofs(elfel_ctx* ctx, int32_t nspaces, const int64_t* nterms, const int32_t* ncomp,
+                                const uint8_t* const* isdatum, int64_t* const* dofnums, int64_t* nfree);
+/* Fused set-up with the DOF numbering on the device: numberdofs! of the
+ * space (heat, elasticity) or of [velocity, pressure] (Stokes) from their
+ * essential-BC masks (src/FESpaces.jl:250-259 -> src/FEFields.jl:137-177:
+ * free DOFs term-major/component-minor, space by space, then the data DOFs),
+ * and the FEIterator DOF tables built from the connectivity
+ * (src/FEIterators.jl:161-171), so that no DOF table crosses the host link.
+ * The spaces' eldofs pointers are not read.  isdatum_u: u.nnodes x u.ncomp
+ * bytes, nonzero where setebc! fixed the DOF (isdatum_p likewise for the
+ * Stokes pressure; else NULL).  d->ndofs must be the spaces' DOF total.
+ * dofnums_u / dofnums_p (may be NULL): the 1-based numbers, as the FEField
+ * dofnums arrays; *nfree (may be NULL): the number of unknowns. */
+ELFEL_API int elfel_fused_setup_numbered(elfel_sysmat* m, const elfel_fused_desc* d, const uint8_t* isdatum_u,
+                                         const uint8_t* isdatum_p, int64_t* dofnums_u, int64_t* dofnums_p,
+                                         int64_t* nfree);
 /* Replace the node coordinates of the primary space (same mesh topology). */
 ELFEL_API int elfel_fused_set_geometry(elfel_sysmat* m, const double* xy);
 /* Heat: K and F for conductivity kappa[nel] (NULL: keep the resident values
@@ -223,6 +247,11 @@ ELFEL_API int elfel_block_dirichlet(elfel_sysmat* m, const double* coef6, double
 ELFEL_API int elfel_fused_tables(elfel_sysmat* m, int64_t* conn, double* xy, int64_t* eldofs);
 /* Sizes of a fused system: elements, nodes of the primary space, DOFs. */
 ELFEL_API int elfel_fused_dims(elfel_sysmat* m, int64_t* nel, int64_t* nnodes, int64_t* ndofs);
+/* The tile reduction plan of a fused system's K pattern (no counterpart in
+ * the reference; built at a T6 heat pattern's second assembly): tiles, the
+ * distinct tile programs they read, tiles summed from the contributor lists.
+ * All zero when no plan is built. */
+ELFEL_API int elfel_sysmat_tile_stats(elfel_sysmat* m, int64_t* ntiles, int64_t* nprograms, int64_t* nfallback);
 
 /* ------------------------------------------------------------------ error integrals
  * evaluate_pressure_error / evaluate_velocity_error of test/test_stokes.jl:438-496
