@@ -616,6 +616,9 @@ def main():
                              "frac": asm_bytes / t_step / 1e9 / hbm, "what": "the same bytes / the whole step"},
                 "kernels": kernel_rows}
 
+    ntiles, nprog, nfb = am.tile_stats()
+    roofline["tile_plan"] = {"tiles": ntiles, "programs": nprog, "fallback_tiles": nfb}
+
     # --- e2e through the C ABI from pinned host buffers -------------------
     conn_h = torch.from_numpy(np.ascontiguousarray(mesh.conn)).pin_memory()
     xy_h = torch.from_numpy(np.ascontiguousarray(mesh.xy)).pin_memory()

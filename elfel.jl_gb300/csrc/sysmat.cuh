@@ -182,8 +182,8 @@ constexpr int kReduceWindow = 128;
 
 // Tile reduction plan of a pattern (tiles.cu).
 constexpr int kTileThreads = 256;
-constexpr int kTileMaxNz = 2048;       // nonzeros of a tile
-constexpr int kTileMaxContrib = 4096;  // contributions of a tile
+constexpr int kTileMaxNz = 512;        // nonzeros of a tile
+constexpr int kTileMaxContrib = 1024;  // contributions of a tile
 constexpr int kTileMaxCols = 256;      // columns of a tile
 constexpr int kTileMaxClass = 15;      // contributions of one nonzero (more: the tile takes the slow path)
 constexpr int kTileMaxEl = 320;        // distinct elements of a tile
@@ -194,25 +194,29 @@ constexpr int kTileFallback = 1, kTileSplit = 2, kTileEmpty = 4;
 struct TileHdr {
   int64_t p0;       // first nonzero of the tile (CSC position)
   int64_t q0;       // first contribution (cptr[p0])
+  int64_t boff;     // byte offset of the tile's program in the blob array
   int32_t col0, ncols;
   int32_t nz, nc;   // nonzeros, contributions
   int32_t nel;      // distinct elements
   int32_t maxcnt;   // largest contributor count
   int32_t emin;     // smallest element
   int32_t flags;    // kTileFallback: summed from the contributor lists; kTileEmpty: no nonzero
-  int32_t prog;     // tile whose program this tile reads
+  int32_t prog;     // tile whose program this tile reads (its representative)
   int32_t pad;
 };
 
 struct TilePlan {
   int built = 0;
   int S = 0, V = 0, emax = 0;  // record entries, value-table entries per element, elements per tile
+  int maxblob = 0;             // bytes of the largest program
+  int maxnel = 0;              // elements of the largest tile
   int64_t ntiles = 0, nprograms = 0, nfallback = 0;
   DBuf<TileHdr> hdr;
-  DBuf<int32_t> elist;    // ntiles x emax: element - emin, ascending
-  DBuf<uint16_t> cls;     // ntiles x (kTileMaxClass + 2): first nonzero (count order) of each count
-  DBuf<uint32_t> firsts;  // nnz, count order within each tile: position << 16 | table index
-  DBuf<uint16_t> rest;    // nslots - nnz: table indices of the further contributions
+  // the distinct programs, each 16-byte aligned: count-class starts (uint16),
+  // element offsets from the tile's smallest element (int32, ascending),
+  // first codes in count order (uint32: position << 16 | table index),
+  // further codes (uint16 table indices, class by class, contribution-major)
+  DBuf<uint8_t> blob;
   void release(Ctx* c);
 };
 

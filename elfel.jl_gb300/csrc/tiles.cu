@@ -20,10 +20,13 @@
 // the order in which SparseArrays.sparse adds duplicates -- so the values are
 // the bits of reduce_values.
 //
-// Tiles whose programs are equal word for word (the tiles of a structured
-// mesh away from its boundary are translates of a few) share one copy of the
-// program: per step a tile reads its own first nonzero and smallest element
-// and the program of its representative, which stays in L2.
+// A program is one contiguous, 16-byte aligned blob (count classes, element
+// offsets, first codes, further codes), copied into shared memory with
+// vector loads at the start of each tile.  Tiles whose programs are equal
+// word for word (the tiles of a structured mesh away from its boundary are
+// translates of a few) share one copy: only distinct programs are kept, and
+// per step a tile reads its own first nonzero and smallest element and the
+// blob of its program, which stays in L2.
 #include <algorithm>
 #include <unordered_map>
 #include <vector>
@@ -46,6 +49,22 @@ struct TileBuildArgs {
   uint8_t map[kTileMaxS];
   int emax;
 };
+
+// Byte layout of a tile program: count classes (kTileMaxClass + 2 uint16,
+// padded to 48 bytes), element offsets (int32), first codes (uint32), further
+// codes (uint16), each part padded to 16 bytes.
+struct BlobLayout {
+  int el, f, r, bytes;
+};
+__host__ __device__ __forceinline__ int pad16(int b) { return (b + 15) & ~15; }
+__host__ __device__ __forceinline__ BlobLayout blob_layout(int nel, int nz, int nc) {
+  BlobLayout L;
+  L.el = 48;
+  L.f = L.el + pad16(4 * nel);
+  L.r = L.f + pad16(4 * nz);
+  L.bytes = L.r + pad16(2 * (nc - nz));
+  return L;
+}
 
 // cq[k] = cptr[colptr[k]]: the first contribution of each column (k <= ncol).
 __global__ void cptr_at_cols_k(const int64_t* __restrict__ colptr, const int32_t* __restrict__ cptr, int64_t ncol,
@@ -120,10 +139,10 @@ __global__ void __launch_bounds__(kTT) tile_count_k(TileHdr* __restrict__ hdr, i
   }
 }
 
-// Second pass: the program of every tile within the limits.
+// Second pass: the program of every tile within the limits, written at the
+// tile's blob offset.
 __global__ void __launch_bounds__(kTT) tile_build_k(TileHdr* __restrict__ hdr, int64_t ntiles, TileBuildArgs a,
-                                                    int32_t* __restrict__ elist, uint16_t* __restrict__ cls,
-                                                    uint32_t* __restrict__ firsts, uint16_t* __restrict__ rest) {
+                                                    uint8_t* __restrict__ blob) {
   __shared__ int32_t el[kTileMaxContrib];
   __shared__ uint8_t cnt[kTileMaxNz];
   __shared__ uint16_t sidx[kTileMaxNz];
@@ -136,10 +155,17 @@ __global__ void __launch_bounds__(kTT) tile_build_k(TileHdr* __restrict__ hdr, i
   if (H.flags) return;
   const int64_t p0 = H.p0, q0 = H.q0;
   const int nz = H.nz, nc = H.nc;
+  const BlobLayout L = blob_layout(H.nel, nz, nc);
+  uint8_t* b0 = blob + H.boff;
+  uint16_t* cls = reinterpret_cast<uint16_t*>(b0);
+  int32_t* elist = reinterpret_cast<int32_t*>(b0 + L.el);
+  uint32_t* firsts = reinterpret_cast<uint32_t*>(b0 + L.f);
+  uint16_t* rest = reinterpret_cast<uint16_t*>(b0 + L.r);
+  for (int k = threadIdx.x; k < L.bytes / 4; k += kTT) reinterpret_cast<uint32_t*>(b0)[k] = 0u;  // the padding
   for (int i = threadIdx.x; i < nc; i += kTT) el[i] = (int32_t)a.sdiv.div((uint32_t)a.contrib[q0 + i]);
   for (int i = threadIdx.x; i < nz; i += kTT) cnt[i] = (uint8_t)(a.cptr[p0 + i + 1] - a.cptr[p0 + i]);
   if (threadIdx.x < kTileMaxClass + 2) cstart[threadIdx.x] = 0;
-  smem_sort(el, nc);
+  smem_sort(el, nc);  // contains __syncthreads (after the padding writes)
   // distinct elements, compacted in place by one warp (ordered ballots)
   if (threadIdx.x < 32) {
     int w = 0;
@@ -158,7 +184,7 @@ __global__ void __launch_bounds__(kTT) tile_build_k(TileHdr* __restrict__ hdr, i
   __syncthreads();
   const int nel = nuniq;
   const int32_t emin = el[0];
-  for (int k = threadIdx.x; k < nel; k += kTT) elist[t * (int64_t)a.emax + k] = el[k] - emin;
+  for (int k = threadIdx.x; k < nel; k += kTT) elist[k] = el[k] - emin;
   // count classes and the stable order within each class
   for (int i = threadIdx.x; i < nz; i += kTT) atomicAdd(&cstart[cnt[i] + 1], 1);
   __syncthreads();
@@ -194,7 +220,7 @@ __global__ void __launch_bounds__(kTT) tile_build_k(TileHdr* __restrict__ hdr, i
   }
   __syncthreads();
   for (int k = threadIdx.x; k < kTileMaxClass + 2; k += kTT)
-    cls[t * (kTileMaxClass + 2) + k] = (uint16_t)(k == kTileMaxClass + 1 ? nz : cstart[k]);
+    cls[k] = (uint16_t)(k == kTileMaxClass + 1 ? nz : cstart[k]);
   // codes: table index of every contribution
   for (int i = threadIdx.x; i < nz; i += kTT) {
     const int c = cnt[i];
@@ -212,9 +238,9 @@ __global__ void __launch_bounds__(kTT) tile_build_k(TileHdr* __restrict__ hdr, i
       }
       const uint32_t code = (uint32_t)(lo * a.V + a.map[s]);
       if (k == 0)
-        firsts[p0 + si] = ((uint32_t)i << 16) | code;
+        firsts[si] = ((uint32_t)i << 16) | code;
       else
-        rest[(q0 - p0) + rbase[c] + (k - 1) * nclass + (si - cstart[c])] = (uint16_t)code;
+        rest[rbase[c] + (k - 1) * nclass + (si - cstart[c])] = (uint16_t)code;
     }
   }
   if (threadIdx.x == 0) {
@@ -236,10 +262,8 @@ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
 
 // A 64-bit digest of each program: a sum of mixed (word, index) pairs, so
 // that it does not depend on the order threads add them.
-__global__ void __launch_bounds__(kTT) tile_hash_k(const TileHdr* __restrict__ hdr, int64_t ntiles, int emax,
-                                                   const int32_t* __restrict__ elist, const uint16_t* __restrict__ cls,
-                                                   const uint32_t* __restrict__ firsts,
-                                                   const uint16_t* __restrict__ rest, uint64_t* __restrict__ hash) {
+__global__ void __launch_bounds__(kTT) tile_hash_k(const TileHdr* __restrict__ hdr, int64_t ntiles,
+                                                   const uint8_t* __restrict__ blob, uint64_t* __restrict__ hash) {
   __shared__ unsigned long long part;
   const int64_t t = blockIdx.x;
   if (t >= ntiles) return;
@@ -250,24 +274,19 @@ __global__ void __launch_bounds__(kTT) tile_hash_k(const TileHdr* __restrict__ h
   }
   if (threadIdx.x == 0) part = 0;
   __syncthreads();
+  const BlobLayout L = blob_layout(H.nel, H.nz, H.nc);
+  const uint32_t* w = reinterpret_cast<const uint32_t*>(blob + H.boff);
   uint64_t h = 0;
-  for (int k = threadIdx.x; k < H.nel; k += kTT) h += mix64(((uint64_t)1 << 60) + ((uint64_t)k << 32) + (uint32_t)elist[t * (int64_t)emax + k]);
-  for (int k = threadIdx.x; k < kTileMaxClass + 2; k += kTT)
-    h += mix64(((uint64_t)2 << 60) + ((uint64_t)k << 32) + cls[t * (kTileMaxClass + 2) + k]);
-  for (int k = threadIdx.x; k < H.nz; k += kTT) h += mix64(((uint64_t)3 << 60) + ((uint64_t)k << 32) + firsts[H.p0 + k]);
-  for (int k = threadIdx.x; k < H.nc - H.nz; k += kTT)
-    h += mix64(((uint64_t)4 << 60) + ((uint64_t)k << 32) + rest[(H.q0 - H.p0) + k]);
+  for (int k = threadIdx.x; k < L.bytes / 4; k += kTT) h += mix64(((uint64_t)k << 32) + w[k]);
   atomicAdd(&part, (unsigned long long)h);
   __syncthreads();
   if (threadIdx.x == 0) hash[t] = mix64(part ^ ((uint64_t)H.nz << 40) ^ ((uint64_t)H.nc << 20) ^ (uint64_t)H.nel);
 }
 
 // A tile keeps its representative's program only if the two are equal word
-// for word; otherwise it reads its own.
-__global__ void __launch_bounds__(kTT) tile_verify_k(TileHdr* __restrict__ hdr, int64_t ntiles, int emax,
-                                                     const int32_t* __restrict__ elist, const uint16_t* __restrict__ cls,
-                                                     const uint32_t* __restrict__ firsts,
-                                                     const uint16_t* __restrict__ rest) {
+// for word; otherwise it is its own representative.
+__global__ void __launch_bounds__(kTT) tile_verify_k(TileHdr* __restrict__ hdr, int64_t ntiles,
+                                                     const uint8_t* __restrict__ blob) {
   __shared__ int diff;
   const int64_t t = blockIdx.x;
   if (t >= ntiles) return;
@@ -277,16 +296,26 @@ __global__ void __launch_bounds__(kTT) tile_verify_k(TileHdr* __restrict__ hdr, 
   if (threadIdx.x == 0) diff = (R.nz != H.nz || R.nc != H.nc || R.nel != H.nel || R.flags) ? 1 : 0;
   __syncthreads();
   if (!diff) {
+    const BlobLayout L = blob_layout(H.nel, H.nz, H.nc);
+    const uint32_t* a = reinterpret_cast<const uint32_t*>(blob + H.boff);
+    const uint32_t* b = reinterpret_cast<const uint32_t*>(blob + R.boff);
     int d = 0;
-    for (int k = threadIdx.x; k < H.nel; k += kTT) d |= elist[t * (int64_t)emax + k] != elist[H.prog * (int64_t)emax + k];
-    for (int k = threadIdx.x; k < kTileMaxClass + 2; k += kTT)
-      d |= cls[t * (kTileMaxClass + 2) + k] != cls[H.prog * (kTileMaxClass + 2) + k];
-    for (int k = threadIdx.x; k < H.nz; k += kTT) d |= firsts[H.p0 + k] != firsts[R.p0 + k];
-    for (int k = threadIdx.x; k < H.nc - H.nz; k += kTT) d |= rest[(H.q0 - H.p0) + k] != rest[(R.q0 - R.p0) + k];
+    for (int k = threadIdx.x; k < L.bytes / 4; k += kTT) d |= a[k] != b[k];
     if (d) atomicOr(&diff, 1);
   }
   __syncthreads();
   if (threadIdx.x == 0 && diff) hdr[t].prog = t;
+}
+
+// Copy of the distinct programs into the compact blob array: job j moves
+// bytes[j] bytes from offset src[j] to offset dst[j] (multiples of 16).
+__global__ void blob_copy_k(const int64_t* __restrict__ src, const int64_t* __restrict__ dst,
+                            const int32_t* __restrict__ bytes, const uint8_t* __restrict__ from,
+                            uint8_t* __restrict__ to) {
+  const int j = blockIdx.x;
+  const uint4* a = reinterpret_cast<const uint4*>(from + src[j]);
+  uint4* b = reinterpret_cast<uint4*>(to + dst[j]);
+  for (int k = threadIdx.x; k < bytes[j] / 16; k += blockDim.x) b[k] = a[k];
 }
 
 // Per-element value tables.  Full records: the S stored values.
@@ -324,23 +353,24 @@ struct RecT6R {
   }
 };
 
-// One CTA per tile: the value table of the tile's elements in shared memory,
-// one thread per nonzero in count order, the tile's values written out in
-// CSC order.
+// One CTA per tile: the tile's program copied into shared memory while the
+// value table of its elements is staged beside it, one thread per nonzero in
+// count order, the tile's values written out in CSC order.
+constexpr int kRT = 128;                 // threads of tile_reduce_k
+constexpr int kRPer = kTileMaxNz / kRT;  // nonzeros per thread
+
 template <class Rec>
-__global__ void __launch_bounds__(kTT) tile_reduce_k(const TileHdr* __restrict__ hdr, int emax, int V,
-                                                     const int32_t* __restrict__ elist, const uint16_t* __restrict__ cls,
-                                                     const uint32_t* __restrict__ firsts,
-                                                     const uint16_t* __restrict__ rest, const int32_t* __restrict__ cptr,
+__global__ void __launch_bounds__(kRT) tile_reduce_k(const TileHdr* __restrict__ hdr, int maxnel, int V, int maxblob,
+                                                     const uint8_t* __restrict__ blob,
+                                                     const int32_t* __restrict__ cptr,
                                                      const int32_t* __restrict__ contrib, Rec rec,
                                                      double* __restrict__ vals) {
-  extern __shared__ double sm[];
-  __shared__ int cstart[kTileMaxClass + 2], rbase[kTileMaxClass + 2];
+  extern __shared__ uint4 smq[];  // program (maxblob bytes) | value table | values
   const TileHdr H = hdr[blockIdx.x];
   if (H.flags) {
     if (H.flags & kTileEmpty) return;
     // beyond the limits: every nonzero from its contributor list
-    for (int i = threadIdx.x; i < H.nz; i += kTT) {
+    for (int i = threadIdx.x; i < H.nz; i += kRT) {
       const int32_t b = cptr[H.p0 + i], e = cptr[H.p0 + i + 1];
       double s = rec.value((uint32_t)contrib[b]);
       for (int32_t k = b + 1; k < e; ++k) s = __dadd_rn(s, rec.value((uint32_t)contrib[k]));
@@ -348,50 +378,50 @@ __global__ void __launch_bounds__(kTT) tile_reduce_k(const TileHdr* __restrict__
     }
     return;
   }
-  const TileHdr P = H.prog == blockIdx.x ? H : hdr[H.prog];
-  double* tbl = sm;
-  double* out = sm + (size_t)emax * V;
-  const int32_t* el = elist + (int64_t)H.prog * emax;
-  for (int k = threadIdx.x; k < H.nel; k += kTT) rec.stage((int64_t)H.emin + el[k], tbl + k * V);
-  if (threadIdx.x < kTileMaxClass + 2) {
-    cstart[threadIdx.x] = cls[(int64_t)H.prog * (kTileMaxClass + 2) + threadIdx.x];
-  }
+  const BlobLayout L = blob_layout(H.nel, H.nz, H.nc);
+  // the program into shared memory and, at the same time, the value table of
+  // the tile's elements (their offsets read from the program in L2)
+  const uint4* src = reinterpret_cast<const uint4*>(blob + H.boff);
+  for (int k = threadIdx.x; k < L.bytes / 16; k += kRT) smq[k] = __ldg(src + k);
+  const uint8_t* sb = reinterpret_cast<const uint8_t*>(smq);
+  double* tbl = reinterpret_cast<double*>(reinterpret_cast<uint8_t*>(smq) + maxblob);
+  double* out = tbl + (size_t)maxnel * V;
+  const int32_t* gel = reinterpret_cast<const int32_t*>(blob + H.boff + L.el);
+  for (int k = threadIdx.x; k < H.nel; k += kRT) rec.stage((int64_t)H.emin + __ldg(gel + k), tbl + k * V);
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int rb = 0;
-    for (int c = 1; c <= kTileMaxClass; ++c) {
-      rbase[c] = rb;
-      rb += (cstart[c + 1] - cstart[c]) * (c - 1);
+  const uint16_t* cstart = reinterpret_cast<const uint16_t*>(sb);
+  const uint32_t* sf = reinterpret_cast<const uint32_t*>(sb + L.f);
+  const uint16_t* sr = reinterpret_cast<const uint16_t*>(sb + L.r);
+  int c = 1, rb = 0;  // class of the current nonzero and the start of its class's further codes
+#pragma unroll
+  for (int j = 0; j < kRPer; ++j) {
+    const int i = threadIdx.x + j * kRT;
+    if (i < H.nz) {
+      while (i >= cstart[c + 1]) {
+        rb += (cstart[c + 1] - cstart[c]) * (c - 1);
+        ++c;
+      }
+      const uint32_t f = sf[i];
+      const int n = cstart[c + 1] - cstart[c];
+      const uint16_t* r = sr + rb + (i - cstart[c]);
+      double s = tbl[f & 0xffffu];
+#pragma unroll 1
+      for (int k = 1; k < c; ++k) s = __dadd_rn(s, tbl[r[(k - 1) * n]]);
+      out[f >> 16] = s;
     }
   }
   __syncthreads();
-  const uint32_t* fp = firsts + P.p0;
-  const uint16_t* rp = rest + (P.q0 - P.p0);
-  int c = 1;
-  for (int i = threadIdx.x; i < H.nz; i += kTT) {
-    while (i >= cstart[c + 1]) ++c;
-    const uint32_t f = __ldg(fp + i);
-    double s = tbl[f & 0xffffu];
-    const int n = cstart[c + 1] - cstart[c];
-    const uint16_t* r = rp + rbase[c] + (i - cstart[c]);
-    for (int k = 1; k < c; ++k) s = __dadd_rn(s, tbl[__ldg(r + (k - 1) * n)]);
-    out[f >> 16] = s;
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < H.nz; i += kTT) vals[H.p0 + i] = out[i];
+  for (int i = threadIdx.x; i < H.nz; i += kRT) vals[H.p0 + i] = out[i];
 }
 
 }  // namespace
 
 void TilePlan::release(Ctx* c) {
   hdr.release(c);
-  elist.release(c);
-  cls.release(c);
-  firsts.release(c);
-  rest.release(c);
+  blob.release(c);
   ntiles = 0;
   built = 0;
-  S = V = emax = 0;
+  S = V = emax = maxblob = maxnel = 0;
   nprograms = nfallback = 0;
 }
 
@@ -421,13 +451,17 @@ int build_tile_plan(Ctx* c, Pattern& P, int S, int V, const uint8_t* map) {
     ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
     d.release(c);
   }
-  // greedy tiles of consecutive columns within the limits
+  // greedy tiles of consecutive columns within the limits; a tile cut short
+  // by a limit keeps a multiple of 4 columns, so that on a structured mesh
+  // (DOFs of a grid line alternate between 2 or 4 kinds) the next tile starts
+  // at the same phase and translated tiles get equal programs
   std::vector<TileHdr> tiles;
   for (int64_t c0 = 0; c0 < ncol;) {
     int64_t c1 = c0 + 1;
     while (c1 < ncol && c1 - c0 < kTileMaxCols && colptr[c1 + 1] - colptr[c0] <= kTileMaxNz &&
            (int64_t)cq[c1 + 1] - cq[c0] <= kTileMaxContrib)
       ++c1;
+    if (c1 < ncol && c1 - c0 >= 8) c1 = c0 + ((c1 - c0) & ~(int64_t)3);
     TileHdr h{};
     h.col0 = (int32_t)c0;
     h.ncols = (int32_t)(c1 - c0);
@@ -471,28 +505,28 @@ int build_tile_plan(Ctx* c, Pattern& P, int S, int V, const uint8_t* map) {
         next.push_back(k);
       }
     }
-    if (!split) {
-      tiles.swap(next);
-      break;
-    }
     tiles.swap(next);
+    if (!split) break;
     T.hdr.release(c);
   }
   const int64_t nt = (int64_t)tiles.size();
+  // blob offsets of the programs (tiles within the limits)
+  int64_t total = 0;
+  for (TileHdr& h : tiles) {
+    h.boff = total;
+    if (!h.flags) total += blob_layout(h.nel, h.nz, h.nc).bytes;
+  }
   ELFEL_CUDA(c, cudaMemcpyAsync(T.hdr.p, tiles.data(), sizeof(TileHdr) * nt, cudaMemcpyHostToDevice, c->stream));
   T.ntiles = nt;
-  ELFEL_TRY(T.elist.alloc(c, (size_t)(nt * T.emax)));
-  ELFEL_TRY(T.cls.alloc(c, (size_t)(nt * (kTileMaxClass + 2))));
-  ELFEL_TRY(T.firsts.alloc(c, (size_t)P.nnz));
-  ELFEL_TRY(T.rest.alloc(c, (size_t)std::max<int64_t>(1, P.nslots - P.nnz)));
-  tile_build_k<<<(unsigned)nt, kTT, 0, c->stream>>>(T.hdr.p, nt, a, T.elist.p, T.cls.p, T.firsts.p, T.rest.p);
+  DBuf<uint8_t> full;
+  ELFEL_TRY(full.alloc(c, (size_t)std::max<int64_t>(16, total)));
+  tile_build_k<<<(unsigned)nt, kTT, 0, c->stream>>>(T.hdr.p, nt, a, full.p);
   ELFEL_LAUNCH_CHECK(c);
   // deduplicate equal programs: digests on the device, groups on the host,
   // then a word-for-word check of every tile against its representative
   DBuf<uint64_t> hash;
   ELFEL_TRY(hash.alloc(c, (size_t)nt));
-  tile_hash_k<<<(unsigned)nt, kTT, 0, c->stream>>>(T.hdr.p, nt, T.emax, T.elist.p, T.cls.p, T.firsts.p, T.rest.p,
-                                                   hash.p);
+  tile_hash_k<<<(unsigned)nt, kTT, 0, c->stream>>>(T.hdr.p, nt, full.p, hash.p);
   ELFEL_LAUNCH_CHECK(c);
   std::vector<uint64_t> hh((size_t)nt);
   ELFEL_CUDA(c, cudaMemcpyAsync(hh.data(), hash.p, sizeof(uint64_t) * nt, cudaMemcpyDeviceToHost, c->stream));
@@ -501,7 +535,7 @@ int build_tile_plan(Ctx* c, Pattern& P, int S, int V, const uint8_t* map) {
   hash.release(c);
   std::unordered_map<uint64_t, int32_t> first;
   first.reserve((size_t)nt);
-  int64_t nprog = 0, nfb = 0;
+  int64_t nfb = 0;
   for (int64_t t = 0; t < nt; ++t) {
     TileHdr& h = tiles[t];
     h.prog = (int32_t)t;
@@ -510,24 +544,69 @@ int build_tile_plan(Ctx* c, Pattern& P, int S, int V, const uint8_t* map) {
       continue;
     }
     auto it = first.find(hh[t]);
-    if (it == first.end()) {
+    if (it == first.end())
       first.emplace(hh[t], (int32_t)t);
-      ++nprog;
-    } else {
+    else
       h.prog = it->second;
-    }
   }
   ELFEL_CUDA(c, cudaMemcpyAsync(T.hdr.p, tiles.data(), sizeof(TileHdr) * nt, cudaMemcpyHostToDevice, c->stream));
-  tile_verify_k<<<(unsigned)nt, kTT, 0, c->stream>>>(T.hdr.p, nt, T.emax, T.elist.p, T.cls.p, T.firsts.p, T.rest.p);
+  tile_verify_k<<<(unsigned)nt, kTT, 0, c->stream>>>(T.hdr.p, nt, full.p);
   ELFEL_LAUNCH_CHECK(c);
+  ELFEL_CUDA(c, cudaMemcpyAsync(tiles.data(), T.hdr.p, sizeof(TileHdr) * nt, cudaMemcpyDeviceToHost, c->stream));
   ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+  // keep the distinct programs only, each tile pointing at its program's copy
+  std::vector<int64_t> src, dst;
+  std::vector<int32_t> bytes;
+  std::vector<int64_t> newoff((size_t)nt, -1);
+  int64_t compact = 0;
+  int maxblob = 16, maxnel = 1;
+  for (int64_t t = 0; t < nt; ++t) {
+    const TileHdr& h = tiles[t];
+    if (h.flags || h.prog != t) continue;
+    const int b = blob_layout(h.nel, h.nz, h.nc).bytes;
+    src.push_back(h.boff);
+    dst.push_back(compact);
+    bytes.push_back(b);
+    newoff[t] = compact;
+    compact += b;
+    maxblob = std::max(maxblob, b);
+    maxnel = std::max(maxnel, h.nel);
+  }
+  for (int64_t t = 0; t < nt; ++t) {
+    TileHdr& h = tiles[t];
+    if (!h.flags) h.boff = newoff[h.prog];
+  }
+  const int64_t nprog = (int64_t)src.size();
+  ELFEL_TRY(T.blob.alloc(c, (size_t)std::max<int64_t>(16, compact)));
+  if (nprog) {
+    DBuf<int64_t> ds, dd;
+    DBuf<int32_t> db;
+    ELFEL_TRY(ds.alloc(c, (size_t)nprog));
+    ELFEL_TRY(dd.alloc(c, (size_t)nprog));
+    ELFEL_TRY(db.alloc(c, (size_t)nprog));
+    ELFEL_CUDA(c, cudaMemcpyAsync(ds.p, src.data(), sizeof(int64_t) * nprog, cudaMemcpyHostToDevice, c->stream));
+    ELFEL_CUDA(c, cudaMemcpyAsync(dd.p, dst.data(), sizeof(int64_t) * nprog, cudaMemcpyHostToDevice, c->stream));
+    ELFEL_CUDA(c, cudaMemcpyAsync(db.p, bytes.data(), sizeof(int32_t) * nprog, cudaMemcpyHostToDevice, c->stream));
+    blob_copy_k<<<(unsigned)nprog, 256, 0, c->stream>>>(ds.p, dd.p, db.p, full.p, T.blob.p);
+    ELFEL_LAUNCH_CHECK(c);
+    ELFEL_CUDA(c, cudaMemcpyAsync(T.hdr.p, tiles.data(), sizeof(TileHdr) * nt, cudaMemcpyHostToDevice, c->stream));
+    ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+    ds.release(c);
+    dd.release(c);
+    db.release(c);
+  }
+  full.release(c);
+  T.maxblob = maxblob;
+  T.maxnel = maxnel;
   T.nprograms = nprog;
   T.nfallback = nfb;
   T.built = 1;
   return ELFEL_OK;
 }
 
-static size_t tile_smem(const TilePlan& T) { return (size_t)T.emax * T.V * sizeof(double) + kTileMaxNz * sizeof(double); }
+static size_t tile_smem(const TilePlan& T) {
+  return (size_t)T.maxblob + (size_t)T.maxnel * T.V * sizeof(double) + kTileMaxNz * sizeof(double);
+}
 
 int tile_reduce(Ctx* c, const Pattern& P, const double* src, int t6r_bases, double* vals) {
   const TilePlan& T = P.tiles;
@@ -538,14 +617,14 @@ int tile_reduce(Ctx* c, const Pattern& P, const double* src, int t6r_bases, doub
     if (T.V != kT6RTable || T.S != 21) return fail(c, ELFEL_ERR_STATE, "tile plan is not for T6 bases");
     RecT6R r{src};
     ELFEL_CUDA(c, cudaFuncSetAttribute(tile_reduce_k<RecT6R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    tile_reduce_k<RecT6R><<<(unsigned)T.ntiles, kTT, sm, c->stream>>>(
-        T.hdr.p, T.emax, T.V, T.elist.p, T.cls.p, T.firsts.p, T.rest.p, P.cptr.p, P.contrib.p, r, vals);
+    tile_reduce_k<RecT6R><<<(unsigned)T.ntiles, kRT, sm, c->stream>>>(T.hdr.p, T.maxnel, T.V, T.maxblob, T.blob.p,
+                                                                       P.cptr.p, P.contrib.p, r, vals);
   } else {
     if (T.V != T.S) return fail(c, ELFEL_ERR_STATE, "tile plan is not for full records");
     RecFull r{src, T.S};
     ELFEL_CUDA(c, cudaFuncSetAttribute(tile_reduce_k<RecFull>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    tile_reduce_k<RecFull><<<(unsigned)T.ntiles, kTT, sm, c->stream>>>(
-        T.hdr.p, T.emax, T.V, T.elist.p, T.cls.p, T.firsts.p, T.rest.p, P.cptr.p, P.contrib.p, r, vals);
+    tile_reduce_k<RecFull><<<(unsigned)T.ntiles, kRT, sm, c->stream>>>(T.hdr.p, T.maxnel, T.V, T.maxblob, T.blob.p,
+                                                                        P.cptr.p, P.contrib.p, r, vals);
   }
   ELFEL_LAUNCH_CHECK(c);
   return ELFEL_OK;
