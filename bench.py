@@ -70,10 +70,14 @@ def serving_workload(n, seed=20261204):
     return [("T6" if t6[i] else "T3", int(N[i]), float(kappa[i]), float(Q[i])) for i in range(n)]
 
 
+SERVE_MEM_BUDGET = 96 << 30  # device bytes a server may hold in resident systems
+
+
 def run_stream(E, ctx, reqs, rate, method="pcg32_ir", batched=True, max_active=64, seed=7):
     """Serve reqs arriving as a Poisson stream of `rate` per second (rate None:
     all at t = 0, closed loop) on a fresh server; per-request latencies."""
-    srv = E.HeatServer(method, batched=batched, max_active=max_active, rtol=1e-10, ctx=ctx)
+    srv = E.HeatServer(method, batched=batched, max_active=max_active, rtol=1e-10, mem_budget=SERVE_MEM_BUDGET,
+                       ctx=ctx)
     n = len(reqs)
     if rate:
         arr = np.cumsum(np.random.default_rng(seed).exponential(1.0 / rate, n))
@@ -105,25 +109,33 @@ def run_stream(E, ctx, reqs, rate, method="pcg32_ir", batched=True, max_active=6
             "elements_total": int(sum(r["nel"] for r in done)), "server": st}
 
 
-def serve_bench(E, ctx, nreq, fracs, plain_sample):
+def serve_bench(E, ctx, nreq, fracs, rate_sample):
+    """The serving stream: capacity (closed loop, all nreq requests), the same
+    requests solved one at a time by the plain FP64 path, and p50/p99 latency
+    under Poisson arrivals at three rates (fractions of the measured capacity,
+    printed as absolute rates) on the first rate_sample requests."""
     reqs = serving_workload(nreq)
     run_stream(E, ctx, reqs[:16], None)  # warm-up: graphs, autotuner records
     cap = run_stream(E, ctx, reqs, None)
+    plain = run_stream(E, ctx, reqs, None, method="pcg64", batched=False)
     out = {"workload": f"{nreq} heat requests: unit square, N log-uniform [16,512], T3/T6 1:1, kappa U[0.5,2], "
                        f"Q U[-10,-1], T = 1 + x^2 + 2y^2 on the boundary, 3-point rule, FP32 CG + FP64 "
-                       f"residual replacement to 1e-10 (seeded; the first {nreq} of the stream)",
-           "closed_loop": cap, "capacity_solves_per_s": cap["solves_per_s"], "rates": []}
+                       f"residual replacement to 1e-10 (seeded)",
+           "closed_loop": cap, "capacity_solves_per_s": cap["solves_per_s"],
+           "plain_fp64_one_at_a_time": {"sample": f"the same {nreq} requests, closed loop, FP64 Jacobi-PCG to 1e-10",
+                                        "solves_per_s": plain["solves_per_s"], "makespan_s": plain["makespan_s"],
+                                        "p50_ms": plain["p50_ms"], "p99_ms": plain["p99_ms"],
+                                        "failed": plain["failed"]},
+           "speedup_vs_plain": cap["solves_per_s"] / plain["solves_per_s"],
+           "rate_sample": f"the first {min(rate_sample, nreq)} requests of the stream, Poisson arrivals",
+           "rates": []}
+    sub = reqs[:rate_sample]
     for f in fracs:
-        out["rates"].append(run_stream(E, ctx, reqs, f * cap["solves_per_s"]))
-    sub = reqs[:plain_sample]
-    plain = run_stream(E, ctx, sub, None, method="pcg64", batched=False)
-    same = run_stream(E, ctx, sub, None)
-    out["plain_fp64_one_at_a_time"] = {"sample": f"first {plain_sample} requests, closed loop",
-                                       "solves_per_s": plain["solves_per_s"], "makespan_s": plain["makespan_s"],
-                                       "failed": plain["failed"]}
-    out["batched_same_sample"] = {"solves_per_s": same["solves_per_s"], "makespan_s": same["makespan_s"],
-                                  "p50_ms": same["p50_ms"], "p99_ms": same["p99_ms"]}
-    out["speedup_vs_plain_same_sample"] = same["solves_per_s"] / plain["solves_per_s"]
+        r = run_stream(E, ctx, sub, f * cap["solves_per_s"])
+        r["fraction_of_capacity"] = f
+        out["rates"].append(r)
+    out["rates_summary"] = [{"offered_per_s": r["offered_rate_per_s"], "achieved_per_s": r["solves_per_s"],
+                             "p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"]} for r in out["rates"]]
     return out
 
 
@@ -462,9 +474,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=2, help="full-size CPU reference steps of the cpu_baseline")
     ap.add_argument("--no-serve", action="store_true")
-    ap.add_argument("--serve-requests", type=int, default=512, help="requests of the serving stream (4096: all)")
+    ap.add_argument("--serve-requests", type=int, default=4096, help="requests of the serving stream")
     ap.add_argument("--serve-rates", default="0.5,0.7,0.9", help="arrival rates as fractions of the capacity")
-    ap.add_argument("--serve-plain-sample", type=int, default=48)
+    ap.add_argument("--serve-rate-sample", type=int, default=1024,
+                    help="requests (from the start of the stream) of each Poisson-arrival pass")
     ap.add_argument("--probe-rates", action="store_true", help="print the device's FP64/FP32 FMA rates and exit")
     args = ap.parse_args()
     if args.steps is None:
@@ -705,7 +718,7 @@ def main():
     serve = None
     if not args.no_serve and rank == 0:
         fr = [float(x) for x in args.serve_rates.split(",") if x]
-        serve = serve_bench(E, ctx, args.serve_requests, fr, args.serve_plain_sample)
+        serve = serve_bench(E, ctx, args.serve_requests, fr, args.serve_rate_sample)
         serve["tuning"] = [t for t, _ in ctx.tuning()]
 
     # --- CPU baseline (oracle restatement on the host cores) --------------
