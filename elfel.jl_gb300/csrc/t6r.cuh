@@ -17,8 +17,16 @@ namespace elfel {
 // double range is the infinity of its sign, infinities and NaNs keep their
 // exponent, and subnormal values (below 2^-1022, negligible next to any entry
 // of an element record) become zero of their sign.
+// The sign flip is an explicit integer XOR: written as an XOR in C++ it is
+// recognised as a floating-point negation and issued on the FP64 pipe.
+__device__ __forceinline__ long long t6r_xor(long long a, long long m) {
+  long long r;
+  asm("xor.b64 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(m));
+  return r;
+}
+
 __device__ __forceinline__ double t6r_scale(double b, int code) {
-  const long long bits = __double_as_longlong(b) ^ (long long)(1ull << 63);  // -b
+  const long long bits = t6r_xor(__double_as_longlong(b), (long long)(1ull << 63));  // -b
   const long long sign = bits & (long long)(1ull << 63);
   const int ex = (int)((bits >> 52) & 0x7ff);
   const int m = code == 1 ? 2 : 3;
