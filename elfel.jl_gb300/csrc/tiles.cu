@@ -356,7 +356,7 @@ struct RecT6R {
 // One CTA per tile: the tile's program copied into shared memory while the
 // value table of its elements is staged beside it, one thread per nonzero in
 // count order, the tile's values written out in CSC order.
-constexpr int kRT = 128;                 // threads of tile_reduce_k
+constexpr int kRT = 64;                  // threads of tile_reduce_k
 constexpr int kRPer = kTileMaxNz / kRT;  // nonzeros per thread
 
 template <class Rec>
