@@ -590,10 +590,15 @@ def main():
     # without a reduce_F phase the integration kernel added the load vector
     # itself (midside DOFs read, the vector written) instead of writing records
     f_direct = "reduce_F" not in per
+    ntiles, nprog, nfb = am.tile_stats()
+    tiles = ntiles > 0  # a resident pattern's assemblies take the tile reduction (8 bases per element)
     design = {  # bytes each kernel itself must move per launch, as designed (its own inputs and outputs)
-        "integrate_heat": nel * 6 * 4 + mesh.nnodes * 16 + nel * 8 + nel * 21 * 8 +
+        "integrate_heat": nel * 6 * 4 + mesh.nnodes * 16 + nel * 8 + nel * (8 if tiles else 21) * 8 +
                           (nel * 3 * 4 + n * 8 if f_direct else nel * 6 * 8),
-        "reduce_K": (nnz_est + 1) * 4 + nslots * 4 + nel * 21 * 8 + nnz_est * 8,
+        # tiles: the bases (64 B per element, read once from DRAM) and the values; the
+        # programs stay in L2. Contributor lists: cptr, contributor indices, records, values
+        "reduce_K": (nel * 8 * 8 + nnz_est * 8) if tiles else
+                    ((nnz_est + 1) * 4 + nslots * 4 + nel * 21 * 8 + nnz_est * 8),
         "reduce_F": (n + 1) * 8 + (n + 1) * 4 + nel * 6 * 4 + nel * 6 * 8 + n * 8,
     }
     dom = max(per, key=per.get)
@@ -607,14 +612,19 @@ def main():
                        "design_gbs": (design[k] / (per[k] * 1e-3) / 1e9) if k in design and per[k] else None}
                    for k in per}
     # DRAM traffic of one launch of each kernel (dram__bytes_read.sum + dram__bytes_write.sum)
-    # measured with ncu on the 700 x 700 case of this workload (980,000 elements; heat_t6s_k<2, 1>
-    # adding the load vector 86.84 + 121.46 MB, heat_t6s_k<2, 0> writing load records 47.34 +
-    # 151.06 MB, reduce_win_k 426.95 + 155.19 MB, reduce_row0_dense_k 94.18 + 8.28 MB), scaled
-    # by the element count; writes still dirty in L2 when a kernel ends are not counted
-    TRAFFIC_PER_ELEMENT = {"integrate_heat": ((86.844672e6 + 121.461504e6) if f_direct else
-                                              (47.341056e6 + 151.063040e6)) / 980000,
-                           "reduce_K": (426.946560e6 + 155.187456e6) / 980000,
-                           "reduce_F": (94.176768e6 + 8.283392e6) / 980000}
+    # measured with ncu on the 700 x 700 case of this workload (980,000 elements), scaled by
+    # the element count; writes still dirty in L2 when a kernel ends are not counted.
+    # Tile path: heat_t6s_k<2, 1, 1> 86.54 + 31.55 MB, tile_reduce_k 65.93 + 124.55 MB.
+    # Contributor-list path: heat_t6s_k<2, 1> 86.84 + 121.46 MB (<2, 0> 47.34 + 151.06 MB),
+    # reduce_win_k 426.95 + 155.19 MB, reduce_row0_dense_k 94.18 + 8.28 MB.
+    if tiles:
+        TRAFFIC_PER_ELEMENT = {"integrate_heat": (86.536704e6 + 31.554816e6) / 980000,
+                               "reduce_K": (65.929984e6 + 124.554496e6) / 980000}
+    else:
+        TRAFFIC_PER_ELEMENT = {"integrate_heat": ((86.844672e6 + 121.461504e6) if f_direct else
+                                                  (47.341056e6 + 151.063040e6)) / 980000,
+                               "reduce_K": (426.946560e6 + 155.187456e6) / 980000,
+                               "reduce_F": (94.176768e6 + 8.283392e6) / 980000}
     traffic = TRAFFIC_PER_ELEMENT[dom] * nel if dom in TRAFFIC_PER_ELEMENT else None
     for k, row in kernel_rows.items():
         row["traffic"] = TRAFFIC_PER_ELEMENT[k] * nel if k in TRAFFIC_PER_ELEMENT else None
@@ -624,12 +634,12 @@ def main():
                 "alg_bytes_what": "one assembly: connectivity + coordinates + conductivity + K values + F, once each "
                                   "(264 B/element); achieved = these bytes / the dominant kernel's mean CUDA-event "
                                   "time",
-                "traffic_source": "ncu DRAM bytes of the kernel at 980,000 elements, scaled per element",
+                "traffic_source": "ncu DRAM bytes of the kernel at 980,000 elements, scaled per element "
+                                  "(profiles/tile_reduce_T6_700.md)",
                 "assembly": {"alg_bytes": asm_bytes, "achieved": asm_bytes / t_step / 1e9,
                              "frac": asm_bytes / t_step / 1e9 / hbm, "what": "the same bytes / the whole step"},
                 "kernels": kernel_rows}
 
-    ntiles, nprog, nfb = am.tile_stats()
     roofline["tile_plan"] = {"tiles": ntiles, "programs": nprog, "fallback_tiles": nfb}
 
     # --- e2e through the C ABI from pinned host buffers -------------------
