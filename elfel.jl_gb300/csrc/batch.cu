@@ -205,9 +205,11 @@ __device__ __forceinline__ void for_items(const BSys* __restrict__ sys, const in
 }
 
 // spmv slot: CG step length, or the FP64 residual of a replacement.
-template <bool IR>
-__global__ void __launch_bounds__(kBlk, 5) b_spmv_k(const BSys* __restrict__ sys, const int4* __restrict__ items,
-                                                 const int* __restrict__ nitems_total) {
+// COH: inside the persistent kernel, whose other blocks write p and x64
+// between the phases (gathers through L2, not the read-only path).
+template <bool IR, bool COH>
+__device__ __forceinline__ void phase_spmv(const BSys* __restrict__ sys, const int4* __restrict__ items,
+                                           const int* __restrict__ nitems_total) {
   __shared__ double wsum[kItemMax * 4 * kWarps];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for_items(sys, items, nitems_total, [&](const int4& it, const BSys& S) {
@@ -221,8 +223,8 @@ __global__ void __launch_bounds__(kBlk, 5) b_spmv_k(const BSys* __restrict__ sys
           if (s < S.A.nslices) {
             const bool in = row < S.A.nrows;
             const float xi = in ? S.p32[row] : 0.f;
-            const float acc = S.A.d16 ? sell_row_acc<float, true, true>(S.A, S.v32, S.p32, s, lane, xi)
-                                      : sell_row_acc<float, false, true>(S.A, S.v32, S.p32, s, lane, xi);
+            const float acc = S.A.d16 ? sell_row_acc<float, true, true, COH>(S.A, S.v32, S.p32, s, lane, xi)
+                                      : sell_row_acc<float, false, true, COH>(S.A, S.v32, S.p32, s, lane, xi);
             if (in) {
               S.q32[row] = acc;
               pq = acc * xi;
@@ -248,8 +250,8 @@ __global__ void __launch_bounds__(kBlk, 5) b_spmv_k(const BSys* __restrict__ sys
           const int64_t row = s * 32 + lane;
           double rr = 0.0;
           if (s < S.A.nslices) {
-            const double acc = S.A.d16 ? sell_row_resid<true>(S.A, S.v64, S.x64, s, lane)
-                                       : sell_row_resid<false>(S.A, S.v64, S.x64, s, lane);
+            const double acc = S.A.d16 ? sell_row_resid<true, COH>(S.A, S.v64, S.x64, s, lane)
+                                       : sell_row_resid<false, COH>(S.A, S.v64, S.x64, s, lane);
             if (row < S.A.nrows) {
               const double rv = S.b64[row] - acc;
               S.r64[row] = rv;
@@ -286,8 +288,8 @@ __global__ void __launch_bounds__(kBlk, 5) b_spmv_k(const BSys* __restrict__ sys
         const int64_t row = s * 32 + lane;
         double pq = 0.0;
         if (s < S.A.nslices) {
-          const double acc = S.A.d16 ? sell_row_acc<double, true, false>(S.A, S.v64, S.p64, s, lane, 0.0)
-                                     : sell_row_acc<double, false, false>(S.A, S.v64, S.p64, s, lane, 0.0);
+          const double acc = S.A.d16 ? sell_row_acc<double, true, false, COH>(S.A, S.v64, S.p64, s, lane, 0.0)
+                                     : sell_row_acc<double, false, false, COH>(S.A, S.v64, S.p64, s, lane, 0.0);
           if (row < S.A.nrows) {
             S.q64[row] = acc;
             pq = acc * S.p64[row];
@@ -306,10 +308,16 @@ __global__ void __launch_bounds__(kBlk, 5) b_spmv_k(const BSys* __restrict__ sys
   });
 }
 
+template <bool IR>
+__global__ void __launch_bounds__(kBlk, 5) b_spmv_k(const BSys* __restrict__ sys, const int4* __restrict__ items,
+                                                 const int* __restrict__ nitems_total) {
+  phase_spmv<IR, false>(sys, items, nitems_total);
+}
+
 // update slot: x, r, z and beta; or the restart after a replacement.
 template <bool IR>
-__global__ void __launch_bounds__(kBlk) b_update_k(const BSys* __restrict__ sys, const int4* __restrict__ items,
-                                                   const int* __restrict__ nitems_total) {
+__device__ __forceinline__ void phase_update(const BSys* __restrict__ sys, const int4* __restrict__ items,
+                                             const int* __restrict__ nitems_total) {
   __shared__ double wsum[kItemMax * 4 * kWarps];
   for_items(sys, items, nitems_total, [&](const int4& it, const BSys& S) {
     const int mode = S.st[I_MODE];
@@ -445,10 +453,16 @@ __global__ void __launch_bounds__(kBlk) b_update_k(const BSys* __restrict__ sys,
   });
 }
 
+template <bool IR>
+__global__ void __launch_bounds__(kBlk) b_update_k(const BSys* __restrict__ sys, const int4* __restrict__ items,
+                                                   const int* __restrict__ nitems_total) {
+  phase_update<IR>(sys, items, nitems_total);
+}
+
 // p slot: p = z + beta p; in M_FOLD also x64 += s x32, x32 = 0.
 template <bool IR>
-__global__ void __launch_bounds__(kBlk) b_p_k(const BSys* __restrict__ sys, const int4* __restrict__ items,
-                                              const int* __restrict__ nitems_total) {
+__device__ __forceinline__ void phase_p(const BSys* __restrict__ sys, const int4* __restrict__ items,
+                                        const int* __restrict__ nitems_total) {
   for_items(sys, items, nitems_total, [&](const int4& it, const BSys& S) {
     const int mode = S.st[I_MODE];
     if (IR) {
@@ -470,6 +484,75 @@ __global__ void __launch_bounds__(kBlk) b_p_k(const BSys* __restrict__ sys, cons
         S.p64[row] = S.z64[row] + beta * S.p64[row];
     }
   });
+}
+
+template <bool IR>
+__global__ void __launch_bounds__(kBlk) b_p_k(const BSys* __restrict__ sys, const int4* __restrict__ items,
+                                              const int* __restrict__ nitems_total) {
+  phase_p<IR>(sys, items, nitems_total);
+}
+
+// ------------------------------------------------------------------ persistent form
+// (ELFEL_BATCH_PERSIST=1) One cooperative launch runs `iters` iterations of
+// every active system: the three phases of an iteration in sequence,
+// separated by a grid barrier; the arithmetic is that of the three kernels,
+// so the iterates are the same bits.
+// The barrier is a counter and a generation word; a block that waits longer
+// than kBarSpins polls (about a second) records the timeout in err and
+// every block leaves the kernel (err also stops the waiting of the others).
+// The host reads err after the launch and fails the step.
+struct GridBar {
+  unsigned* count;
+  unsigned* gen;
+  int* err;
+};
+constexpr unsigned kBarSpins = 1u << 24;
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ bool grid_sync(const GridBar& gb) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned g = ld_acquire_u32(gb.gen);
+    __threadfence();  // this block's writes before its arrival
+    if (atomicAdd(gb.count, 1u) == gridDim.x - 1u) {
+      atomicExch(gb.count, 0u);
+      __threadfence();
+      atomicAdd(gb.gen, 1u);
+    } else {
+      unsigned spins = 0;
+      while (ld_acquire_u32(gb.gen) == g) {
+        if (*(volatile int*)gb.err) break;
+        if (++spins > kBarSpins) {
+          atomicExch(gb.err, 1);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();  // the other blocks' writes before ours reads
+    ok = *(volatile int*)gb.err == 0;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+template <bool IR>
+__global__ void __launch_bounds__(kBlk) b_persist_k(const BSys* __restrict__ sys, const int4* __restrict__ items,
+                                                    const int* __restrict__ nitems_total, int iters, GridBar gb) {
+  for (int k = 0; k < iters; ++k) {
+    phase_spmv<IR, true>(sys, items, nitems_total);
+    if (!grid_sync(gb)) return;
+    phase_update<IR>(sys, items, nitems_total);
+    if (!grid_sync(gb)) return;
+    phase_p<IR>(sys, items, nitems_total);
+    if (!grid_sync(gb)) return;
+  }
 }
 
 // Start of one system (its own launch, before it joins the item map): x = 0,
@@ -589,6 +672,10 @@ struct elfel_batch {
   std::vector<GridCfg> cfgs;
   std::vector<cudaGraphExec_t> graphs;
   int occ_spmv = 1, occ_vec = 1;
+  // the persistent form (b_persist_k): its resident blocks per SM and the
+  // grid barrier's words (count, generation, error)
+  int persist = 0, occ_persist = 1;
+  DBuf<unsigned> gbar;
   std::map<int, int> tuned;  // log2(tiles) bucket -> chosen configuration
   int64_t launches = 0, kernel_launches = 0;
 };
@@ -683,7 +770,10 @@ int read_states(elfel_batch* b) {
   Ctx* c = ctx_of(b);
   ELFEL_CUDA(c, cudaMemcpyAsync(b->hst.data(), b->st.p, sizeof(int) * b->hst.size(), cudaMemcpyDeviceToHost,
                                 c->stream));
+  unsigned bar[3] = {0, 0, 0};
+  if (b->persist) ELFEL_CUDA(c, cudaMemcpyAsync(bar, b->gbar.p, sizeof(bar), cudaMemcpyDeviceToHost, c->stream));
   ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (bar[2]) return fail(c, ELFEL_ERR_CUDA, "batch: a grid barrier of the persistent iteration kernel timed out");
   const auto now = std::chrono::steady_clock::now();
   for (int i = 0; i < b->cap; ++i) {
     Slot& s = b->slots[i];
@@ -851,7 +941,23 @@ int batch_step(elfel_batch* b, int32_t graphs, int32_t* active) {
   Ctx* c = ctx_of(b);
   cudaSetDevice(c->device);
   if (b->map_dirty) ELFEL_TRY(rebuild_map(b));
-  for (int gi = 0; gi < graphs && b->total_tiles > 0; ++gi) {
+  for (int gi = 0; b->persist && gi < graphs && b->total_tiles > 0; ++gi) {
+    // one cooperative launch of iters iterations (all blocks resident)
+    const BSys* sy = b->sys.p;
+    const int4* itp = b->items.p;
+    const int* ntp = b->ntot.p;
+    int iters = b->iters;
+    GridBar gb{b->gbar.p, b->gbar.p + 1, reinterpret_cast<int*>(b->gbar.p + 2)};
+    void* args[] = {(void*)&sy, (void*)&itp, (void*)&ntp, (void*)&iters, (void*)&gb};
+    const dim3 grid((unsigned)(c->sm_count * b->occ_persist)), block(kBlk);
+    if (b->method == ELFEL_PCG32_IR)
+      ELFEL_CUDA(c, cudaLaunchCooperativeKernel((const void*)b_persist_k<true>, grid, block, args, 0, c->stream));
+    else
+      ELFEL_CUDA(c, cudaLaunchCooperativeKernel((const void*)b_persist_k<false>, grid, block, args, 0, c->stream));
+    b->launches++;
+    b->kernel_launches++;
+  }
+  for (int gi = 0; !b->persist && gi < graphs && b->total_tiles > 0; ++gi) {
     const int bucket = bucket_of(b->total_tiles);
     auto it = b->tuned.find(bucket);
     if (it == b->tuned.end()) {
@@ -970,6 +1076,27 @@ extern "C" int elfel_batch_create(elfel_ctx* h, int32_t method, int32_t capacity
   o2 = std::max(o2, 1);
   b->occ_spmv = o1;
   b->occ_vec = o2;
+  // the persistent form when ELFEL_BATCH_PERSIST=1 (and the device can launch
+  // it cooperatively).  Measured on GB300 it is slower than the graphs of
+  // three kernels (its three grid barriers per iteration cost more than the
+  // launches they replace, and one grid serves all phases), so the graphs
+  // stay the default.
+  int coop = 0, op = 0;
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, c->device);
+  if (method == ELFEL_PCG32_IR)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&op, b_persist_k<true>, kBlk, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&op, b_persist_k<false>, kBlk, 0);
+  const char* pe = getenv("ELFEL_BATCH_PERSIST");
+  b->persist = (coop && op > 0 && pe && pe[0] == '1') ? 1 : 0;
+  b->occ_persist = std::max(op, 1);
+  if (b->persist) {
+    if ((rc = b->gbar.alloc(c, 4))) {
+      delete b;
+      return rc;
+    }
+    cudaMemsetAsync(b->gbar.p, 0, 4 * sizeof(unsigned), c->stream);
+  }
   b->cfgs = {{o1, o2}, {std::max(o1 / 2, 1), std::max(o2 / 2, 1)}, {2 * o1, o2}, {o1, 2 * o2}};
   b->graphs.assign(b->cfgs.size(), nullptr);
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
@@ -990,6 +1117,7 @@ extern "C" int elfel_batch_destroy(elfel_batch* b) {
     if (s.m) s.m->busy = 0;
   }
   drop_graphs(b);
+  b->gbar.release(c);
   b->sys.release(c);
   b->sc.release(c);
   b->st.release(c);

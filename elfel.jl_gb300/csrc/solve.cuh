@@ -182,12 +182,20 @@ __device__ __forceinline__ T xterm(const T xc, int c, int64_t row, T xi) {
   return (int64_t)c == row ? xi : xc - xi;
 }
 
+// A gathered entry of x: through the read-only path when x does not change
+// during the kernel, else (COH: a persistent kernel in which other blocks
+// write x between its phases) through L2.
+template <typename T, bool COH>
+__device__ __forceinline__ T xload(const T* p) {
+  return COH ? __ldcg(p) : __ldg(p);
+}
+
 // (A x)_row for row = s * 32 + lane of slice s (0 for lanes past the last
 // row); xi = x[row] in the difference form.  Eight entries per lane in
 // flight: all column and value loads of a group are issued before the
 // dependent gathers of x.
-template <typename T, bool D16, bool DIFF>
-__device__ __forceinline__ T sell_row_acc(const SellView& A, const T* __restrict__ v, const T* __restrict__ x,
+template <typename T, bool D16, bool DIFF, bool COH = false>
+__device__ __forceinline__ T sell_row_acc(const SellView& A, const T* __restrict__ v, const T* x,
                                           int64_t s, int lane, T xi) {
   const int64_t base = A.sptr[s] + lane;
   const int64_t row = s * 32 + lane;
@@ -204,7 +212,7 @@ __device__ __forceinline__ T sell_row_acc(const SellView& A, const T* __restrict
     for (int u = 0; u < 8; ++u) vv[u] = __ldcs(v + k + 32 * u);
     T xx[8];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) xx[u] = xterm<T, DIFF>(__ldg(x + cc[u]), cc[u], row, xi);
+    for (int u = 0; u < 8; ++u) xx[u] = xterm<T, DIFF>(xload<T, COH>(x + cc[u]), cc[u], row, xi);
     a0 += vv[0] * xx[0];
     a1 += vv[1] * xx[1];
     a2 += vv[2] * xx[2];
@@ -219,31 +227,31 @@ __device__ __forceinline__ T sell_row_acc(const SellView& A, const T* __restrict
     const int c0 = sell_col<D16>(A, k, row), c1 = sell_col<D16>(A, k + 32, row);
     const int c2 = sell_col<D16>(A, k + 64, row), c3 = sell_col<D16>(A, k + 96, row);
     const T v0 = __ldcs(v + k), v1 = __ldcs(v + k + 32), v2 = __ldcs(v + k + 64), v3 = __ldcs(v + k + 96);
-    a0 += v0 * xterm<T, DIFF>(__ldg(x + c0), c0, row, xi);
-    a1 += v1 * xterm<T, DIFF>(__ldg(x + c1), c1, row, xi);
-    a2 += v2 * xterm<T, DIFF>(__ldg(x + c2), c2, row, xi);
-    a3 += v3 * xterm<T, DIFF>(__ldg(x + c3), c3, row, xi);
+    a0 += v0 * xterm<T, DIFF>(xload<T, COH>(x + c0), c0, row, xi);
+    a1 += v1 * xterm<T, DIFF>(xload<T, COH>(x + c1), c1, row, xi);
+    a2 += v2 * xterm<T, DIFF>(xload<T, COH>(x + c2), c2, row, xi);
+    a3 += v3 * xterm<T, DIFF>(xload<T, COH>(x + c3), c3, row, xi);
     j += 4;
   }
   for (; j < w; ++j) {
     const int64_t k = base + (int64_t)j * 32;
     const int cj = sell_col<D16>(A, k, row);
-    a0 += __ldcs(v + k) * xterm<T, DIFF>(__ldg(x + cj), cj, row, xi);
+    a0 += __ldcs(v + k) * xterm<T, DIFF>(xload<T, COH>(x + cj), cj, row, xi);
   }
   return (a0 + a1) + (a2 + a3);
 }
 
 // (A x)_row in FP64 for row = s * 32 + lane, one entry at a time (residuals).
-template <bool D16>
-__device__ __forceinline__ double sell_row_resid(const SellView& A, const double* __restrict__ v,
-                                                 const double* __restrict__ x, int64_t s, int lane) {
+template <bool D16, bool COH = false>
+__device__ __forceinline__ double sell_row_resid(const SellView& A, const double* __restrict__ v, const double* x,
+                                                 int64_t s, int lane) {
   const int64_t base = A.sptr[s] + lane;
   const int64_t row = s * 32 + lane;
   const int w = row < A.nrows ? A.sw[s] : 0;
   double acc = 0.0;
   for (int j = 0; j < w; ++j) {
     const int64_t k = base + (int64_t)j * 32;
-    acc += __ldcs(v + k) * __ldg(x + sell_col<D16>(A, k, row));
+    acc += __ldcs(v + k) * xload<double, COH>(x + sell_col<D16>(A, k, row));
   }
   return acc;
 }

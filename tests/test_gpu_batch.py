@@ -109,3 +109,28 @@ def test_batch_holds_system_and_errors(E, gpu):
     b.close()
     with pytest.raises(ValueError):
         E.BatchSolver("minres64")
+
+
+@pytest.mark.parametrize("method", ["pcg32_ir", "pcg64"])
+def test_persistent_form_same_bits(E, gpu, method, monkeypatch):
+    """The persistent form (one cooperative launch per group of iterations, grid
+    barriers between the phases, ELFEL_BATCH_PERSIST=1) iterates exactly as the
+    graphs of three kernels: the same solutions bit for bit and the same
+    iteration counts."""
+    rtol = 1e-10
+    probs = [make(E, *m) for m in MIX[:4]]
+
+    def run():
+        b = E.BatchSolver(method, capacity=8)
+        slots = [b.add(p["am"], p["T"], p["nu"], rtol=rtol) for p in probs]
+        out = b.run(graphs=2)
+        b.close()
+        return [out[s] for s in slots]
+
+    monkeypatch.setenv("ELFEL_BATCH_PERSIST", "0")
+    graph_res = run()
+    monkeypatch.setenv("ELFEL_BATCH_PERSIST", "1")
+    pers_res = run()
+    for (Tg, stg), (Tp, stp) in zip(graph_res, pers_res):
+        assert stp["converged"] and stp["relres"] <= rtol, stp
+        assert np.array_equal(Tg, Tp) and stg["iterations"] == stp["iterations"]
