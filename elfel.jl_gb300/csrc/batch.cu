@@ -3,9 +3,10 @@
 // together: every launch works on the row tiles of all active systems.
 //
 // Layout.  Each system keeps its own SELL-C-sigma matrix and Krylov vectors
-// (the one-system solver data).  A tile is kBlk consecutive permuted rows of
-// one system (kBlk / 32 SELL slices); a work item is a run of consecutive
-// tiles of one system.  A device item map lists the items of all active
+// (the one-system solver data).  A tile is sl * kBlk consecutive permuted
+// rows of one system (sl * kBlk / 32 SELL slices; each warp works through sl
+// of them and forms one partial; sl = 4 for large systems, 1 for small
+// ones); a work item is a run of consecutive tiles of one system.  A device item map lists the items of all active
 // systems; the three kernels of an iteration loop over it with a fixed grid,
 // so one captured CUDA graph of kIters iterations serves any mix of systems,
 // and systems join or leave between graph launches by rewriting the map.
@@ -55,6 +56,7 @@ struct BSys {
   double *x64, *r64, *z64, *p64, *q64;
   const double* b64;
   int64_t ntiles;
+  int sl, pad_;        // row groups of kBlk per tile (kSlSmall or kSlLarge: fixed per system by its size)
   double* part;        // ntiles x 4 partial sums
   unsigned* ticket;    // work items finished in the current kernel
   const int* nitems;   // work items of this system in the current map
@@ -64,6 +66,14 @@ struct BSys {
 
 constexpr int kItemMax = 32;  // tiles per work item (bounds the shared staging)
 constexpr int kWarps = kBlk / 32;
+// A tile: sl groups of kBlk rows; each warp accumulates its sl slices (or
+// rows) in registers and reduces once, so a tile partial costs one warp
+// reduction per sl * 32 rows.  sl is a property of the system (its size),
+// never of the mix: large systems take kSlLarge (fewer reductions), small
+// ones kSlSmall (no empty row groups).
+constexpr int kSlSmall = 1, kSlLarge = 4;
+constexpr int64_t kSlLargeRows = 65536;  // unknowns from which a system takes kSlLarge
+constexpr int kTileRowsMax = kSlLarge * kBlk;
 
 // Warp sums of the warp's NV per-lane values (the warp's slice or rows of
 // tile jt of the item) in the working precision T, staged in shared memory
@@ -217,18 +227,20 @@ __device__ __forceinline__ void phase_spmv(const BSys* __restrict__ sys, const i
     if (IR && (mode == M_CG || mode == M_STARTED)) {
       {
         for (int64_t j = it.y; j < it.y + it.z; ++j) {
-          const int64_t s = j * (kBlk / 32) + wid;
-          const int64_t row = s * 32 + lane;
           float pq = 0.f, rp = 0.f;
-          if (s < S.A.nslices) {
-            const bool in = row < S.A.nrows;
-            const float xi = in ? S.p32[row] : 0.f;
-            const float acc = S.A.d16 ? sell_row_acc<float, true, true, COH>(S.A, S.v32, S.p32, s, lane, xi)
-                                      : sell_row_acc<float, false, true, COH>(S.A, S.v32, S.p32, s, lane, xi);
-            if (in) {
-              S.q32[row] = acc;
-              pq = acc * xi;
-              rp = S.r32[row] * xi;
+          for (int u = 0; u < S.sl; ++u) {
+            const int64_t s = (j * S.sl + u) * kWarps + wid;
+            const int64_t row = s * 32 + lane;
+            if (s < S.A.nslices) {
+              const bool in = row < S.A.nrows;
+              const float xi = in ? S.p32[row] : 0.f;
+              const float acc = S.A.d16 ? sell_row_acc<float, true, true, COH>(S.A, S.v32, S.p32, s, lane, xi)
+                                        : sell_row_acc<float, false, true, COH>(S.A, S.v32, S.p32, s, lane, xi);
+              if (in) {
+                S.q32[row] = acc;
+                pq += acc * xi;
+                rp += S.r32[row] * xi;
+              }
             }
           }
           float v[2] = {pq, rp};
@@ -246,16 +258,18 @@ __device__ __forceinline__ void phase_spmv(const BSys* __restrict__ sys, const i
       // the FP64 recurrence's claim of convergence
       {
         for (int64_t j = it.y; j < it.y + it.z; ++j) {
-          const int64_t s = j * (kBlk / 32) + wid;
-          const int64_t row = s * 32 + lane;
           double rr = 0.0;
-          if (s < S.A.nslices) {
-            const double acc = S.A.d16 ? sell_row_resid<true, COH>(S.A, S.v64, S.x64, s, lane)
-                                       : sell_row_resid<false, COH>(S.A, S.v64, S.x64, s, lane);
-            if (row < S.A.nrows) {
-              const double rv = S.b64[row] - acc;
-              S.r64[row] = rv;
-              rr = rv * rv;
+          for (int u = 0; u < S.sl; ++u) {
+            const int64_t s = (j * S.sl + u) * kWarps + wid;
+            const int64_t row = s * 32 + lane;
+            if (s < S.A.nslices) {
+              const double acc = S.A.d16 ? sell_row_resid<true, COH>(S.A, S.v64, S.x64, s, lane)
+                                         : sell_row_resid<false, COH>(S.A, S.v64, S.x64, s, lane);
+              if (row < S.A.nrows) {
+                const double rv = S.b64[row] - acc;
+                S.r64[row] = rv;
+                rr += rv * rv;
+              }
             }
           }
           double v[1] = {rr};
@@ -284,15 +298,17 @@ __device__ __forceinline__ void phase_spmv(const BSys* __restrict__ sys, const i
       }
     } else if (!IR && (mode == M_CG || mode == M_STARTED)) {
       for (int64_t j = it.y; j < it.y + it.z; ++j) {
-        const int64_t s = j * (kBlk / 32) + wid;
-        const int64_t row = s * 32 + lane;
         double pq = 0.0;
-        if (s < S.A.nslices) {
-          const double acc = S.A.d16 ? sell_row_acc<double, true, false, COH>(S.A, S.v64, S.p64, s, lane, 0.0)
-                                     : sell_row_acc<double, false, false, COH>(S.A, S.v64, S.p64, s, lane, 0.0);
-          if (row < S.A.nrows) {
-            S.q64[row] = acc;
-            pq = acc * S.p64[row];
+        for (int u = 0; u < S.sl; ++u) {
+          const int64_t s = (j * S.sl + u) * kWarps + wid;
+          const int64_t row = s * 32 + lane;
+          if (s < S.A.nslices) {
+            const double acc = S.A.d16 ? sell_row_acc<double, true, false, COH>(S.A, S.v64, S.p64, s, lane, 0.0)
+                                       : sell_row_acc<double, false, false, COH>(S.A, S.v64, S.p64, s, lane, 0.0);
+            if (row < S.A.nrows) {
+              S.q64[row] = acc;
+              pq += acc * S.p64[row];
+            }
           }
         }
         double v[1] = {pq};
@@ -327,19 +343,22 @@ __device__ __forceinline__ void phase_update(const BSys* __restrict__ sys, const
         const bool brk = !(pq > 0.0) || !isfinite(pq);
         const float alpha = brk ? 0.f : (float)S.sc[B_ALPHA];
         for (int64_t j = it.y; j < it.y + it.z; ++j) {
-          const int64_t row = j * kBlk + threadIdx.x;
           float prz = 0.f, prr = 0.f, pzo = 0.f;
-          if (row < S.A.nrows) {
-            const float pi = S.p32[row];
-            S.x32[row] += alpha * pi;
-            const float ro = S.r32[row];
-            const float ri = ro - alpha * S.q32[row];
-            S.r32[row] = ri;
-            const float zi = S.dinv32[row] * ri;
-            S.z32[row] = zi;
-            prz = ri * zi;
-            prr = ri * ri;
-            pzo = zi * ro;
+#pragma unroll
+          for (int u = 0; u < S.sl; ++u) {
+            const int64_t row = (j * S.sl + u) * kBlk + threadIdx.x;
+            if (row < S.A.nrows) {
+              const float pi = S.p32[row];
+              S.x32[row] += alpha * pi;
+              const float ro = S.r32[row];
+              const float ri = ro - alpha * S.q32[row];
+              S.r32[row] = ri;
+              const float zi = S.dinv32[row] * ri;
+              S.z32[row] = zi;
+              prz += ri * zi;
+              prr += ri * ri;
+              pzo += zi * ro;
+            }
           }
           float v[3] = {prz, prr, pzo};
           warp_part<3>(v, wsum, (int)(j - it.y));
@@ -374,15 +393,18 @@ __device__ __forceinline__ void phase_update(const BSys* __restrict__ sys, const
         const double inv = 1.0 / S.sc[B_SCALE];
         const int restart = S.st[I_RESTART];
         for (int64_t j = it.y; j < it.y + it.z; ++j) {
-          const int64_t row = j * kBlk + threadIdx.x;
           float prz = 0.f;
-          if (row < S.A.nrows) {
-            const float ri = (float)(S.r64[row] * inv);
-            S.r32[row] = ri;
-            const float zi = S.dinv32[row] * ri;
-            S.z32[row] = zi;
-            if (restart) S.p32[row] = zi;
-            prz = ri * zi;
+#pragma unroll
+          for (int u = 0; u < S.sl; ++u) {
+            const int64_t row = (j * S.sl + u) * kBlk + threadIdx.x;
+            if (row < S.A.nrows) {
+              const float ri = (float)(S.r64[row] * inv);
+              S.r32[row] = ri;
+              const float zi = S.dinv32[row] * ri;
+              S.z32[row] = zi;
+              if (restart) S.p32[row] = zi;
+              prz += ri * zi;
+            }
           }
           float v[1] = {prz};
           warp_part<1>(v, wsum, (int)(j - it.y));
@@ -399,16 +421,19 @@ __device__ __forceinline__ void phase_update(const BSys* __restrict__ sys, const
       const bool brk = !(pq > 0.0) || !isfinite(pq);
       const double alpha = brk ? 0.0 : S.sc[B_ALPHA];
       for (int64_t j = it.y; j < it.y + it.z; ++j) {
-        const int64_t row = j * kBlk + threadIdx.x;
         double prz = 0.0, prr = 0.0;
-        if (row < S.A.nrows) {
-          S.x64[row] += alpha * S.p64[row];
-          const double ri = S.r64[row] - alpha * S.q64[row];
-          S.r64[row] = ri;
-          const double zi = S.dinv64[row] * ri;
-          S.z64[row] = zi;
-          prz = ri * zi;
-          prr = ri * ri;
+#pragma unroll
+        for (int u = 0; u < S.sl; ++u) {
+          const int64_t row = (j * S.sl + u) * kBlk + threadIdx.x;
+          if (row < S.A.nrows) {
+            S.x64[row] += alpha * S.p64[row];
+            const double ri = S.r64[row] - alpha * S.q64[row];
+            S.r64[row] = ri;
+            const double zi = S.dinv64[row] * ri;
+            S.z64[row] = zi;
+            prz += ri * zi;
+            prr += ri * ri;
+          }
         }
         double v[2] = {prz, prr};
         warp_part<2>(v, wsum, (int)(j - it.y));
@@ -431,15 +456,17 @@ __device__ __forceinline__ void phase_update(const BSys* __restrict__ sys, const
       }
     } else if (mode == M_RESTART) {
       // restart from the true residual: z = D r, p = z
-      double prz = 0.0;
       for (int64_t j = it.y; j < it.y + it.z; ++j) {
-        const int64_t row = j * kBlk + threadIdx.x;
-        prz = 0.0;
-        if (row < S.A.nrows) {
-          const double zi = S.dinv64[row] * S.r64[row];
-          S.z64[row] = zi;
-          S.p64[row] = zi;
-          prz = S.r64[row] * zi;
+        double prz = 0.0;
+#pragma unroll
+        for (int u = 0; u < S.sl; ++u) {
+          const int64_t row = (j * S.sl + u) * kBlk + threadIdx.x;
+          if (row < S.A.nrows) {
+            const double zi = S.dinv64[row] * S.r64[row];
+            S.z64[row] = zi;
+            S.p64[row] = zi;
+            prz += S.r64[row] * zi;
+          }
         }
         double v[1] = {prz};
         warp_part<1>(v, wsum, (int)(j - it.y));
@@ -469,8 +496,8 @@ __device__ __forceinline__ void phase_p(const BSys* __restrict__ sys, const int4
       if (mode != M_CG && mode != M_FOLD) return;
       const float beta = (float)S.sc[B_BETA];
       const double s = S.sc[B_SCALE];
-      for (int64_t row = (int64_t)it.y * kBlk + threadIdx.x; row < (int64_t)(it.y + it.z) * kBlk && row < S.A.nrows;
-           row += kBlk) {
+      for (int64_t row = (int64_t)it.y * S.sl * kBlk + threadIdx.x;
+           row < (int64_t)(it.y + it.z) * S.sl * kBlk && row < S.A.nrows; row += kBlk) {
         S.p32[row] = S.z32[row] + beta * S.p32[row];
         if (mode == M_FOLD) {
           S.x64[row] += s * (double)S.x32[row];
@@ -479,8 +506,8 @@ __device__ __forceinline__ void phase_p(const BSys* __restrict__ sys, const int4
       }
     } else if (mode == M_CG) {
       const double beta = S.sc[B_BETA];
-      for (int64_t row = (int64_t)it.y * kBlk + threadIdx.x; row < (int64_t)(it.y + it.z) * kBlk && row < S.A.nrows;
-           row += kBlk)
+      for (int64_t row = (int64_t)it.y * S.sl * kBlk + threadIdx.x;
+           row < (int64_t)(it.y + it.z) * S.sl * kBlk && row < S.A.nrows; row += kBlk)
         S.p64[row] = S.z64[row] + beta * S.p64[row];
     }
   });
@@ -564,33 +591,37 @@ __global__ void __launch_bounds__(kBlk) b_init_k(const BSys* __restrict__ sysp, 
   const BSys& S = *sysp;
   const double bn2 = *bn2p;
   for (int64_t j = blockIdx.x; j < S.ntiles; j += gridDim.x) {
-    const int64_t row = j * kBlk + threadIdx.x;
-    const bool in = row < S.A.nrows;
     if (IR) {
       const double inv = bn2 > 0.0 ? 1.0 / sqrt(bn2) : 0.0;
       float prz = 0.f;
-      if (in) {
-        S.x64[row] = 0.0;
-        S.x32[row] = 0.f;
-        const float ri = (float)(S.b64[row] * inv);
-        S.r32[row] = ri;
-        const float zi = S.dinv32[row] * ri;
-        S.z32[row] = zi;
-        S.p32[row] = zi;
-        prz = ri * zi;
+      for (int u = 0; u < S.sl; ++u) {
+        const int64_t row = (j * S.sl + u) * kBlk + threadIdx.x;
+        if (row < S.A.nrows) {
+          S.x64[row] = 0.0;
+          S.x32[row] = 0.f;
+          const float ri = (float)(S.b64[row] * inv);
+          S.r32[row] = ri;
+          const float zi = S.dinv32[row] * ri;
+          S.z32[row] = zi;
+          S.p32[row] = zi;
+          prz += ri * zi;
+        }
       }
       float v[1] = {prz};
       warp_part<1>(v, wsum, 0);
     } else {
       double prz = 0.0;
-      if (in) {
-        S.x64[row] = 0.0;
-        const double ri = S.b64[row];
-        S.r64[row] = ri;
-        const double zi = S.dinv64[row] * ri;
-        S.z64[row] = zi;
-        S.p64[row] = zi;
-        prz = ri * zi;
+      for (int u = 0; u < S.sl; ++u) {
+        const int64_t row = (j * S.sl + u) * kBlk + threadIdx.x;
+        if (row < S.A.nrows) {
+          S.x64[row] = 0.0;
+          const double ri = S.b64[row];
+          S.r64[row] = ri;
+          const double zi = S.dinv64[row] * ri;
+          S.z64[row] = zi;
+          S.p64[row] = zi;
+          prz += ri * zi;
+        }
       }
       double v[1] = {prz};
       warp_part<1>(v, wsum, 0);
@@ -852,7 +883,7 @@ int batch_add_dev(elfel_batch* b, elfel_sysmat* m, const double* F, const double
   if (nu < 0 || nu > m->nrow || !T) return fail(c, ELFEL_ERR_ARG, "batch_add: nu outside 0..%lld", (long long)m->nrow);
   if (!F && !m->has_rhs) return fail(c, ELFEL_ERR_ARG, "batch_add: no right-hand side");
   if (!(rtol > 0.0) || maxit < 1) return fail(c, ELFEL_ERR_ARG, "batch_add: rtol > 0 and maxit >= 1 required");
-  if (nu > (int64_t)0x7fffffff - kBlk) return fail(c, ELFEL_ERR_ARG, "batch_add: system too large");
+  if (nu > (int64_t)0x7fffffff - kTileRowsMax) return fail(c, ELFEL_ERR_ARG, "batch_add: system too large");
   int k = -1;
   for (int i = 0; i < b->cap; ++i)
     if (b->slots[i].state == 0) {
@@ -868,7 +899,8 @@ int batch_add_dev(elfel_batch* b, elfel_sysmat* m, const double* F, const double
   s.m = m;
   s.nu = nu;
   s.rtol = rtol;
-  s.ntiles = (nu + kBlk - 1) / kBlk;
+  const int sl = nu >= kSlLargeRows ? kSlLarge : kSlSmall;
+  s.ntiles = (nu + (int64_t)sl * kBlk - 1) / ((int64_t)sl * kBlk);
   s.t_add = std::chrono::steady_clock::now();
   if (nu > 0) {
     ELFEL_TRY(lift_rhs(m, F, T, t_dev));
@@ -896,6 +928,7 @@ int batch_add_dev(elfel_batch* b, elfel_sysmat* m, const double* F, const double
   d.q64 = S->q64.p;
   d.b64 = S->b64.p;
   d.ntiles = s.ntiles;
+  d.sl = sl;
   d.part = s.part.p;
   d.ticket = b->tickets.p + k;
   d.nitems = b->nitems.p + k;
