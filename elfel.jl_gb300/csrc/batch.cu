@@ -5,11 +5,12 @@
 // Layout.  Each system keeps its own SELL-C-sigma matrix and Krylov vectors
 // (the one-system solver data).  A tile is sl * kBlk consecutive permuted
 // rows of one system (sl * kBlk / 32 SELL slices; each warp works through sl
-// of them and forms one partial; sl = 4 for large systems, 1 for small
-// ones); a work item is a run of consecutive tiles of one system.  A device item map lists the items of all active
-// systems; the three kernels of an iteration loop over it with a fixed grid,
-// so one captured CUDA graph of kIters iterations serves any mix of systems,
-// and systems join or leave between graph launches by rewriting the map.
+// of them and forms one partial; sl = 8 from 2M unknowns, 4 from 64k, 1
+// below); a work item is a run of consecutive tiles of one system.  A device
+// item map lists the items of all active systems; the three kernels of an
+// iteration loop over it with a fixed grid, so one captured CUDA graph of
+// kIters iterations serves any mix of systems, and systems join or leave
+// between graph launches by rewriting the map.
 //
 // Reductions are per system and deterministic: each tile writes its partial
 // sums (a fixed tree inside the tile), and the block that completes a
@@ -56,7 +57,7 @@ struct BSys {
   double *x64, *r64, *z64, *p64, *q64;
   const double* b64;
   int64_t ntiles;
-  int sl, pad_;        // row groups of kBlk per tile (kSlSmall or kSlLarge: fixed per system by its size)
+  int sl, pad_;        // row groups of kBlk per tile (1, 4 or 8: fixed per system by its size)
   double* part;        // ntiles x 4 partial sums
   unsigned* ticket;    // work items finished in the current kernel
   const int* nitems;   // work items of this system in the current map
@@ -69,11 +70,18 @@ constexpr int kWarps = kBlk / 32;
 // A tile: sl groups of kBlk rows; each warp accumulates its sl slices (or
 // rows) in registers and reduces once, so a tile partial costs one warp
 // reduction per sl * 32 rows.  sl is a property of the system (its size),
-// never of the mix: large systems take kSlLarge (fewer reductions), small
-// ones kSlSmall (no empty row groups).
-constexpr int kSlSmall = 1, kSlLarge = 4;
-constexpr int64_t kSlLargeRows = 65536;  // unknowns from which a system takes kSlLarge
+// never of the mix: large systems take more row groups (fewer reductions and
+// partials), small ones fewer (no empty row groups).  Measured on the heat
+// serving stream (up to about 1M unknowns) and a 4M-unknown system, 16 row
+// groups were slower than 8 on both.
+constexpr int kSlSmall = 1, kSlMid = 4, kSlLarge = 8;
+constexpr int64_t kSlMidRows = 65536;     // unknowns from which a system takes kSlMid
+constexpr int64_t kSlLargeRows = 1 << 21; // unknowns from which a system takes kSlLarge
 constexpr int kTileRowsMax = kSlLarge * kBlk;
+
+static int tile_row_groups(int64_t nu) {
+  return nu >= kSlLargeRows ? kSlLarge : nu >= kSlMidRows ? kSlMid : kSlSmall;
+}
 
 // Warp sums of the warp's NV per-lane values (the warp's slice or rows of
 // tile jt of the item) in the working precision T, staged in shared memory
@@ -899,7 +907,7 @@ int batch_add_dev(elfel_batch* b, elfel_sysmat* m, const double* F, const double
   s.m = m;
   s.nu = nu;
   s.rtol = rtol;
-  const int sl = nu >= kSlLargeRows ? kSlLarge : kSlSmall;
+  const int sl = tile_row_groups(nu);
   s.ntiles = (nu + (int64_t)sl * kBlk - 1) / ((int64_t)sl * kBlk);
   s.t_add = std::chrono::steady_clock::now();
   if (nu > 0) {
