@@ -590,7 +590,7 @@ def main():
     # without a reduce_F phase the integration kernel added the load vector
     # itself (midside DOFs read, the vector written) instead of writing records
     f_direct = "reduce_F" not in per
-    ntiles, nprog, nfb = am.tile_stats()
+    ntiles, nprog, nfb, nruns = am.tile_stats()
     tiles = ntiles > 0  # a resident pattern's assemblies take the tile reduction (8 bases per element)
     design = {  # bytes each kernel itself must move per launch, as designed (its own inputs and outputs)
         "integrate_heat": nel * 6 * 4 + mesh.nnodes * 16 + nel * 8 + nel * (8 if tiles else 21) * 8 +
@@ -640,7 +640,7 @@ def main():
                              "frac": asm_bytes / t_step / 1e9 / hbm, "what": "the same bytes / the whole step"},
                 "kernels": kernel_rows}
 
-    roofline["tile_plan"] = {"tiles": ntiles, "programs": nprog, "fallback_tiles": nfb}
+    roofline["tile_plan"] = {"tiles": ntiles, "programs": nprog, "fallback_tiles": nfb, "runs": nruns}
 
     # --- e2e through the C ABI from pinned host buffers -------------------
     conn_h = torch.from_numpy(np.ascontiguousarray(mesh.conn)).pin_memory()

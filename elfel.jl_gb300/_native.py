@@ -168,7 +168,7 @@ SIGNATURES = {
     "elfel_block_dirichlet": (ctypes.c_int, [_vp, _dp, _dp]),
     "elfel_fused_tables": (ctypes.c_int, [_vp, _i64p, _dp, _i64p]),
     "elfel_fused_dims": (ctypes.c_int, [_vp, _i64p, _i64p, _i64p]),
-    "elfel_sysmat_tile_stats": (ctypes.c_int, [_vp, _i64p, _i64p, _i64p]),
+    "elfel_sysmat_tile_stats": (ctypes.c_int, [_vp, _i64p, _i64p, _i64p, _i64p]),
     "elfel_fused_setup_numbered": (ctypes.c_int, [_vp, _vp, _vp, _vp, _i64p, _i64p, _i64p]),
     "elfel_number_dofs": (ctypes.c_int, [_vp, ctypes.c_int32, _i64p, ctypes.POINTER(ctypes.c_int32),
                                          ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(_i64p), _i64p]),

@@ -378,12 +378,12 @@ class SysmatAssemblerGPU:
         return self
 
     def tile_stats(self):
-        """(tiles, distinct tile programs, tiles on the contributor-list path) of the K pattern's
-        tile reduction plan; zeros before the plan is built."""
-        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        """(tiles, distinct tile programs, tiles on the contributor-list path, runs of tiles of one
+        program) of the K pattern's tile reduction plan; zeros before the plan is built."""
+        a, b, c, d = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
         self._hd.check(self._hd.lib.elfel_sysmat_tile_stats(self._hd.h, ctypes.byref(a), ctypes.byref(b),
-                                                            ctypes.byref(c)))
-        return a.value, b.value, c.value
+                                                            ctypes.byref(c), ctypes.byref(d)))
+        return a.value, b.value, c.value, d.value
 
     def set_geometry(self, xy):
         xy = N.f64(xy)

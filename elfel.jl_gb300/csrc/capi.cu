@@ -789,12 +789,14 @@ extern "C" int elfel_fused_dims(elfel_sysmat* m, int64_t* nel, int64_t* nnodes, 
   return ELFEL_OK;
 }
 
-extern "C" int elfel_sysmat_tile_stats(elfel_sysmat* m, int64_t* ntiles, int64_t* nprograms, int64_t* nfallback) {
+extern "C" int elfel_sysmat_tile_stats(elfel_sysmat* m, int64_t* ntiles, int64_t* nprograms, int64_t* nfallback,
+                                       int64_t* nruns) {
   CHECK_M(m);
   const TilePlan& T = m->P.tiles;
   if (ntiles) *ntiles = T.built ? T.ntiles : 0;
   if (nprograms) *nprograms = T.built ? T.nprograms : 0;
   if (nfallback) *nfallback = T.built ? T.nfallback : 0;
+  if (nruns) *nruns = T.built ? T.nruns : 0;
   return ELFEL_OK;
 }
 

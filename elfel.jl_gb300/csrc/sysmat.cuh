@@ -211,6 +211,11 @@ struct TilePlan {
   int maxblob = 0;             // bytes of the largest program
   int maxnel = 0;              // elements of the largest tile
   int64_t ntiles = 0, nprograms = 0, nfallback = 0;
+  // runs of consecutive tiles that read one program (or are all beyond the
+  // limits), at most runlen tiles each: (first tile, tiles)
+  int64_t nruns = 0;
+  int runlen = 0;
+  DBuf<int2> runs;
   DBuf<TileHdr> hdr;
   // the distinct programs, each 16-byte aligned: count-class starts (uint16),
   // element offsets from the tile's smallest element (int32, ascending),

@@ -331,6 +331,20 @@ struct RecFull {
 // The 8 bases of the exact-rational T6 record (64 bytes per element).
 struct RecT6R {
   const double* bases;
+  __device__ __forceinline__ void load(int64_t e, double2 (&x)[4]) const {
+    const double2* p = reinterpret_cast<const double2*>(bases + e * 8);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) x[k] = __ldg(p + k);
+  }
+  __device__ __forceinline__ static void expand(const double2 (&x)[4], double* v) {
+    double b[8];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      b[2 * k] = x[k].x;
+      b[2 * k + 1] = x[k].y;
+    }
+    t6r_table(b, v);
+  }
   __device__ __forceinline__ void stage(int64_t e, double* v) const {
     const double2* p = reinterpret_cast<const double2*>(bases + e * 8);
     double b[8];
@@ -353,12 +367,41 @@ struct RecT6R {
   }
 };
 
+constexpr int kRT = 64;                  // threads of tile_reduce_k and tile_run_k
+constexpr int kTileRun = 4;              // tiles per run of tile_run_k
+constexpr int kRPer = kTileMaxNz / kRT;  // nonzeros per thread
+
+// Adds of one tile: one thread per nonzero in count order (the program's
+// first codes), each summing its contributions in slot order from the value
+// table, the sums placed in CSC order in out.
+__device__ __forceinline__ void tile_adds(const uint8_t* sb, const BlobLayout& L, int nz, const double* tbl,
+                                          double* out) {
+  const uint16_t* cstart = reinterpret_cast<const uint16_t*>(sb);
+  const uint32_t* sf = reinterpret_cast<const uint32_t*>(sb + L.f);
+  const uint16_t* sr = reinterpret_cast<const uint16_t*>(sb + L.r);
+  int c = 1, rb = 0;  // class of the current nonzero and the start of its class's further codes
+#pragma unroll
+  for (int j = 0; j < kRPer; ++j) {
+    const int i = threadIdx.x + j * kRT;
+    if (i < nz) {
+      while (i >= cstart[c + 1]) {
+        rb += (cstart[c + 1] - cstart[c]) * (c - 1);
+        ++c;
+      }
+      const uint32_t f = sf[i];
+      const int n = cstart[c + 1] - cstart[c];
+      const uint16_t* r = sr + rb + (i - cstart[c]);
+      double s = tbl[f & 0xffffu];
+#pragma unroll 1
+      for (int k = 1; k < c; ++k) s = __dadd_rn(s, tbl[r[(k - 1) * n]]);
+      out[f >> 16] = s;
+    }
+  }
+}
+
 // One CTA per tile: the tile's program copied into shared memory while the
 // value table of its elements is staged beside it, one thread per nonzero in
 // count order, the tile's values written out in CSC order.
-constexpr int kRT = 64;                  // threads of tile_reduce_k
-constexpr int kRPer = kTileMaxNz / kRT;  // nonzeros per thread
-
 template <class Rec>
 __global__ void __launch_bounds__(kRT) tile_reduce_k(const TileHdr* __restrict__ hdr, int maxnel, int V, int maxblob,
                                                      const uint8_t* __restrict__ blob,
@@ -389,34 +432,87 @@ __global__ void __launch_bounds__(kRT) tile_reduce_k(const TileHdr* __restrict__
   const int32_t* gel = reinterpret_cast<const int32_t*>(blob + H.boff + L.el);
   for (int k = threadIdx.x; k < H.nel; k += kRT) rec.stage((int64_t)H.emin + __ldg(gel + k), tbl + k * V);
   __syncthreads();
-  const uint16_t* cstart = reinterpret_cast<const uint16_t*>(sb);
-  const uint32_t* sf = reinterpret_cast<const uint32_t*>(sb + L.f);
-  const uint16_t* sr = reinterpret_cast<const uint16_t*>(sb + L.r);
-  int c = 1, rb = 0;  // class of the current nonzero and the start of its class's further codes
-#pragma unroll
-  for (int j = 0; j < kRPer; ++j) {
-    const int i = threadIdx.x + j * kRT;
-    if (i < H.nz) {
-      while (i >= cstart[c + 1]) {
-        rb += (cstart[c + 1] - cstart[c]) * (c - 1);
-        ++c;
-      }
-      const uint32_t f = sf[i];
-      const int n = cstart[c + 1] - cstart[c];
-      const uint16_t* r = sr + rb + (i - cstart[c]);
-      double s = tbl[f & 0xffffu];
-#pragma unroll 1
-      for (int k = 1; k < c; ++k) s = __dadd_rn(s, tbl[r[(k - 1) * n]]);
-      out[f >> 16] = s;
-    }
-  }
+  tile_adds(sb, L, H.nz, tbl, out);
   __syncthreads();
   for (int i = threadIdx.x; i < H.nz; i += kRT) vals[H.p0 + i] = out[i];
+}
+
+// One CTA per run of consecutive tiles that read the same program (T6 bases).
+// The program is copied into shared memory once per run; a thread's elements
+// (positions in the program's element list) are the same in every tile of the
+// run, so the 8 bases of the next tile's elements are loaded into registers
+// before the current tile's adds and expanded into the value table after
+// them: the gather of tile t + 1 overlaps the adds of tile t. P elements per
+// thread (the run kernel is used when the largest tile has at most P * 64).
+template <int P>
+__global__ void __launch_bounds__(kRT) tile_run_k(const TileHdr* __restrict__ hdr, const int2* __restrict__ runs,
+                                                  int maxnel, int maxblob, const uint8_t* __restrict__ blob,
+                                                  const int32_t* __restrict__ cptr,
+                                                  const int32_t* __restrict__ contrib, RecT6R rec,
+                                                  double* __restrict__ vals) {
+  extern __shared__ uint4 smq[];  // program (maxblob bytes) | value table | values
+  const int2 run = runs[blockIdx.x];
+  const TileHdr H0 = hdr[run.x];
+  if (H0.flags) {
+    // tiles beyond the limits: every nonzero from its contributor list
+    for (int t = run.x; t < run.x + run.y; ++t) {
+      const TileHdr H = hdr[t];
+      if (H.flags & kTileEmpty) continue;
+      for (int i = threadIdx.x; i < H.nz; i += kRT) {
+        const int32_t b = cptr[H.p0 + i], e = cptr[H.p0 + i + 1];
+        double s = rec.value((uint32_t)contrib[b]);
+        for (int32_t k = b + 1; k < e; ++k) s = __dadd_rn(s, rec.value((uint32_t)contrib[k]));
+        vals[H.p0 + i] = s;
+      }
+    }
+    return;
+  }
+  const BlobLayout L = blob_layout(H0.nel, H0.nz, H0.nc);
+  const int nel = H0.nel, nz = H0.nz;
+  const int32_t* gel = reinterpret_cast<const int32_t*>(blob + H0.boff + L.el);
+  int eo[P];
+  double2 x[P][4];
+#pragma unroll
+  for (int p = 0; p < P; ++p) {
+    const int k = threadIdx.x + p * kRT;
+    eo[p] = k < nel ? __ldg(gel + k) : 0;
+    if (k < nel) rec.load((int64_t)H0.emin + eo[p], x[p]);
+  }
+  const uint4* src = reinterpret_cast<const uint4*>(blob + H0.boff);
+  for (int k = threadIdx.x; k < L.bytes / 16; k += kRT) smq[k] = __ldg(src + k);
+  const uint8_t* sb = reinterpret_cast<const uint8_t*>(smq);
+  double* tbl = reinterpret_cast<double*>(reinterpret_cast<uint8_t*>(smq) + maxblob);
+  double* out = tbl + (size_t)maxnel * kT6RTable;
+  int64_t p0 = H0.p0;
+  for (int t = 0; t < run.y; ++t) {
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+      const int k = threadIdx.x + p * kRT;
+      if (k < nel) RecT6R::expand(x[p], tbl + k * kT6RTable);
+    }
+    int64_t pn = 0;
+    if (t + 1 < run.y) {
+      const TileHdr* hn = hdr + run.x + t + 1;
+      pn = hn->p0;
+      const int64_t en = hn->emin;
+#pragma unroll
+      for (int p = 0; p < P; ++p)
+        if (threadIdx.x + p * kRT < nel) rec.load(en + eo[p], x[p]);
+    }
+    __syncthreads();  // the program and the table are in place; out is free
+    tile_adds(sb, L, nz, tbl, out);
+    __syncthreads();  // out is complete; the table is free
+    for (int i = threadIdx.x; i < nz; i += kRT) vals[p0 + i] = out[i];
+    p0 = pn;
+  }
 }
 
 }  // namespace
 
 void TilePlan::release(Ctx* c) {
+  runs.release(c);
+  nruns = 0;
+  runlen = 0;
   hdr.release(c);
   blob.release(c);
   ntiles = 0;
@@ -596,6 +692,27 @@ int build_tile_plan(Ctx* c, Pattern& P, int S, int V, const uint8_t* map) {
     db.release(c);
   }
   full.release(c);
+  // runs of consecutive tiles of one program (translated tiles of a
+  // structured mesh follow one another), or of consecutive tiles beyond the
+  // limits, at most kTileRun tiles each (ELFEL_TILE_RUN; 0: one CTA per tile)
+  int run_max = kTileRun;
+  if (const char* e = getenv("ELFEL_TILE_RUN")) run_max = std::max(0, std::min(1 << 20, atoi(e)));
+  if (run_max > 0) {
+    std::vector<int2> runs;
+    for (int64_t t = 0; t < nt;) {
+      const TileHdr& h = tiles[t];
+      int64_t u = t + 1;
+      while (u < nt && u - t < run_max && (h.flags ? tiles[u].flags != 0 : (!tiles[u].flags && tiles[u].prog == h.prog)))
+        ++u;
+      runs.push_back(make_int2((int)t, (int)(u - t)));
+      t = u;
+    }
+    T.nruns = (int64_t)runs.size();
+    T.runlen = run_max;
+    ELFEL_TRY(T.runs.alloc(c, runs.size()));
+    ELFEL_CUDA(c, cudaMemcpyAsync(T.runs.p, runs.data(), sizeof(int2) * runs.size(), cudaMemcpyHostToDevice, c->stream));
+    ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
   T.maxblob = maxblob;
   T.maxnel = maxnel;
   T.nprograms = nprog;
@@ -608,6 +725,30 @@ static size_t tile_smem(const TilePlan& T) {
   return (size_t)T.maxblob + (size_t)T.maxnel * T.V * sizeof(double) + kTileMaxNz * sizeof(double);
 }
 
+static bool tile_runs_ok(const TilePlan& T) { return T.nruns > 0 && T.maxnel <= 2 * kRT && T.V == kT6RTable; }
+
+// Runs [r0, r0 + nr) of the plan's run kernel on stream s (T6 bases).
+static int tile_reduce_runs(Ctx* c, const Pattern& P, const double* bases, double* vals, int64_t r0, int64_t nr,
+                            cudaStream_t s) {
+  const TilePlan& T = P.tiles;
+  if (!T.built || !tile_runs_ok(T) || T.S != 21) return fail(c, ELFEL_ERR_STATE, "tile runs without a T6 run plan");
+  if (r0 < 0 || nr < 0 || r0 + nr > T.nruns) return fail(c, ELFEL_ERR_ARG, "tile runs outside the plan");
+  if (nr == 0) return ELFEL_OK;
+  const size_t sm = tile_smem(T);
+  RecT6R r{bases};
+  if (T.maxnel <= kRT) {
+    ELFEL_CUDA(c, cudaFuncSetAttribute(tile_run_k<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    tile_run_k<1><<<(unsigned)nr, kRT, sm, s>>>(T.hdr.p, T.runs.p + r0, T.maxnel, T.maxblob, T.blob.p, P.cptr.p,
+                                                P.contrib.p, r, vals);
+  } else {
+    ELFEL_CUDA(c, cudaFuncSetAttribute(tile_run_k<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    tile_run_k<2><<<(unsigned)nr, kRT, sm, s>>>(T.hdr.p, T.runs.p + r0, T.maxnel, T.maxblob, T.blob.p, P.cptr.p,
+                                                P.contrib.p, r, vals);
+  }
+  ELFEL_LAUNCH_CHECK(c);
+  return ELFEL_OK;
+}
+
 int tile_reduce(Ctx* c, const Pattern& P, const double* src, int t6r_bases, double* vals) {
   const TilePlan& T = P.tiles;
   if (!T.built) return fail(c, ELFEL_ERR_STATE, "tile reduction without a plan");
@@ -616,6 +757,7 @@ int tile_reduce(Ctx* c, const Pattern& P, const double* src, int t6r_bases, doub
   if (t6r_bases) {
     if (T.V != kT6RTable || T.S != 21) return fail(c, ELFEL_ERR_STATE, "tile plan is not for T6 bases");
     RecT6R r{src};
+    if (tile_runs_ok(T)) return tile_reduce_runs(c, P, src, vals, 0, T.nruns, c->stream);
     ELFEL_CUDA(c, cudaFuncSetAttribute(tile_reduce_k<RecT6R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     tile_reduce_k<RecT6R><<<(unsigned)T.ntiles, kRT, sm, c->stream>>>(T.hdr.p, T.maxnel, T.V, T.maxblob, T.blob.p,
                                                                        P.cptr.p, P.contrib.p, r, vals);

@@ -249,9 +249,11 @@ ELFEL_API int elfel_fused_tables(elfel_sysmat* m, int64_t* conn, double* xy, int
 ELFEL_API int elfel_fused_dims(elfel_sysmat* m, int64_t* nel, int64_t* nnodes, int64_t* ndofs);
 /* The tile reduction plan of a fused system's K pattern (no counterpart in
  * the reference; built at a T6 heat pattern's second assembly): tiles, the
- * distinct tile programs they read, tiles summed from the contributor lists.
- * All zero when no plan is built. */
-ELFEL_API int elfel_sysmat_tile_stats(elfel_sysmat* m, int64_t* ntiles, int64_t* nprograms, int64_t* nfallback);
+ * distinct tile programs they read, tiles summed from the contributor lists,
+ * runs of consecutive tiles reading one program (one CTA each; 0 when the
+ * reduction runs one CTA per tile). All zero when no plan is built. */
+ELFEL_API int elfel_sysmat_tile_stats(elfel_sysmat* m, int64_t* ntiles, int64_t* nprograms, int64_t* nfallback,
+                                      int64_t* nruns);
 
 /* ------------------------------------------------------------------ error integrals
  * evaluate_pressure_error / evaluate_velocity_error of test/test_stokes.jl:438-496

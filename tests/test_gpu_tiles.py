@@ -42,7 +42,7 @@ def _assemble_twice(E, mesh, fesp, kappa):
     am = E.start(E.SysmatAssemblerGPU(), n, n)
     E.assemble_heat(am, E.FEIterator(fesp), E.QPIterator(fesp, {"kind": "default", "npts": 3}), kappa, -6.0)
     K1, F1 = E.finish(am), am.rhs().copy()
-    assert am.tile_stats() == (0, 0, 0)
+    assert am.tile_stats() == (0, 0, 0, 0)
     am.heat(None, -6.0)
     K2, F2 = E.finish(am), am.rhs().copy()
     am.heat(None, -6.0)
@@ -77,8 +77,8 @@ def test_tile_reduction_bits(E, O, gpu, case):
     fesp = heat_space(E, mesh, E.FEH1_T6())
     kappa = np.exp(np.random.default_rng(8).uniform(np.log(0.5), np.log(2.0), mesh.nel))
     am, (K1, F1), (K2, F2), K3 = _assemble_twice(E, mesh, fesp, kappa)
-    ntiles, nprog, nfb = am.tile_stats()
-    assert ntiles > 0 and nfb == 0
+    ntiles, nprog, nfb, nruns = am.tile_stats()
+    assert ntiles > 0 and nfb == 0 and 0 < nruns <= ntiles
     if name == "wide":
         assert 2 * nprog < ntiles  # translated tiles along the grid lines share their programs
     for K in (K2, K3):
@@ -97,9 +97,52 @@ def test_tile_reduction_beyond_limits(E, O, gpu):
     fesp = heat_space(E, mesh, E.FEH1_T6())
     kappa = np.linspace(0.5, 2.0, mesh.nel)
     am, (K1, F1), (K2, F2), K3 = _assemble_twice(E, mesh, fesp, kappa)
-    ntiles, nprog, nfb = am.tile_stats()
+    ntiles, nprog, nfb, nruns = am.tile_stats()
     assert nfb >= 1
     assert np.array_equal(_bits(K2.data), _bits(K1.data))
     assert np.array_equal(_bits(K3.data), _bits(K1.data))
     K0, F0 = heat_oracle(E, O, mesh, fesp, 3, kappa, -6.0)
     assert np.abs(K2.data - K0.data).max() <= 1e-12 * np.abs(K0.data).max()
+
+
+@pytest.mark.parametrize("run", ["0", "1", "3", "64"])
+@pytest.mark.parametrize("case", [CASES[1], CASES[4]], ids=["wide", "shuffled"])
+def test_tile_run_lengths_same_bits(E, O, gpu, monkeypatch, run, case):
+    """The run kernel (one CTA per run of consecutive tiles of one program,
+    the next tile's bases loaded during the current tile's adds) at several
+    run lengths, and the one-CTA-per-tile kernel (ELFEL_TILE_RUN=0), give the
+    contributor-list values bit for bit."""
+    monkeypatch.setenv("ELFEL_TILE_RUN", run)
+    name, nx, ny, orient, jit, shuffle = case
+    mesh = E.jitter(E.T6block(1.0, 1.0, nx, ny, orientation=orient), jit / max(nx, ny), seed=3)
+    if shuffle:
+        perm = np.random.default_rng(9).permutation(mesh.nel)
+        mesh = E.Mesh("T6", mesh.conn[perm], mesh.xy)
+    fesp = heat_space(E, mesh, E.FEH1_T6())
+    kappa = np.exp(np.random.default_rng(4).uniform(np.log(0.5), np.log(2.0), mesh.nel))
+    am, (K1, F1), (K2, F2), K3 = _assemble_twice(E, mesh, fesp, kappa)
+    ntiles, nprog, nfb, nruns = am.tile_stats()
+    if run == "0":
+        assert nruns == 0
+    else:
+        assert -(-ntiles // int(run)) <= nruns <= ntiles
+        if name == "wide" and run != "1":
+            assert nruns < ntiles  # consecutive translated tiles share a run
+    for K in (K2, K3):
+        assert np.array_equal(_bits(K.data), _bits(K1.data)), (name, run)
+    assert np.array_equal(_bits(F2), _bits(F1))
+
+
+def test_tile_run_beyond_limits(E, O, gpu, monkeypatch):
+    """Runs of tiles beyond the limits take the contributor lists in the run kernel."""
+    monkeypatch.setenv("ELFEL_TILE_RUN", "4")
+    conn, xy = _fan_t6(20)
+    mesh = E.Mesh("T6", conn, xy)
+    fesp = heat_space(E, mesh, E.FEH1_T6())
+    kappa = np.linspace(0.5, 2.0, mesh.nel)
+    am, (K1, F1), (K2, F2), K3 = _assemble_twice(E, mesh, fesp, kappa)
+    ntiles, nprog, nfb, nruns = am.tile_stats()
+    assert nfb >= 1 and nruns >= 1
+    assert np.array_equal(_bits(K2.data), _bits(K1.data))
+    assert np.array_equal(_bits(K3.data), _bits(K1.data))
+
