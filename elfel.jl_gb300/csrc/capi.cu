@@ -161,6 +161,16 @@ static void release_all(elfel_sysmat* m) {
   m->has_rhs = 0;
   m->fused = 0;
   m->finished = 0;
+  m->pattern_recorded = 0;
+}
+
+// Marks m->P complete at this point of the context stream.
+static int record_pattern(elfel_sysmat* m) {
+  Ctx* c = &m->h->c;
+  if (!m->ev_pattern) ELFEL_CUDA(c, cudaEventCreateWithFlags(&m->ev_pattern, cudaEventDisableTiming));
+  ELFEL_CUDA(c, cudaEventRecord(m->ev_pattern, c->stream));
+  m->pattern_recorded = 1;
+  return ELFEL_OK;
 }
 
 extern "C" int elfel_sysmat_destroy(elfel_sysmat* m) {
@@ -170,6 +180,7 @@ extern "C" int elfel_sysmat_destroy(elfel_sysmat* m) {
     cudaSetDevice(m->h->c.device);
     release_all(m);
     cudaStreamSynchronize(m->h->c.stream);
+    if (m->ev_pattern) cudaEventDestroy(m->ev_pattern);
   }
   delete stage_of(m);
   delete m;
@@ -245,6 +256,7 @@ extern "C" int elfel_sysmat_finish(elfel_sysmat* m, int64_t* nnz) {
     {
       Phase ph(c, "pattern_coo");
       ELFEL_TRY(build_pattern(c, g, m->nrow, m->ncol, &m->P));
+      ELFEL_TRY(record_pattern(m));
     }
     I.release(c);
     J.release(c);
@@ -282,11 +294,17 @@ extern "C" int elfel_sysmat_csc(elfel_sysmat* m, int64_t* colptr, int64_t* rowva
   if (colptr && rowval && cpd && rvd && pin_c && pin_r) {
     // pinned arrays: the 1-based indices are written straight into them (one
     // block per SM: more blocks writing across the host link run slower;
-    // pageable arrays take the staged copy, which measured faster there)
+    // pageable arrays take the staged copy, which measured faster there).
+    // The indices depend on the pattern only: they go out on the auxiliary
+    // stream from the moment the pattern was complete, alongside the values'
+    // assembly still running on the context stream, whose copy follows it.
+    cudaStream_t s = c->stream;
+    if (m->pattern_recorded) ELFEL_TRY(aux_after(c, m->ev_pattern, &s));
+    csc_out_k<<<(unsigned)c->sm_count, 256, 0, s>>>(m->P.colptr.p, ncol, m->P.rowval.p, nnz, cpd, rvd);
+    ELFEL_LAUNCH_CHECK(c);
     if (nzval && nnz)
       ELFEL_CUDA(c, cudaMemcpyAsync(nzval, m->vals.p, sizeof(double) * nnz, cudaMemcpyDeviceToHost, c->stream));
-    csc_out_k<<<(unsigned)c->sm_count, 256, 0, c->stream>>>(m->P.colptr.p, ncol, m->P.rowval.p, nnz, cpd, rvd);
-    ELFEL_LAUNCH_CHECK(c);
+    if (s != c->stream) ELFEL_TRY(aux_join(c));
     ELFEL_CUDA(c, cudaStreamSynchronize(c->stream));
     return ELFEL_OK;
   }
@@ -553,6 +571,7 @@ int fused_build(elfel_sysmat* m, int64_t ndofs) {
   {
     Phase ph(c, "pattern_K");
     ELFEL_TRY(build_pattern(c, g, ndofs, ndofs, &m->P));
+    ELFEL_TRY(record_pattern(m));
   }
   // right-hand side: a 1 x ndofs "matrix" of the element vectors
   SlotGen& fg = F.fgen;

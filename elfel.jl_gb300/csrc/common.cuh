@@ -103,6 +103,9 @@ int fail(Ctx* c, int code, const char* fmt, ...);
 // c->stream so far (fork); join() makes c->stream wait for it.
 int aux_fork(Ctx* c, cudaStream_t* aux);
 int aux_join(Ctx* c);
+// The auxiliary stream, made to wait only for the event ev (recorded on
+// c->stream earlier); join with aux_join.
+int aux_after(Ctx* c, cudaEvent_t ev, cudaStream_t* aux);
 
 // A device-usable address of a host array: the device address of pinned
 // memory, the host address itself where kernels read pageable memory (ATS),

@@ -253,6 +253,17 @@ int aux_fork(Ctx* c, cudaStream_t* aux) {
   return ELFEL_OK;
 }
 
+int aux_after(Ctx* c, cudaEvent_t ev, cudaStream_t* aux) {
+  if (!c->aux) {
+    ELFEL_CUDA(c, cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking));
+    ELFEL_CUDA(c, cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    ELFEL_CUDA(c, cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+  }
+  ELFEL_CUDA(c, cudaStreamWaitEvent(c->aux, ev, 0));
+  *aux = c->aux;
+  return ELFEL_OK;
+}
+
 int aux_join(Ctx* c) {
   if (!c->aux) return ELFEL_OK;
   ELFEL_CUDA(c, cudaEventRecord(c->ev_join, c->aux));

@@ -347,6 +347,9 @@ struct elfel_sysmat {
   elfel::SolverData* solver = nullptr;
   uint64_t values_version = 0;  // bumped whenever vals change
   int busy = 0;                 // held by a batch slot (its solver data is in use)
+  // recorded on the context stream when P (its colptr and rowval) is complete
+  cudaEvent_t ev_pattern = nullptr;
+  int pattern_recorded = 0;
 };
 
 namespace elfel {

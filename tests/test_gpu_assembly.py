@@ -378,3 +378,52 @@ def test_fused_edge_cases(E, O, gpu):
     F = np.ones(nn)
     am0._hd.check(lib.elfel_sysmat_rhs(h, N_.ptr(F)))
     assert K.shape == (nn, nn) and K.nnz == 0 and (F == 0.0).all()
+
+
+def _csc_pinned(E, hd):
+    """elfel_sysmat_csc into pinned host arrays (1-based colptr, rowval, values)."""
+    import ctypes
+    torch = pytest.importorskip("torch")
+    N_ = E._native
+    nr, nc, nnz = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+    hd.check(hd.lib.elfel_sysmat_dims(hd.h, ctypes.byref(nr), ctypes.byref(nc), ctypes.byref(nnz)))
+    cp = torch.full((nc.value + 1,), -7, dtype=torch.int64).pin_memory()
+    rv = torch.full((max(nnz.value, 1),), -7, dtype=torch.int64).pin_memory()
+    nz = torch.full((max(nnz.value, 1),), np.nan, dtype=torch.float64).pin_memory()
+
+    def p(t, typ):
+        return ctypes.cast(ctypes.c_void_p(t.data_ptr()), typ)
+
+    hd.check(hd.lib.elfel_sysmat_csc(hd.h, p(cp, N_._i64p), p(rv, N_._i64p), p(nz, N_._dp)))
+    k = nnz.value
+    return cp.numpy().copy(), rv.numpy()[:k].copy(), nz.numpy()[:k].copy()
+
+
+def test_csc_pinned_output(E, O, gpu):
+    """CSC output into pinned arrays: the indices are written by a kernel on the
+    auxiliary stream from the moment the pattern is complete, alongside an
+    assembly still running on the context stream; the values are copied after
+    it.  Equal to the staged copy into pageable arrays, right after a fused
+    assembly (first and tile form) and after a COO assembly."""
+    mesh = E.jitter(E.T6block(1.0, 1.0, 90, 70), 0.1 / 90, seed=2)
+    fesp = heat_space(E, mesh, E.FEH1_T6())
+    n = E.ndofs(fesp)
+    kappa = np.exp(np.random.default_rng(1).uniform(np.log(0.5), np.log(2.0), mesh.nel))
+    am = E.start(E.SysmatAssemblerGPU(), n, n)
+    E.assemble_heat(am, E.FEIterator(fesp), E.QPIterator(fesp, {"kind": "default", "npts": 3}), kappa, -6.0)
+    for rep in range(3):
+        if rep:
+            am.heat(None, -6.0)  # not awaited: the pinned output follows it directly
+        cp, rv, nz = _csc_pinned(E, am._hd)
+        K = am.csc()
+        assert np.array_equal(cp, K.indptr + 1) and np.array_equal(rv, K.indices + 1)
+        assert np.array_equal(nz.view(np.int64), K.data.view(np.int64)), rep
+    rng = np.random.default_rng(3)
+    I, J = rng.integers(1, 301, 50000), rng.integers(1, 201, 50000)
+    V = rng.standard_normal(50000)
+    a = E.start(E.SysmatAssemblerSparse(0.0), 300, 200)
+    a._chunks.append((I, J, V))
+    A = E.finish(a)
+    cp, rv, nz = _csc_pinned(E, a._hd)
+    assert np.array_equal(cp, A.indptr + 1) and np.array_equal(rv, A.indices + 1)
+    assert np.array_equal(nz, A.data)
