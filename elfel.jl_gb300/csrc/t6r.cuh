@@ -38,8 +38,22 @@ __device__ __forceinline__ double t6r_scale(double b, int code) {
   return code == 0 ? b : (code == 3 ? 0.0 : scaled);
 }
 
-// Value table of one element for the tile reduction: v[0..6] = b0..b6,
-// v[7] = +0, v[8..10] = -4 b1, -4 b3, -4 b4, v[11..13] = -8 b1, -8 b3, -8 b4.
+// t6r_scale(b, 1) and t6r_scale(b, 2) from one decode of b (the same bits).
+__device__ __forceinline__ void t6r_scale48(double b, double* m4, double* m8) {
+  const long long bits = t6r_xor(__double_as_longlong(b), (long long)(1ull << 63));  // -b
+  const long long sign = bits & (long long)(1ull << 63);
+  const int ex = (int)((bits >> 52) & 0x7ff);
+  const bool zero = ex == 0, special = ex == 0x7ff;
+  const long long inf = sign | 0x7ff0000000000000LL;
+  long long r4 = bits + (2LL << 52), r8 = bits + (3LL << 52);
+  r4 = zero ? sign : (special ? bits : (ex + 2 > 2046 ? inf : r4));
+  r8 = zero ? sign : (special ? bits : (ex + 3 > 2046 ? inf : r8));
+  *m4 = __longlong_as_double(r4);
+  *m8 = __longlong_as_double(r8);
+}
+
+// Value table of one element for the tile reduction, entry j at v[j * ld]:
+// b0..b6, +0, -4 b1, -4 b3, -4 b4, -8 b1, -8 b3, -8 b4.
 constexpr int kT6RTable = 14;
 // Stored K entry k (0..20, column-packed upper triangle) -> its table index.
 constexpr uint8_t kT6REntry[21] = {0, 1, 2, 3, 4, 5, 8, 8, 7, 6, 7, 10, 10, 12, 6, 9, 7, 9, 13, 11, 6};
@@ -49,16 +63,13 @@ __device__ __forceinline__ int t6r_entry(int s) {
   return s < 16 ? (int)((0x96caa76788543210ull >> (4 * s)) & 15u) : (int)((0x6bd97u >> (4 * (s - 16))) & 15u);
 }
 
-__device__ __forceinline__ void t6r_table(const double* b, double* v) {
+__device__ __forceinline__ void t6r_table(const double* b, double* v, int ld = 1) {
 #pragma unroll
-  for (int k = 0; k < 7; ++k) v[k] = b[k];
-  v[7] = 0.0;
-  v[8] = t6r_scale(b[1], 1);
-  v[9] = t6r_scale(b[3], 1);
-  v[10] = t6r_scale(b[4], 1);
-  v[11] = t6r_scale(b[1], 2);
-  v[12] = t6r_scale(b[3], 2);
-  v[13] = t6r_scale(b[4], 2);
+  for (int k = 0; k < 7; ++k) v[k * ld] = b[k];
+  v[7 * ld] = 0.0;
+  t6r_scale48(b[1], v + 8 * ld, v + 11 * ld);
+  t6r_scale48(b[3], v + 9 * ld, v + 12 * ld);
+  t6r_scale48(b[4], v + 10 * ld, v + 13 * ld);
 }
 
 }  // namespace elfel

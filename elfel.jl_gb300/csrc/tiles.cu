@@ -15,18 +15,21 @@
 //     each round of a warp reads consecutive codes.
 // A value table holds V values per element of the tile: the element's K
 // record (V = S), or for the exact-rational T6 heat record the 14 values its
-// 8 bases expand to (t6r_table).  Every nonzero adds its contributions in
+// 8 bases expand to (t6r_table), entry-major (value j of the tile's element
+// k at j * nel + k, so that the threads staging consecutive elements write
+// consecutive words).  Every nonzero adds its contributions in
 // slot order -- the order of the contributor lists of the pattern, which is
 // the order in which SparseArrays.sparse adds duplicates -- so the values are
 // the bits of reduce_values.
 //
 // A program is one contiguous, 16-byte aligned blob (count classes, element
 // offsets, first codes, further codes), copied into shared memory with
-// vector loads at the start of each tile.  Tiles whose programs are equal
-// word for word (the tiles of a structured mesh away from its boundary are
-// translates of a few) share one copy: only distinct programs are kept, and
-// per step a tile reads its own first nonzero and smallest element and the
-// blob of its program, which stays in L2.
+// vector loads (once per tile, or once per run of consecutive tiles of one
+// program in tile_run_k).  Tiles whose programs are equal word for word (the
+// tiles of a structured mesh away from its boundary are translates of a few)
+// share one copy: only distinct programs are kept, and per step a tile reads
+// its own first nonzero and smallest element and the blob of its program,
+// which stays in L2.
 #include <algorithm>
 #include <unordered_map>
 #include <vector>
@@ -236,7 +239,7 @@ __global__ void __launch_bounds__(kTT) tile_build_k(TileHdr* __restrict__ hdr, i
         const int mid = (lo + hi) >> 1;
         if (el[mid] < (int32_t)e) lo = mid + 1; else hi = mid;
       }
-      const uint32_t code = (uint32_t)(lo * a.V + a.map[s]);
+      const uint32_t code = (uint32_t)(a.map[s] * nel + lo);  // entry-major value table
       if (k == 0)
         firsts[si] = ((uint32_t)i << 16) | code;
       else
@@ -322,8 +325,8 @@ __global__ void blob_copy_k(const int64_t* __restrict__ src, const int64_t* __re
 struct RecFull {
   const double* store;
   int S;
-  __device__ __forceinline__ void stage(int64_t e, double* v) const {
-    for (int k = 0; k < S; ++k) v[k] = __ldg(store + e * S + k);
+  __device__ __forceinline__ void stage(int64_t e, double* v, int ld) const {
+    for (int k = 0; k < S; ++k) v[k * ld] = __ldg(store + e * S + k);
   }
   __device__ __forceinline__ double value(uint32_t st) const { return __ldg(store + st); }
 };
@@ -336,25 +339,19 @@ struct RecT6R {
 #pragma unroll
     for (int k = 0; k < 4; ++k) x[k] = __ldg(p + k);
   }
-  __device__ __forceinline__ static void expand(const double2 (&x)[4], double* v) {
+  __device__ __forceinline__ static void expand(const double2 (&x)[4], double* v, int ld) {
     double b[8];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       b[2 * k] = x[k].x;
       b[2 * k + 1] = x[k].y;
     }
-    t6r_table(b, v);
+    t6r_table(b, v, ld);
   }
-  __device__ __forceinline__ void stage(int64_t e, double* v) const {
-    const double2* p = reinterpret_cast<const double2*>(bases + e * 8);
-    double b[8];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const double2 x = __ldg(p + k);
-      b[2 * k] = x.x;
-      b[2 * k + 1] = x.y;
-    }
-    t6r_table(b, v);
+  __device__ __forceinline__ void stage(int64_t e, double* v, int ld) const {
+    double2 x[4];
+    load(e, x);
+    expand(x, v, ld);
   }
   // stored entry st = e * 21 + s of the record
   __device__ __forceinline__ double value(uint32_t st) const {
@@ -430,7 +427,7 @@ __global__ void __launch_bounds__(kRT) tile_reduce_k(const TileHdr* __restrict__
   double* tbl = reinterpret_cast<double*>(reinterpret_cast<uint8_t*>(smq) + maxblob);
   double* out = tbl + (size_t)maxnel * V;
   const int32_t* gel = reinterpret_cast<const int32_t*>(blob + H.boff + L.el);
-  for (int k = threadIdx.x; k < H.nel; k += kRT) rec.stage((int64_t)H.emin + __ldg(gel + k), tbl + k * V);
+  for (int k = threadIdx.x; k < H.nel; k += kRT) rec.stage((int64_t)H.emin + __ldg(gel + k), tbl + k, H.nel);
   __syncthreads();
   tile_adds(sb, L, H.nz, tbl, out);
   __syncthreads();
@@ -488,7 +485,7 @@ __global__ void __launch_bounds__(kRT) tile_run_k(const TileHdr* __restrict__ hd
 #pragma unroll
     for (int p = 0; p < P; ++p) {
       const int k = threadIdx.x + p * kRT;
-      if (k < nel) RecT6R::expand(x[p], tbl + k * kT6RTable);
+      if (k < nel) RecT6R::expand(x[p], tbl + k, nel);
     }
     int64_t pn = 0;
     if (t + 1 < run.y) {
