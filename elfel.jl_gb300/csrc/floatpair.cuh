@@ -99,10 +99,18 @@ __device__ __forceinline__ int dexp(double x) { return (int)((__double_as_longlo
 // pattern 0x4b000000 | i, and subtracting 2^23 from it is exact.  Returns
 // false (and zero) when x * 2^-k is outside [2^-68, 2^127] in magnitude and
 // not zero.
+// The zero test masks the sign with an explicit integer and.b64: written in
+// C++ it is recognised as the comparison x == 0.0 and issued on the FP64 pipe.
+__device__ __forceinline__ long long and_b64(long long a, long long m) {
+  long long r;
+  asm("and.b64 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(m));
+  return r;
+}
+
 __device__ __forceinline__ bool split_scaled(double x, int k, f2* out) {
   const long long b = __double_as_longlong(x);
   *out = {0.0f, 0.0f};
-  if ((b & 0x7fffffffffffffffLL) == 0) return true;
+  if (and_b64(b, 0x7fffffffffffffffLL) == 0) return true;
   const int ex = (int)((b >> 52) & 0x7ff) - k;  // biased exponent of x * 2^-k
   if (ex < 955 || ex > 1150) return false;
   const unsigned sign = (unsigned)((unsigned long long)b >> 63) << 31;

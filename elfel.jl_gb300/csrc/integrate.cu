@@ -549,7 +549,7 @@ __global__ void __launch_bounds__(kIntThreads) heat_t6s_k(int64_t nel, const int
   extern __shared__ double acc[];  // (NS + NN) * LD
   __shared__ int32_t sconn[NT * NN];
   __shared__ double sS[3][NS];
-  stage_tensors<NN, NT>(tab, sS);
+  if (PAT != kPatT6R) stage_tensors<NN, NT>(tab, sS);  // the exact-rational form needs no tensors
   const int64_t e0 = (int64_t)blockIdx.x * NT;
   const int64_t base = e0 * NN, lim = nel * NN;
   for (int k = threadIdx.x; k < NT * NN; k += NT) {
@@ -571,6 +571,20 @@ __global__ void __launch_bounds__(kIntThreads) heat_t6s_k(int64_t nel, const int
                 Q, tab.P[3], bs);
     }
     double* a = acc + t;
+    if (BASES && FDIRECT) {
+      // each element's 8 bases straight from registers into its 64-byte
+      // record (no shared memory), the load vector added in place
+      if (e < nel) {
+        double2* o = reinterpret_cast<double2*>(kstore + e * 8);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) o[k] = make_double2(bs[2 * k], bs[2 * k + 1]);
+        const int32_t* d = dofs + e * NN;
+        atomicAdd(fglob + __ldg(d + 3), bs[7]);
+        atomicAdd(fglob + __ldg(d + 4), bs[7]);
+        atomicAdd(fglob + __ldg(d + 5), bs[7]);
+      }
+      return;
+    }
     if (BASES) {
       if (e < nel) {
 #pragma unroll
@@ -698,7 +712,7 @@ int launch_heat_bases(Ctx* c, int64_t nel, const int32_t* conn, const double* xy
   const size_t sm = 11 * (kIntThreads + 1) * sizeof(double);
   if (fglob) {
     if (!dofs) return fail(c, ELFEL_ERR_STATE, "heat: direct load-vector assembly needs the DOF table");
-    heat_t6s_k<kPatT6R, true, true><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, (const double2*)xy, kappa, Q,
+    heat_t6s_k<kPatT6R, true, true><<<grid, kIntThreads, 0, c->stream>>>(nel, conn, (const double2*)xy, kappa, Q,
                                                                            tab, bases, fstore, dofs, fglob);
   } else {
     heat_t6s_k<kPatT6R, false, true><<<grid, kIntThreads, sm, c->stream>>>(nel, conn, (const double2*)xy, kappa, Q,
