@@ -364,13 +364,13 @@ struct RecT6R {
   }
 };
 
-constexpr int kRT = 64;                  // threads of tile_reduce_k and tile_run_k
+constexpr int kRT = 64;                  // threads of tile_reduce_k
 constexpr int kTileRun = 4;              // tiles per run of tile_run_k
-constexpr int kRPer = kTileMaxNz / kRT;  // nonzeros per thread
 
 // Adds of one tile: one thread per nonzero in count order (the program's
 // first codes), each summing its contributions in slot order from the value
 // table, the sums placed in CSC order in out.
+template <int RT>
 __device__ __forceinline__ void tile_adds(const uint8_t* sb, const BlobLayout& L, int nz, const double* tbl,
                                           double* out) {
   const uint16_t* cstart = reinterpret_cast<const uint16_t*>(sb);
@@ -378,8 +378,8 @@ __device__ __forceinline__ void tile_adds(const uint8_t* sb, const BlobLayout& L
   const uint16_t* sr = reinterpret_cast<const uint16_t*>(sb + L.r);
   int c = 1, rb = 0;  // class of the current nonzero and the start of its class's further codes
 #pragma unroll
-  for (int j = 0; j < kRPer; ++j) {
-    const int i = threadIdx.x + j * kRT;
+  for (int j = 0; j < kTileMaxNz / RT; ++j) {
+    const int i = threadIdx.x + j * RT;
     if (i < nz) {
       while (i >= cstart[c + 1]) {
         rb += (cstart[c + 1] - cstart[c]) * (c - 1);
@@ -429,24 +429,27 @@ __global__ void __launch_bounds__(kRT) tile_reduce_k(const TileHdr* __restrict__
   const int32_t* gel = reinterpret_cast<const int32_t*>(blob + H.boff + L.el);
   for (int k = threadIdx.x; k < H.nel; k += kRT) rec.stage((int64_t)H.emin + __ldg(gel + k), tbl + k, H.nel);
   __syncthreads();
-  tile_adds(sb, L, H.nz, tbl, out);
+  tile_adds<kRT>(sb, L, H.nz, tbl, out);
   __syncthreads();
   for (int i = threadIdx.x; i < H.nz; i += kRT) vals[H.p0 + i] = out[i];
 }
 
-// One CTA per run of consecutive tiles that read the same program (T6 bases).
-// The program is copied into shared memory once per run; a thread's elements
-// (positions in the program's element list) are the same in every tile of the
-// run, so the 8 bases of the next tile's elements are loaded into registers
-// before the current tile's adds and expanded into the value table after
-// them: the gather of tile t + 1 overlaps the adds of tile t. P elements per
-// thread (the run kernel is used when the largest tile has at most P * 64).
-template <int P>
-__global__ void __launch_bounds__(kRT) tile_run_k(const TileHdr* __restrict__ hdr, const int2* __restrict__ runs,
-                                                  int maxnel, int maxblob, const uint8_t* __restrict__ blob,
-                                                  const int32_t* __restrict__ cptr,
-                                                  const int32_t* __restrict__ contrib, RecT6R rec,
-                                                  double* __restrict__ vals) {
+// One CTA of kRunThreads per run of consecutive tiles that read the same
+// program (T6 bases).  The program is copied into shared memory once per run;
+// a thread's element (its position in the program's element list, at most
+// one per thread) is the same in every tile of the run, so the 8 bases of the
+// next tile's element are loaded into registers before the current tile's
+// adds and expanded into the value table after them: the gather of tile t + 1
+// overlaps the adds of tile t.
+constexpr int kRunThreads = 128;
+
+__global__ void __launch_bounds__(kRunThreads) tile_run_k(const TileHdr* __restrict__ hdr,
+                                                          const int2* __restrict__ runs, int maxnel, int maxblob,
+                                                          const uint8_t* __restrict__ blob,
+                                                          const int32_t* __restrict__ cptr,
+                                                          const int32_t* __restrict__ contrib, RecT6R rec,
+                                                          double* __restrict__ vals) {
+  constexpr int RT = kRunThreads;
   extern __shared__ uint4 smq[];  // program (maxblob bytes) | value table | values
   const int2 run = runs[blockIdx.x];
   const TileHdr H0 = hdr[run.x];
@@ -455,7 +458,7 @@ __global__ void __launch_bounds__(kRT) tile_run_k(const TileHdr* __restrict__ hd
     for (int t = run.x; t < run.x + run.y; ++t) {
       const TileHdr H = hdr[t];
       if (H.flags & kTileEmpty) continue;
-      for (int i = threadIdx.x; i < H.nz; i += kRT) {
+      for (int i = threadIdx.x; i < H.nz; i += RT) {
         const int32_t b = cptr[H.p0 + i], e = cptr[H.p0 + i + 1];
         double s = rec.value((uint32_t)contrib[b]);
         for (int32_t k = b + 1; k < e; ++k) s = __dadd_rn(s, rec.value((uint32_t)contrib[k]));
@@ -466,40 +469,28 @@ __global__ void __launch_bounds__(kRT) tile_run_k(const TileHdr* __restrict__ hd
   }
   const BlobLayout L = blob_layout(H0.nel, H0.nz, H0.nc);
   const int nel = H0.nel, nz = H0.nz;
-  const int32_t* gel = reinterpret_cast<const int32_t*>(blob + H0.boff + L.el);
-  int eo[P];
-  double2 x[P][4];
-#pragma unroll
-  for (int p = 0; p < P; ++p) {
-    const int k = threadIdx.x + p * kRT;
-    eo[p] = k < nel ? __ldg(gel + k) : 0;
-    if (k < nel) rec.load((int64_t)H0.emin + eo[p], x[p]);
-  }
+  const bool mine = (int)threadIdx.x < nel;  // the thread stages element threadIdx.x of each tile
+  const int32_t eo = mine ? __ldg(reinterpret_cast<const int32_t*>(blob + H0.boff + L.el) + threadIdx.x) : 0;
+  double2 x[4];
+  if (mine) rec.load((int64_t)H0.emin + eo, x);
   const uint4* src = reinterpret_cast<const uint4*>(blob + H0.boff);
-  for (int k = threadIdx.x; k < L.bytes / 16; k += kRT) smq[k] = __ldg(src + k);
+  for (int k = threadIdx.x; k < L.bytes / 16; k += RT) smq[k] = __ldg(src + k);
   const uint8_t* sb = reinterpret_cast<const uint8_t*>(smq);
   double* tbl = reinterpret_cast<double*>(reinterpret_cast<uint8_t*>(smq) + maxblob);
   double* out = tbl + (size_t)maxnel * kT6RTable;
   int64_t p0 = H0.p0;
   for (int t = 0; t < run.y; ++t) {
-#pragma unroll
-    for (int p = 0; p < P; ++p) {
-      const int k = threadIdx.x + p * kRT;
-      if (k < nel) RecT6R::expand(x[p], tbl + k, nel);
-    }
+    if (mine) RecT6R::expand(x, tbl + threadIdx.x, nel);
     int64_t pn = 0;
     if (t + 1 < run.y) {
       const TileHdr* hn = hdr + run.x + t + 1;
       pn = hn->p0;
-      const int64_t en = hn->emin;
-#pragma unroll
-      for (int p = 0; p < P; ++p)
-        if (threadIdx.x + p * kRT < nel) rec.load(en + eo[p], x[p]);
+      if (mine) rec.load((int64_t)hn->emin + eo, x);
     }
     __syncthreads();  // the program and the table are in place; out is free
-    tile_adds(sb, L, nz, tbl, out);
+    tile_adds<RT>(sb, L, nz, tbl, out);
     __syncthreads();  // out is complete; the table is free
-    for (int i = threadIdx.x; i < nz; i += kRT) vals[p0 + i] = out[i];
+    for (int i = threadIdx.x; i < nz; i += RT) vals[p0 + i] = out[i];
     p0 = pn;
   }
 }
@@ -722,26 +713,22 @@ static size_t tile_smem(const TilePlan& T) {
   return (size_t)T.maxblob + (size_t)T.maxnel * T.V * sizeof(double) + kTileMaxNz * sizeof(double);
 }
 
-static bool tile_runs_ok(const TilePlan& T) { return T.nruns > 0 && T.maxnel <= 2 * kRT && T.V == kT6RTable; }
+static bool tile_runs_ok(const TilePlan& T) {
+  return T.nruns > 0 && T.maxnel <= kRunThreads && T.V == kT6RTable && T.S == 21;
+}
 
 // Runs [r0, r0 + nr) of the plan's run kernel on stream s (T6 bases).
 static int tile_reduce_runs(Ctx* c, const Pattern& P, const double* bases, double* vals, int64_t r0, int64_t nr,
                             cudaStream_t s) {
   const TilePlan& T = P.tiles;
-  if (!T.built || !tile_runs_ok(T) || T.S != 21) return fail(c, ELFEL_ERR_STATE, "tile runs without a T6 run plan");
+  if (!T.built || !tile_runs_ok(T)) return fail(c, ELFEL_ERR_STATE, "tile runs without a T6 run plan");
   if (r0 < 0 || nr < 0 || r0 + nr > T.nruns) return fail(c, ELFEL_ERR_ARG, "tile runs outside the plan");
   if (nr == 0) return ELFEL_OK;
   const size_t sm = tile_smem(T);
   RecT6R r{bases};
-  if (T.maxnel <= kRT) {
-    ELFEL_CUDA(c, cudaFuncSetAttribute(tile_run_k<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    tile_run_k<1><<<(unsigned)nr, kRT, sm, s>>>(T.hdr.p, T.runs.p + r0, T.maxnel, T.maxblob, T.blob.p, P.cptr.p,
-                                                P.contrib.p, r, vals);
-  } else {
-    ELFEL_CUDA(c, cudaFuncSetAttribute(tile_run_k<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    tile_run_k<2><<<(unsigned)nr, kRT, sm, s>>>(T.hdr.p, T.runs.p + r0, T.maxnel, T.maxblob, T.blob.p, P.cptr.p,
-                                                P.contrib.p, r, vals);
-  }
+  ELFEL_CUDA(c, cudaFuncSetAttribute(tile_run_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  tile_run_k<<<(unsigned)nr, kRunThreads, sm, s>>>(T.hdr.p, T.runs.p + r0, T.maxnel, T.maxblob, T.blob.p, P.cptr.p,
+                                                   P.contrib.p, r, vals);
   ELFEL_LAUNCH_CHECK(c);
   return ELFEL_OK;
 }
