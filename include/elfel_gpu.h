@@ -119,8 +119,7 @@ ELFEL_API int elfel_sysvec_assemble(elfel_ctx* ctx, int64_t nrow, const int64_t*
  *   - sizes are limited to ELFEL_NOALLOC_MAX_ROWS rows and
  *     ELFEL_NOALLOC_MAX_ENTRIES entries; larger calls return ELFEL_ERR_ARG;
  *   - the first call on a device looks up the array's device address (once,
- *     with that device current); make that first call before any stream
- *     capture;
+ *     with that device current);
  *   - every call reuses the same array, which keeps the previous call's
  *     contents; calls whose work overlaps on the GPU (other streams, other
  *     contexts on the same device) race on it.
