@@ -710,6 +710,21 @@ def main():
             st32, T32 = res["pcg32_ir"]
             pcg["speedup"] = st64["seconds"] / st32["seconds"]
             pcg["fp32_vs_fp64_rel_err_max"] = float(np.abs(T32[:nu] - T64[:nu]).max() / np.abs(T64[:nu]).max())
+        # per-iteration roofline: algorithmic bytes of one iteration on the free-free block
+        # (FP64: values 8 + column index 4 per nonzero, row pointer 4 and ~10 vector
+        # accesses of 8 per unknown; FP32 inner iteration: 4 + 4 per nonzero, ~10 vector
+        # accesses of 4 per unknown) x iterations / solve time
+        cp1 = colptr_h.numpy()
+        rv1 = rowval_h.numpy()[: int(cp1[nu]) - 1]
+        nnz_ff = int(np.count_nonzero(rv1 <= nu))
+        per_it = {"fp64": nnz_ff * 12 + nu * 4 + 10 * nu * 8, "fp32_ir": nnz_ff * 8 + 10 * nu * 4}
+        pcg["roofline"] = {"nnz_ff": nnz_ff, "nu": nu, "peak": hbm, "unit": "GB/s",
+                           "what": "iterations x algorithmic bytes per iteration / solve time (FP32: the inner "
+                                   "iterations; the FP64 residual replacements are not counted)"}
+        for key in ("fp64", "fp32_ir"):
+            if key in pcg:
+                gbs = pcg[key]["iterations"] * per_it[key] / pcg[key]["seconds"] / 1e9
+                pcg["roofline"][key] = {"bytes_per_iteration": per_it[key], "achieved": gbs, "frac": gbs / hbm}
         if "pcg32_ir" in res:
             # the batched form with this one system: per-tile kernels, device-side replacement
             b = E.BatchSolver("pcg32_ir", capacity=1, ctx=ctx)
