@@ -365,7 +365,7 @@ struct RecT6R {
 };
 
 constexpr int kRT = 64;                  // threads of tile_reduce_k
-constexpr int kTileRun = 4;              // tiles per run of tile_run_k
+constexpr int kTileRun = 6;              // tiles per run of tile_run_k
 
 // Adds of one tile: one thread per nonzero in count order (the program's
 // first codes), each summing its contributions in slot order from the value
