@@ -4,9 +4,11 @@ The 2M-element T6 heat system that bench.py times (1000 x 1000 cells, jittered
 vertices, conductivity log-uniform in [0.5, 2] per element, Q = -6) is
 assembled on the device and by the oracle (element loop, COO triplets,
 SparseArrays.sparse semantics, test/test_heat.jl:35-71); the plane-strain
-elasticity and Taylor-Hood cavity systems are compared at 200 x 100 and
-100 x 100 cells.  Bars: pattern bit-exact, values within 1e-12 of the largest
-entry (relative), as in the small-mesh parity tests.
+elasticity system at 1000 x 500 cells (1M vector T6 elements, 4,006,002
+DOFs) and the Taylor-Hood cavity at 600 x 600 cells (720,000 elements,
+3,246,003 DOFs) are compared at their benchmark sizes too.  Bars: pattern
+bit-exact, values within 1e-12 of the largest entry (relative), as in the
+small-mesh parity tests.
 
 The FP32-refinement solution of the 2M-element system (FP32 CG with FP64
 residual replacement, stopped at relative residual 1e-10) is compared with a
@@ -85,8 +87,8 @@ def test_c1_fp32_refinement_error(E, c1):
 
 
 def test_c2_elasticity_parity(E, O, gpu):
-    """Plane-strain T6 elasticity on [0,2]x[0,1] with 200 x 100 cells."""
-    mesh, fesp, bforce, right = elasticity_setup(E, 200, 100)
+    """Plane-strain T6 elasticity on [0,2]x[0,1] with 1000 x 500 cells."""
+    mesh, fesp, bforce, right = elasticity_setup(E, 1000, 500)
     n = E.ndofs(fesp)
     elit = E.FEIterator(fesp)
     am = E.start(E.SysmatAssemblerGPU(gpu), n, n)
@@ -96,18 +98,20 @@ def test_c2_elasticity_parity(E, O, gpu):
     ed = elit.eldofs_table() - 1
     K0 = O.sparse(*O.local_coo(ed, ed, ke), n, n)
     F0 = O.vec_assemble(n, ed, fe) + traction_oracle(mesh, ed, right, (1.0, 0.0), n)
-    assert K0.nnz == 368 * 100 ** 2 + 96 * 100 + 4
+    assert mesh.nel == 1_000_000 and n == 4_006_002
+    assert K0.nnz == 368 * 500 ** 2 + 96 * 500 + 4
     assert _same_pattern(K, K0)
     assert _close(K.data, K0.data) and _close(F, F0)
 
 
 def test_c3_stokes_cavity_parity(E, O, gpu):
-    """Taylor-Hood lid-driven cavity with 100 x 100 cells."""
-    vmesh, pmesh, ufesp, pfesp = stokes_setup(E, 100, lid=True)
+    """Taylor-Hood lid-driven cavity with 600 x 600 cells."""
+    vmesh, pmesh, ufesp, pfesp = stokes_setup(E, 600, lid=True)
     K0, n = stokes_oracle_K(E, O, vmesh, ufesp, pfesp)
     am = E.start(E.SysmatAssemblerGPU(gpu), n, n)
     E.assemble_stokes(am, E.FEIterator(ufesp), E.FEIterator(pfesp), E.QPIterator(ufesp, {"npts": 3}), 1.0)
     K = E.finish(am)
-    assert K0.nnz == 260 * 100 ** 2 + 104 * 100 + 8
+    assert vmesh.nel == 720_000 and n == 3_246_003
+    assert K0.nnz == 260 * 600 ** 2 + 104 * 600 + 8
     assert _same_pattern(K, K0)
     assert _close(K.data, K0.data)
