@@ -15,9 +15,12 @@ reduction into the device CSC built once).  The JSON line reports
           assembly, download of the CSC and F, every step;
   pcg     the solve of the same system to relative residual 1e-10 with
           FP64 Jacobi-PCG and with FP32 CG + FP64 residual replacement
-          (one system, and the same in the batched engine);
+          (one system, and the same in the batched engine), with the
+          per-iteration roofline of both;
   serve   the serving stream: capacity, p50/p99 latency at three arrival
           rates, batched vs plain FP64 one request at a time;
+  configs plane-strain T6 elasticity 1000 x 500 and the Taylor-Hood cavity
+          600 x 600: assembly rate and both solver forms;
   roofline the dominant kernel's algorithmic bytes over its CUDA-event time
           against the measured HBM copy peak, with its measured DRAM traffic;
   cpu_baseline the CPU restatement of the reference path on the host cores;
@@ -197,15 +200,23 @@ def build_shape_problem(E, kind, N, seed=20261203, jit=0.2):
 def problem_bench(E, ctx, args):
     """Elasticity (plane strain T6), Stokes (Taylor-Hood cavity) or heat on
     Q4 / T4 meshes at scale: fused assembly rate, and the FP64 vs
-    FP32-refinement solves."""
+    FP32-refinement solves (one JSON line)."""
+    out = problem_run(E, ctx, args.problem, args.n, args.steps, args.warmup, not args.no_pcg)
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def problem_run(E, ctx, problem, n_cells, steps, warmup, solves):
+    """The measurements of problem_bench as a dict: assembly (steps timed
+    after warmup, L2 flushed between) and, with solves, both solver forms."""
     import torch
 
     stream = torch.cuda.ExternalStream(ctx.stream())
     t0 = time.perf_counter()
     alg = None
-    if args.problem in ("heat-q4", "heat-t4"):
-        kind = "Q4" if args.problem == "heat-q4" else "T4"
-        N = args.n or (1414 if kind == "Q4" else 70)
+    if problem in ("heat-q4", "heat-t4"):
+        kind = "Q4" if problem == "heat-q4" else "T4"
+        N = n_cells or (1414 if kind == "Q4" else 70)
         mesh, fesp, kappa = build_shape_problem(E, kind, N)
         n, nu = E.ndofs(fesp), E.nunknowns(fesp)
         qs = {"kind": "Gauss", "order": 2} if kind == "Q4" else {"npts": 1}
@@ -220,8 +231,8 @@ def problem_bench(E, ctx, args):
         work = (f"heat {kind} {'x'.join([str(N)] * (2 if kind == 'Q4' else 3))} ({mesh.nel} elements, {n} DOFs), "
                 f"{'2x2 Gauss' if kind == 'Q4' else '1-point rule'}, fused K+F assembly, pattern reused")
         spaces = fesp
-    elif args.problem == "elasticity":
-        nx = args.n or 1000
+    elif problem == "elasticity":
+        nx = n_cells or 1000
         mesh, fesp, bforce, right = build_elasticity(E, nx, nx // 2)
         n, nu = E.ndofs(fesp), E.nunknowns(fesp)
         elit, qpit = E.FEIterator(fesp), E.QPIterator(fesp, {"npts": 3})
@@ -231,7 +242,7 @@ def problem_bench(E, ctx, args):
         work = f"plane-strain elasticity T6 {nx}x{nx // 2} on [0,2]x[0,1] ({mesh.nel} elements, {n} DOFs)"
         spaces = fesp
     else:
-        N = args.n or 600
+        N = n_cells or 600
         vmesh, pmesh, ufesp, pfesp = build_cavity(E, N)
         n = E.ndofs(ufesp) + E.ndofs(pfesp)
         nu = E.nunknowns(ufesp) + E.nunknowns(pfesp)
@@ -247,13 +258,13 @@ def problem_bench(E, ctx, args):
     ctx.synchronize()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             flush.zero_()
             step()
         torch.cuda.synchronize()
         ctx.profile(True)
         evs = []
-        for _ in range(args.steps):
+        for _ in range(steps):
             flush.zero_()  # L2 (129 MB) flushed between timed steps
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
@@ -263,7 +274,7 @@ def problem_bench(E, ctx, args):
         torch.cuda.synchronize()
         phases = ctx.phases()
         ctx.profile(False)
-    t_asm = sum(a.elapsed_time(b) for a, b in evs) / 1e3 / args.steps
+    t_asm = sum(a.elapsed_time(b) for a, b in evs) / 1e3 / steps
     per = {k: (ms / cnt if cnt else 0.0) for k, (ms, cnt) in phases.items()}
     kernels = {k: {"ms_per_launch": v, "share": v / sum(per.values())} for k, v in per.items()}
     if alg:
@@ -272,10 +283,10 @@ def problem_bench(E, ctx, args):
             if per.get(k):
                 kernels[k].update({"alg_bytes": b, "gbs": b / (per[k] * 1e-3) / 1e9,
                                    "frac": b / (per[k] * 1e-3) / 1e9 / hbm, "peak": hbm, "peak_kind": peak_kind})
-    out = {"problem": args.problem, "workload": work, "elements": mesh.nel, "ndofs": n, "nunknowns": nu,
+    out = {"problem": problem, "workload": work, "elements": mesh.nel, "ndofs": n, "nunknowns": nu,
            "assembly_elements_per_s": mesh.nel / t_asm, "assembly_ms": t_asm * 1e3, "host_setup_s": host_s,
            "kernels": kernels, "l2": "256 MB buffer written between timed steps", "data": "synthetic (seeded)"}
-    if not args.no_pcg:
+    if solves:
         U0 = np.zeros(n)
         E.gathersysvec(U0, spaces)
         sols = {}
@@ -286,9 +297,8 @@ def problem_bench(E, ctx, args):
         (s64, U64), (s32, U32) = sols[methods[0]], sols[methods[1]]
         out.update({"rtol": rtol, methods[0]: s64, methods[1]: s32, "speedup": s64["seconds"] / s32["seconds"],
                     "fp32_vs_fp64_rel_err_max": float(np.abs(U32[:nu] - U64[:nu]).max() / np.abs(U64[:nu]).max())})
-    print(json.dumps(out), flush=True)
     del am
-    return 0
+    return out
 
 
 def read_peaks():
@@ -474,6 +484,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=2, help="full-size CPU reference steps of the cpu_baseline")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the elasticity 1000x500 and Stokes 600x600 legs (assembly and both solves)")
     ap.add_argument("--serve-requests", type=int, default=4096, help="requests of the serving stream")
     ap.add_argument("--serve-rates", default="0.5,0.7,0.9", help="arrival rates as fractions of the capacity")
     ap.add_argument("--serve-rate-sample", type=int, default=1024,
@@ -746,6 +758,13 @@ def main():
         serve = serve_bench(E, ctx, args.serve_requests, fr, args.serve_rate_sample)
         serve["tuning"] = [t for t, _ in ctx.tuning()]
 
+    # --- the other configurations: plane-strain elasticity 1000 x 500 and the
+    # Taylor-Hood cavity 600 x 600 (assembly, FP64 and FP32-refinement solves)
+    configs = None
+    if not args.no_configs and rank == 0:
+        configs = {prob: problem_run(E, ctx, prob, ncell, 5, 3, not args.no_pcg)
+                   for prob, ncell in (("elasticity", 1000), ("stokes", 600))}
+
     # --- CPU baseline (oracle restatement on the host cores) --------------
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -762,7 +781,7 @@ def main():
            "dtype": "f64", "data": "synthetic (seeded T6 mesh, jitter 0.2h, kappa log-uniform [0.5,2])",
            "config": heat_config(N, ws),
            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": (2 if f_direct else 3) * args.steps, "clocks": clk,
-           "pcg": pcg, "serve": serve, "fma_rates": rates, "pattern_build_s": pattern_s, "setup_phases_ms": {k: v[0] for k, v in setup_phases.items()},
+           "pcg": pcg, "serve": serve, "configs": configs, "fma_rates": rates, "pattern_build_s": pattern_s, "setup_phases_ms": {k: v[0] for k, v in setup_phases.items()},
            "wall_s_timed": wall, "host_mesh_setup_s": host_setup_s}
     if rank == 0:
         print(json.dumps(out), flush=True)
