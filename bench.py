@@ -626,11 +626,11 @@ def main():
     # DRAM traffic of one launch of each kernel (dram__bytes_read.sum + dram__bytes_write.sum)
     # measured with ncu on the 700 x 700 case of this workload (980,000 elements), scaled by
     # the element count; writes still dirty in L2 when a kernel ends are not counted.
-    # Tile path: heat_t6s_k<2, 1, 1> 86.53 + 28.88 MB, tile_run_k 66.04 + 126.17 MB.
+    # Tile path: heat_t6_bases_k 86.67 + 28.99 MB, tile_run_k 66.04 + 126.17 MB.
     # Contributor-list path: heat_t6s_k<2, 1> 86.84 + 121.46 MB (<2, 0> 47.34 + 151.06 MB),
     # reduce_win_k 426.95 + 155.19 MB, reduce_row0_dense_k 94.18 + 8.28 MB.
     if tiles:
-        TRAFFIC_PER_ELEMENT = {"integrate_heat": (86.528512e6 + 28.880640e6) / 980000,
+        TRAFFIC_PER_ELEMENT = {"integrate_heat": (86.668288e6 + 28.988672e6) / 980000,
                                "reduce_K": (66.036480e6 + 126.165248e6) / 980000}
     else:
         TRAFFIC_PER_ELEMENT = {"integrate_heat": ((86.844672e6 + 121.461504e6) if f_direct else
