@@ -26,6 +26,10 @@ reduction into the device CSC built once).  The JSON line reports
   cpu_baseline the CPU restatement of the reference path on the host cores;
   clocks  SM clocks and throttle reasons sampled during the timed region.
 
+At N > 1 (torchrun, one rank per GPU) each rank assembles its own replica
+and the line reports the sum; the pcg, serve and configs legs and the CPU
+baseline run at N = 1 only.
+
 ``--impl reference`` times the CPU restatement of the reference path (the
 oracle: element loop, COO triplets, SparseArrays.sparse semantics) on the
 host cores instead.
@@ -702,9 +706,14 @@ def main():
            "what": "C-ABI fused_setup (H2D mesh+eldofs, device pattern build) + fused_heat (H2D kappa) + CSC/F D2H"}
     assert int(colptr_h[-1]) == nnz_dev + 1  # pattern size of the uniform T6 block
 
+    # The solver, serving and configuration legs and the CPU baseline are
+    # single-GPU measurements: they run at N = 1 only (N > 1 times the
+    # assembly replicas alone).
+    single = ws == 1
+
     # --- PCG: FP64 vs FP32 + FP64 refinement, to 1e-10 ---------------------
     pcg = None
-    if not args.no_pcg:
+    if not args.no_pcg and single:
         T0 = np.zeros(n)
         E.gathersysvec(T0, fesp)
         res = {}
@@ -753,7 +762,7 @@ def main():
 
     # --- serving stream: p50/p99 at three arrival rates ------------------
     serve = None
-    if not args.no_serve and rank == 0:
+    if not args.no_serve and single:
         fr = [float(x) for x in args.serve_rates.split(",") if x]
         serve = serve_bench(E, ctx, args.serve_requests, fr, args.serve_rate_sample)
         serve["tuning"] = [t for t, _ in ctx.tuning()]
@@ -761,13 +770,13 @@ def main():
     # --- the other configurations: plane-strain elasticity 1000 x 500 and the
     # Taylor-Hood cavity 600 x 600 (assembly, FP64 and FP32-refinement solves)
     configs = None
-    if not args.no_configs and rank == 0:
+    if not args.no_configs and single:
         configs = {prob: problem_run(E, ctx, prob, ncell, 5, 3, not args.no_pcg)
                    for prob, ncell in (("elasticity", 1000), ("stokes", 600))}
 
     # --- CPU baseline (oracle restatement on the host cores) --------------
     cpu = None
-    if rank == 0 and not args.no_cpu:
+    if single and not args.no_cpu:
         O = entry.oracle()
         threads = os.cpu_count() or 1
         rate, tper, reps = cpu_reference_rate(O, mesh, fesp, kappa, E, threads, args.cpu_steps)
